@@ -1,0 +1,389 @@
+"""cdlgb -- GB300-native convolutional-dictionary-learning hot path of CDLmotif.jl.
+
+Host-side mirror of the reference's Julia interface for the hot path.  Every
+compute call goes through the C ABI of ``libcdlgb.so`` (include/cdlgb.h); there is
+no CPU fallback.  Names follow the reference (a trailing ``!`` becomes nothing):
+
+=====================  =========================================================
+this module            reference (kchu25/CDLmotif.jl)
+=====================  =========================================================
+CDLSetup               CDL_setup          src/SETUP/WRAPPER_setup.jl:1-13
+init_cdl -> CDL        init_cdl / cdl     src/SETUP/CDL_setup.jl:165-283
+code_update            code_update!       src/CDL/train.jl:1-44
+dict_update            dict_update!       src/CDL/train.jl:46-89
+update_best            update_best!       src/CDL/train.jl:91-98
+objective              objective          src/SETUP/CDL_setup.jl:286
+cdl_train              one training of cdl_optimize   src/WRAPPER/wrap.jl:5-12
+scan_w_gpu             scan_w_gpu!        src/SEARCH/scan.jl:176-221
+overlapping_scan       overlapping_scan!  src/SEARCH/scan.jl:89-121
+posdicts2pfms          posdicts2pfms      src/SEARCH/helpers.jl:59-96
+pfm2pwm                pfm2pwm            src/SEARCH/helpers.jl:12-13
+save_pfms_as_transfac  save_pfms_as_transfac  src/SAVE/save_learned_results.jl:184-217
+=====================  =========================================================
+
+Array layouts: a Julia column-major array of dims (a, b, c) is a C-order numpy
+array of shape (c, b, a) -- e.g. the one-hot data (4L, N) is numpy (N, 4L), X is
+numpy (N, M, Lg), D is numpy (M, Lg), pwms (K, 4, maxlen) is numpy (maxlen, 4, K).
+
+Errors raise ``CDLGBError`` (never ValueError/ArgumentError-like types: the
+reference's retry loop, src/WRAPPER/wrap.jl:141, treats ArgumentError as "no motif
+found, relax and retry").
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from . import synth
+from ._lib import CdlgbParams, ptr
+
+__all__ = ["CDLSetup", "CDL", "CDLGBError", "init_cdl", "code_update", "dict_update",
+           "update_best", "objective", "cdl_train", "scan_w_gpu", "overlapping_scan",
+           "posdicts2pfms", "count_matrices", "pfm2pwm", "pwm_complement",
+           "save_pfms_as_transfac", "transfac_text", "FIELDS", "build"]
+
+FIELDS = {"X": 0, "X_best": 1, "d": 2, "D_best": 3, "G1": 4, "G3": 5, "DX": 6, "Y1": 7,
+          "y2": 8, "y3": 9, "g1": 10, "g3": 11, "Td": 12, "G2": 13, "g2": 14, "y1": 15}
+_LMN = {"X", "X_best", "d", "y2", "y3", "g1", "g3"}
+_LN = {"DX", "Y1", "Td", "G2", "g2", "y1"}
+_LM = {"D_best", "G1", "G3"}
+
+
+class CDLGBError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"cdlgb {_lib.STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def build(verbose: bool = False) -> str:
+    from . import buildlib as _b
+    return _b.build(verbose=verbose)
+
+
+@dataclass
+class CDLSetup:
+    """CDL_setup (src/SETUP/WRAPPER_setup.jl:1-13), same defaults."""
+    M: int = 10
+    filter_size: int = 4
+    rho: float = 100.0
+    sigma: float = 100.0
+    lambda_: float = 0.01
+    count_threshold: int = 50
+    csc_iter_num: int = 15
+    cdl_iter_num: int = 1
+    iter_num: int = 10
+    std_threshold_multiplier: float = 1.0
+    num_train: int = 2
+
+    def params(self, device: int = 0, fft_mode: int = 0, init_mode: int = 0,
+               hbm_budget_bytes: int = 0) -> CdlgbParams:
+        p = CdlgbParams()
+        _lib.lib().cdlgb_params_default(C.byref(p))
+        p.M, p.filter_size = int(self.M), int(self.filter_size)
+        p.rho, p.sigma, p.lambda_ = float(self.rho), float(self.sigma), float(self.lambda_)
+        p.csc_iter_num, p.cdl_iter_num = int(self.csc_iter_num), int(self.cdl_iter_num)
+        p.iter_num = int(self.iter_num)
+        p.std_threshold_multiplier = float(self.std_threshold_multiplier)
+        p.device, p.fft_mode, p.init_mode = int(device), int(fft_mode), int(init_mode)
+        p.hbm_budget_bytes = int(hbm_budget_bytes)
+        return p
+
+
+def _check(ctx, st: int):
+    if st != 0:
+        msg = _lib.lib().cdlgb_last_error(ctx)
+        raise CDLGBError(st, msg.decode() if msg else "")
+
+
+class CDL:
+    """Handle to one dataset's ADMM state resident on the GPU (the reference's
+    ``cdl`` struct, src/SETUP/CDL_setup.jl:70-163).  Fields are downloaded on
+    access; ``L`` is 4 x bases as in the reference."""
+
+    def __init__(self, setup: CDLSetup, device: int = 0, fft_mode: int = 0,
+                 init_mode: int = 0, hbm_budget_bytes: int = 0):
+        L = _lib.lib()
+        self.setup = setup
+        self._p = setup.params(device, fft_mode, init_mode, hbm_budget_bytes)
+        h = C.c_void_p()
+        st = L.cdlgb_create(C.byref(self._p), C.byref(h))
+        if st != 0:
+            raise CDLGBError(st, "cdlgb_create failed")
+        self._h = h
+        self.N = self.M = self.L = self.gamma = self.Lg = None
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().cdlgb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- data
+    def load_data(self, data_matrix: np.ndarray):
+        S = np.ascontiguousarray(data_matrix, dtype=np.float32)
+        if S.ndim != 2:
+            raise CDLGBError(-1, "data_matrix must be (N, 4L)")
+        N, L4 = S.shape
+        _check(self._h, _lib.lib().cdlgb_load_data(self._h, ptr(S, C.c_float), L4, N))
+        d = [C.c_int32() for _ in range(5)]
+        _check(self._h, _lib.lib().cdlgb_dims(self._h, *[C.byref(x) for x in d]))
+        self.L, self.N, self.M, self.gamma, self.Lg = [x.value for x in d]
+
+    def init_state(self, X0=None, D0=None, seed: int = 0):
+        X0c = None if X0 is None else np.ascontiguousarray(X0, np.float32).reshape(self.N, self.M, self.Lg)
+        D0c = None if D0 is None else np.ascontiguousarray(D0, np.float32).reshape(self.M, self.Lg)
+        _check(self._h, _lib.lib().cdlgb_init_state(self._h, ptr(X0c, C.c_float),
+                                                    ptr(D0c, C.c_float), C.c_uint64(seed)))
+
+    # -- fields
+    def get(self, name: str) -> np.ndarray:
+        if name == "obj_best":
+            return self.obj_best
+        if name in _LMN:
+            shape = (self.N, self.M, self.Lg)
+        elif name in _LN:
+            shape = (self.N, self.Lg)
+        elif name in _LM:
+            shape = (self.M, self.Lg)
+        else:
+            raise CDLGBError(-1, f"unknown field {name}")
+        out = np.empty(shape, np.float32)
+        _check(self._h, _lib.lib().cdlgb_get(self._h, FIELDS[name], out.ctypes.data_as(C.c_void_p),
+                                             out.nbytes))
+        return out
+
+    @property
+    def obj_best(self) -> float:
+        v = C.c_double()
+        _check(self._h, _lib.lib().cdlgb_get(self._h, 16, C.cast(C.byref(v), C.c_void_p), 8))
+        return v.value
+
+    def __getattr__(self, name):
+        if name in FIELDS:
+            return self.get(name)
+        raise AttributeError(name)
+
+    # -- instrumentation
+    def set_stream(self, stream_ptr: int | None):
+        _check(self._h, _lib.lib().cdlgb_set_stream(self._h, C.c_void_p(stream_ptr or 0) if stream_ptr else None))
+
+    def profile(self, enable: bool = True):
+        _check(self._h, _lib.lib().cdlgb_profile(self._h, 1 if enable else 0))
+
+    PHASES = ("xstep", "dstep", "objective", "xfused", "dfused_a", "dfused_b", "scan", "spare")
+
+    def profile_read(self, reset: bool = True) -> dict:
+        ms = (C.c_double * 8)()
+        cnt = (C.c_int64 * 8)()
+        la, ff = C.c_int64(), C.c_int64()
+        _check(self._h, _lib.lib().cdlgb_profile_read(self._h, ms, cnt, C.byref(la), C.byref(ff),
+                                                      1 if reset else 0))
+        out = {p: (ms[i], cnt[i]) for i, p in enumerate(self.PHASES)}
+        out["launches"] = la.value
+        out["fft_calls"] = ff.value
+        return out
+
+
+# ---------------------------------------------------------------------------- ADMM
+def init_cdl(cdl_setup: CDLSetup, data_matrix: np.ndarray, X0=None, D0=None, seed: int = 0,
+             device: int = 0, fft_mode: int = 0, init_mode: int = 0,
+             hbm_budget_bytes: int = 0) -> CDL:
+    """init_cdl (src/SETUP/CDL_setup.jl:273-283): upload the one-hot data (N, 4L),
+    allocate the state and initialise it.  X0 (N, M, Lg) / D0 (M, Lg) replace the
+    reference's unseeded random draws when given."""
+    c = CDL(cdl_setup, device=device, fft_mode=fft_mode, init_mode=init_mode,
+            hbm_budget_bytes=hbm_budget_bytes)
+    c.load_data(data_matrix)
+    c.init_state(X0, D0, seed)
+    return c
+
+
+def code_update(c: CDL, num_iter: int):
+    """code_update! (src/CDL/train.jl:1-44)."""
+    _check(c._h, _lib.lib().cdlgb_code_update(c._h, int(num_iter)))
+
+
+def dict_update(c: CDL, num_iter: int):
+    """dict_update! (src/CDL/train.jl:46-89)."""
+    _check(c._h, _lib.lib().cdlgb_dict_update(c._h, int(num_iter)))
+
+
+def objective(c: CDL) -> float:
+    """objective (src/SETUP/CDL_setup.jl:286), float64."""
+    v = C.c_double()
+    _check(c._h, _lib.lib().cdlgb_objective(c._h, C.byref(v)))
+    return v.value
+
+
+def update_best(c: CDL) -> tuple[float, bool]:
+    """update_best! (src/CDL/train.jl:91-98).  Returns (objective, improved)."""
+    v, imp = C.c_double(), C.c_int32()
+    _check(c._h, _lib.lib().cdlgb_update_best(c._h, C.byref(v), C.byref(imp)))
+    return v.value, bool(imp.value)
+
+
+def run_outer(c: CDL, iter_num: int) -> np.ndarray:
+    """iter_num passes of cdl_optimize's loop body (src/WRAPPER/wrap.jl:6-11)."""
+    objs = np.zeros(max(iter_num, 1), np.float64)
+    _check(c._h, _lib.lib().cdlgb_run_outer(c._h, int(iter_num), ptr(objs, C.c_double)))
+    return objs[:iter_num]
+
+
+def code_threshold(c: CDL) -> float:
+    """std_threshold_multiplier * std(X_best[X_best .> 0]) (src/WRAPPER/wrap.jl:12)."""
+    v = C.c_double()
+    _check(c._h, _lib.lib().cdlgb_code_threshold(c._h, C.byref(v)))
+    return v.value
+
+
+def cdl_train(cdl_setup: CDLSetup, data_matrix: np.ndarray, X0=None, D0=None, seed: int = 0,
+              verbose: bool = False, **kw):
+    """One training of cdl_optimize (src/WRAPPER/wrap.jl:5-12): init, iter_num outer
+    iterations, code threshold.  Returns (CDL handle, code_thresh, objectives)."""
+    c = init_cdl(cdl_setup, data_matrix, X0, D0, seed, **kw)
+    objs = []
+    for it in range(1, cdl_setup.iter_num + 1):
+        code_update(c, cdl_setup.csc_iter_num)
+        o, _ = update_best(c)
+        dict_update(c, cdl_setup.cdl_iter_num)
+        objs.append(o)
+        if verbose and it % 5 == 0:
+            print("obj: ", round(objective(c), 2))
+    return c, code_threshold(c), objs
+
+
+# ---------------------------------------------------------------------------- search
+def _pack_pwms(pwms, lens=None):
+    """List of (4, w_k) PWMs -> (maxlen, 4, K) float32 (Julia (K, 4, maxlen)), zero padded."""
+    K = len(pwms)
+    if lens is None:
+        lens = [np.asarray(p).shape[1] for p in pwms]
+    lens = np.asarray(lens, np.int32)
+    maxlen = int(lens.max())
+    arr = np.zeros((maxlen, 4, K), np.float32)
+    for k, p in enumerate(pwms):
+        p = np.asarray(p, np.float32)
+        arr[: lens[k], :, k] = p[:, : lens[k]].T
+    return np.ascontiguousarray(arr), lens, maxlen
+
+
+def scan_w_gpu(c: CDL, pwms, thresh, lens=None) -> np.ndarray:
+    """scan_w_gpu! + greedy_search! (src/SEARCH/scan.jl:176-239) on c's data.
+    Returns positions int32 (N, K) == Julia (K, N): 1-based argmax of the
+    thresholded forward-strand score, 0 = not found (position 1 also reads 0)."""
+    arr, lens, maxlen = _pack_pwms(pwms, lens)
+    K = len(lens)
+    th = np.ascontiguousarray(thresh, np.float32)
+    out = np.zeros((c.N, K), np.int32)
+    _check(c._h, _lib.lib().cdlgb_scan_fwd(c._h, ptr(arr, C.c_float), ptr(lens, C.c_int32),
+                                           ptr(th, C.c_float), K, maxlen, ptr(out, C.c_int32)))
+    return out
+
+
+def positions_to_dicts(pos: np.ndarray) -> list[dict]:
+    """(N, K) positions -> one Dict(n => pos) per motif, 1-based n, as scan_w_gpu!
+    builds them (scan.jl:200-205)."""
+    N, K = pos.shape
+    return [{int(n) + 1: int(pos[n, k]) for n in np.nonzero(pos[:, k])[0]} for k in range(K)]
+
+
+def overlapping_scan(c: CDL, pwms, thresh, lens=None):
+    """overlapping_scan! (src/SEARCH/scan.jl:89-121): both strands.  Returns
+    (positions int32 (N, K), scores float32 (N, K), use_comp uint8 (N, K)); position
+    0 = no score above the threshold."""
+    arr, lens, maxlen = _pack_pwms(pwms, lens)
+    K = len(lens)
+    th = np.ascontiguousarray(thresh, np.float32)
+    pos = np.zeros((c.N, K), np.int32)
+    sc = np.zeros((c.N, K), np.float32)
+    uc = np.zeros((c.N, K), np.uint8)
+    _check(c._h, _lib.lib().cdlgb_scan_both(c._h, ptr(arr, C.c_float), ptr(lens, C.c_int32),
+                                            ptr(th, C.c_float), K, maxlen, ptr(pos, C.c_int32),
+                                            ptr(sc, C.c_float), ptr(uc, C.c_uint8)))
+    return pos, sc, uc
+
+
+def count_matrices(c: CDL, positions: np.ndarray, lens, use_comp=None):
+    """Integer count matrices of the windows at ``positions`` (N, K) (1-based, 0 = none),
+    reverse-complemented where use_comp != 0.  Returns (counts int32 (K, maxlen, 4) ==
+    Julia (4, maxlen, K), nseq int32 (K,))."""
+    pos = np.ascontiguousarray(positions, np.int32)
+    lens = np.ascontiguousarray(lens, np.int32)
+    K = len(lens)
+    maxlen = int(lens.max())
+    uc = None if use_comp is None else np.ascontiguousarray(use_comp, np.uint8)
+    counts = np.zeros((K, maxlen, 4), np.int32)
+    nseq = np.zeros(K, np.int32)
+    _check(c._h, _lib.lib().cdlgb_count_pfms(c._h, ptr(pos, C.c_int32), ptr(uc, C.c_uint8),
+                                             ptr(lens, C.c_int32), K, maxlen,
+                                             ptr(counts, C.c_int32), ptr(nseq, C.c_int32)))
+    return counts, nseq
+
+
+def posdicts2pfms(c: CDL, positions: np.ndarray, lens, use_comp=None, pseudocounts_r=0.0295,
+                  pseudo_count=5.0, smoothing=True, less_pseudocount=False) -> list:
+    """posdicts2pfms (src/SEARCH/helpers.jl:59-96): count matrices on the GPU, the
+    float32 normalisation on the host.  Returns a list of (4, w_k) float32 PFMs."""
+    counts, nseq = count_matrices(c, positions, lens, use_comp)
+    lens = np.ascontiguousarray(lens, np.int32)
+    K, maxlen = len(lens), int(lens.max())
+    out = np.zeros((K, maxlen, 4), np.float32)
+    st = _lib.lib().cdlgb_counts_to_pfms(ptr(counts, C.c_int32), ptr(nseq, C.c_int32),
+                                         ptr(lens, C.c_int32), K, maxlen, float(pseudocounts_r),
+                                         float(pseudo_count), 1 if smoothing else 0,
+                                         1 if less_pseudocount else 0, ptr(out, C.c_float))
+    if st != 0:
+        raise CDLGBError(st, "counts_to_pfms")
+    return [out[k, : lens[k], :].T.copy() for k in range(K)]
+
+
+def pfm2pwm(pfm, bg=(0.25, 0.25, 0.25, 0.25)):
+    """pfm2pwm (src/SEARCH/helpers.jl:12-13): log2(pfm ./ bg) in the pfm's precision."""
+    pfm = np.asarray(pfm)
+    return np.log2(pfm / np.asarray(bg, pfm.dtype).reshape(4, 1))
+
+
+def pwm_complement(pwm):
+    """pwm_complement = reverse (src/SEARCH/helpers.jl:16)."""
+    return np.asarray(pwm)[::-1, ::-1].copy()
+
+
+def transfac_text(pfm, reverse_complement: bool = False) -> str:
+    """One transfac file body as save_pfms_as_transfac writes it."""
+    p = np.ascontiguousarray(np.asarray(pfm, np.float32).T)   # (w, 4) == Julia (4, w)
+    w = p.shape[0]
+    L = _lib.lib()
+    n = L.cdlgb_transfac_format(ptr(p, C.c_float), w, 1 if reverse_complement else 0, None, 0)
+    if n < 0:
+        raise CDLGBError(int(n), "transfac_format")
+    buf = C.create_string_buffer(int(n) + 1)
+    L.cdlgb_transfac_format(ptr(p, C.c_float), w, 1 if reverse_complement else 0, buf, n + 1)
+    return buf.value.decode()
+
+
+def save_pfms_as_transfac(logo_folder: str, pfms: list, sort_perm=None):
+    """save_pfms_as_transfac (src/SAVE/save_learned_results.jl:184-217) without the
+    weblogo calls (an external tool): writes d{i}.transfac and d{i}_c.transfac."""
+    os.makedirs(logo_folder, exist_ok=True)
+    sort_perm = list(range(1, len(pfms) + 1)) if sort_perm is None else list(sort_perm)
+    for i, ind in enumerate(sort_perm, start=1):
+        with open(os.path.join(logo_folder, f"d{i}.transfac"), "w") as f:
+            f.write(transfac_text(pfms[ind - 1], False))
+        with open(os.path.join(logo_folder, f"d{i}_c.transfac"), "w") as f:
+            f.write(transfac_text(pfms[ind - 1], True))

@@ -1,0 +1,792 @@
+// ADMM state, initialisation, objective and the cuFFT-transform path of the X- and
+// D-steps.
+//
+// Algebra (exact in real arithmetic; restates src/CDL/train.jl:1-89):
+//   The reference keeps ~20 complex spectra and runs 6 LMN-sized c2c FFTs per X-step.
+//   Because every signal is real and FFTs are linear, the X-step right-hand side
+//     RHS = conj(G1h)(Y1h - y1h) + (Y2h - y2h) + (Y3h - y3h)
+//   equals conj(G1h) * rfft(U) + rfft(V) with U = Y1 - y1', V = (Y2 - y2') + (Y3 - y3'),
+//   and the Sherman-Morrison solve (csc_kernels.jl:8-49) reduces to one cross-filter sum
+//     P = sum_m G1h[m] Vh[m],  alpha = (A Uh + P) / (A + k),  W = Uh - alpha,
+//     Xh[m] = (Vh[m] + conj(G1h[m]) W) / k,   DXh = (P + A W) / k,   A = sum_m |G1h[m]|^2.
+//   Y3 = projectionX(X + y3) holds at the start of every X-step, so it is recomputed
+//   instead of stored.  In the D-step the consensus spectrum d-hat equals rfft(d), so it
+//   is recomputed as well, and with H = (G1 - g1) + (G3 - g3), Z = G2 - g2:
+//     B = sum|Y3h|^2, Q = sum Y3h Hh, T = sum Y3h rfft(d_old),
+//     beta = (Zh B + Q) / (B + k),  dh[m] = Hh[m] + conj(Y3h[m]) (Zh - beta),  Td = irfft(T).
+//   Half spectra (F = Lg/2 + 1 bins) replace full complex spectra.
+#include "cdlgb_internal.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <algorithm>
+#include <vector>
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__host__ __device__ inline uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // a*b + c
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {  // conj(a)*b + c
+    return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, c.y)));
+}
+
+// ---------------------------------------------------------------- init kernels
+__global__ void k_randn_masked(float* __restrict__ X, size_t n, int Lg, uint64_t seed) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        int l = (int)(i % (size_t)Lg);
+        float v = 0.f;
+        if ((l & 3) == 0) {
+            uint64_t h = splitmix64(seed * 0x2545F4914F6CDD1Dull ^ (uint64_t)i);
+            float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
+            float u2 = ((float)(h & 0xFFFFFFull) + 0.5f) * (1.0f / 16777216.0f);
+            v = sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+        }
+        X[i] = v;
+    }
+}
+
+__global__ void k_mask4(float4* __restrict__ X, size_t n4) {
+    // Lg % 4 == 0, so component .x of every float4 sits on a row with (l-1) % 4 == 0
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = X[i];
+        X[i] = make_float4(v.x, 0.f, 0.f, 0.f);
+    }
+}
+
+__global__ void k_bcast_plane(float4* __restrict__ dst, const float4* __restrict__ plane,
+                              size_t pl4, size_t n4) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = plane[i % pl4];
+}
+
+// DXh[n,f] = scale * sum_m Gh[m,f] Xh[n,m,f]
+__global__ void k_spec_dot(const float2* __restrict__ Xh, const float2* __restrict__ Gh,
+                           float2* __restrict__ out, int F, int M, int N, float scale) {
+    size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= (size_t)F * N) return;
+    int f = (int)(t % F);
+    size_t n = t / F;
+    float2 acc = make_float2(0.f, 0.f);
+    const float2* x = Xh + n * M * F + f;
+    for (int m = 0; m < M; ++m) acc = cfma(Gh[(size_t)m * F + f], x[(size_t)m * F], acc);
+    out[t] = make_float2(acc.x * scale, acc.y * scale);
+}
+
+// A[f] = sum_m |Gh[m,f]|^2
+__global__ void k_colnorm(const float2* __restrict__ Gh, float* __restrict__ A, int F, int M) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    float a = 0.f;
+    for (int m = 0; m < M; ++m) {
+        float2 g = Gh[(size_t)m * F + f];
+        a = fmaf(g.x, g.x, fmaf(g.y, g.y, a));
+    }
+    A[f] = a;
+}
+
+// ---------------------------------------------------------------- X-step kernels
+__device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
+                                       float& na, float& nb, float& v) {
+    float t = x + a;                                        // X + y2
+    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);    // shrink!  (csc_kernels.jl:53-64)
+    float Y3 = keep ? x + b : 0.f;                          // projectionX! (:68-82)
+    na = (a + x) - Y2;                                      // y2 .+ X .- Y2  (train.jl:13)
+    nb = (b + x) - Y3;                                      // y3 .+ X .- Y3  (train.jl:14)
+    v = (Y2 - na) + (Y3 - nb);
+}
+
+__global__ void k_xprep(const float4* __restrict__ X, float4* __restrict__ y2,
+                        float4* __restrict__ y3, float4* __restrict__ V, size_t n4, float lam) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 x = X[i], a = y2[i], b = y3[i], na, nb, v;
+        xprep1(x.x, a.x, b.x, lam, true, na.x, nb.x, v.x);
+        xprep1(x.y, a.y, b.y, lam, false, na.y, nb.y, v.y);
+        xprep1(x.z, a.z, b.z, lam, false, na.z, nb.z, v.z);
+        xprep1(x.w, a.w, b.w, lam, false, na.w, nb.w, v.w);
+        y2[i] = na;
+        y3[i] = nb;
+        V[i] = v;
+    }
+}
+
+// y1' = y1 + DX - Y1 (train.jl:12); U = Y1 - y1'
+__global__ void k_xprep_ln(float* __restrict__ y1, const float* __restrict__ DX,
+                           const float* __restrict__ Y1, float* __restrict__ U, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float Yv = Y1[i];
+        float yn = (y1[i] + DX[i]) - Yv;
+        y1[i] = yn;
+        U[i] = Yv - yn;
+    }
+}
+
+// Per (f, n): the Sherman-Morrison code solve (csc_kernels.jl:8-49, train.jl:18-27).
+__global__ void k_xsolve(float2* __restrict__ Vh, const float2* __restrict__ Uh,
+                         const float2* __restrict__ G1h, const float* __restrict__ Ah,
+                         float2* __restrict__ DXh, int F, int M, int nfb, float kc, float scale) {
+    int fb = blockIdx.x % nfb;
+    size_t n = blockIdx.x / nfb;
+    int f = fb * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    float2* v = Vh + n * M * F + f;
+    float2 P = make_float2(0.f, 0.f);
+    for (int m = 0; m < M; ++m) P = cfma(G1h[(size_t)m * F + f], v[(size_t)m * F], P);
+    float A = Ah[f];
+    float2 u = Uh[n * F + f];
+    float inv_s = 1.f / (A + kc);
+    float2 alpha = make_float2(fmaf(A, u.x, P.x) * inv_s, fmaf(A, u.y, P.y) * inv_s);
+    float2 W = make_float2(u.x - alpha.x, u.y - alpha.y);
+    float sc = scale / kc;
+    for (int m = 0; m < M; ++m) {
+        float2 x = cjfma(G1h[(size_t)m * F + f], W, v[(size_t)m * F]);
+        v[(size_t)m * F] = make_float2(x.x * sc, x.y * sc);
+    }
+    DXh[n * F + f] = make_float2(fmaf(A, W.x, P.x) * sc, fmaf(A, W.y, P.y) * sc);
+}
+
+// Y1 = (W'S + rho (DX + y1')) / (W'W_ll + rho)   (update_Y1!, csc_kernels.jl:86-95)
+// W'S and diag(W'W) are the data placed in rows gamma..gamma+4L-1 (CDL_setup.jl:213-217).
+__global__ void k_mask_update(float* __restrict__ out, const float* __restrict__ a,
+                              const float* __restrict__ b, const float* __restrict__ S,
+                              int Lg, int L4, int gamma, size_t n, float pen) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        size_t nn = i / Lg;
+        int l = (int)(i - nn * Lg);
+        bool in = l >= gamma && l < gamma + L4;
+        float wts = in ? S[nn * L4 + (l - gamma)] : 0.f;
+        float dg = in ? 1.f : 0.f;
+        out[i] = (wts + pen * (a[i] + b[i])) / (dg + pen);
+    }
+}
+
+// ---------------------------------------------------------------- D-step kernels
+// Y3 = projectionX(X + y3), H = (G1 - g1) + (G3 - g3)
+__global__ void k_dprep(const float4* __restrict__ X, const float4* __restrict__ y3,
+                        const float4* __restrict__ g1, const float4* __restrict__ g3,
+                        const float4* __restrict__ G1, const float4* __restrict__ G3,
+                        float4* __restrict__ Y3o, float4* __restrict__ Ho, size_t n4, size_t pl4) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 x = X[i], b = y3[i], p = g1[i], q = g3[i];
+        size_t j = i % pl4;
+        float4 A = G1[j], C = G3[j];
+        Y3o[i] = make_float4(x.x + b.x, 0.f, 0.f, 0.f);
+        Ho[i] = make_float4((A.x - p.x) + (C.x - q.x), (A.y - p.y) + (C.y - q.y),
+                            (A.z - p.z) + (C.z - q.z), (A.w - p.w) + (C.w - q.w));
+    }
+}
+
+__global__ void k_sub(const float* __restrict__ a, const float* __restrict__ b,
+                      float* __restrict__ o, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        o[i] = a[i] - b[i];
+}
+
+// Per (f, n): the Sherman-Morrison dictionary solve (cdl_kernels.jl:2-33, train.jl:52-61),
+// with T = sum_m Y3h * rfft(d_old) for Td (train.jl:56).
+__global__ void k_dsolve(const float2* __restrict__ Yh, float2* __restrict__ Hh,
+                         const float2* __restrict__ Dh, const float2* __restrict__ Zh,
+                         float2* __restrict__ Th, int F, int M, int nfb, float kd, float scale) {
+    int fb = blockIdx.x % nfb;
+    size_t n = blockIdx.x / nfb;
+    int f = fb * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    size_t base = n * M * F + f;
+    float B = 0.f;
+    float2 Q = make_float2(0.f, 0.f), T = make_float2(0.f, 0.f);
+    for (int m = 0; m < M; ++m) {
+        float2 y = Yh[base + (size_t)m * F];
+        B = fmaf(y.x, y.x, fmaf(y.y, y.y, B));
+        Q = cfma(y, Hh[base + (size_t)m * F], Q);
+        T = cfma(y, Dh[base + (size_t)m * F], T);
+    }
+    float2 z = Zh[n * F + f];
+    float inv = 1.f / (B + kd);
+    float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
+    float2 W = make_float2(z.x - beta.x, z.y - beta.y);
+    for (int m = 0; m < M; ++m) {
+        float2 y = Yh[base + (size_t)m * F];
+        float2 h = cjfma(y, W, Hh[base + (size_t)m * F]);
+        Hh[base + (size_t)m * F] = make_float2(h.x * scale, h.y * scale);
+    }
+    Th[n * F + f] = make_float2(T.x * scale, T.y * scale);
+}
+
+// G2' = (W'S + sigma (Td + g2)) / (W'W_ll + sigma)  (update_g2!, cdl_kernels.jl:68-77);
+// g2' = g2 + Td - G2'  (train.jl:71)
+__global__ void k_dg2(const float* __restrict__ Td, float* __restrict__ g2,
+                      float* __restrict__ G2, const float* __restrict__ S, int Lg, int L4,
+                      int gamma, size_t n, float sigma) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        size_t nn = i / Lg;
+        int l = (int)(i - nn * Lg);
+        bool in = l >= gamma && l < gamma + L4;
+        float wts = in ? S[nn * L4 + (l - gamma)] : 0.f;
+        float dg = in ? 1.f : 0.f;
+        float t = Td[i], g = g2[i];
+        float Gn = (wts + sigma * (t + g)) / (dg + sigma);
+        G2[i] = Gn;
+        g2[i] = (g + t) - Gn;
+    }
+}
+
+// g1 += d - G1, g3 += d - G3 (train.jl:70,72) and per-chunk partial sums over sequences
+// of (d + g3'), (d + g1') and d for the consensus means (train.jl:76,83; update_best! :95).
+__global__ void k_dcons(const float4* __restrict__ d, float4* __restrict__ g1,
+                        float4* __restrict__ g3, const float4* __restrict__ G1,
+                        const float4* __restrict__ G3, float4* __restrict__ part, size_t pl4,
+                        int N, int nchunk) {
+    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= pl4) return;
+    int ch = blockIdx.y;
+    int n0 = (int)((int64_t)N * ch / nchunk), n1 = (int)((int64_t)N * (ch + 1) / nchunk);
+    float4 A = G1[j], C = G3[j];
+    float4 s1 = make_float4(0, 0, 0, 0), s3 = s1, sd = s1;
+    for (int n = n0; n < n1; ++n) {
+        size_t i = (size_t)n * pl4 + j;
+        float4 dv = d[i], a = g1[i], b = g3[i];
+        a = make_float4((a.x + dv.x) - A.x, (a.y + dv.y) - A.y, (a.z + dv.z) - A.z, (a.w + dv.w) - A.w);
+        b = make_float4((b.x + dv.x) - C.x, (b.y + dv.y) - C.y, (b.z + dv.z) - C.z, (b.w + dv.w) - C.w);
+        g1[i] = a;
+        g3[i] = b;
+        s1.x += dv.x + a.x; s1.y += dv.y + a.y; s1.z += dv.z + a.z; s1.w += dv.w + a.w;
+        s3.x += dv.x + b.x; s3.y += dv.y + b.y; s3.z += dv.z + b.z; s3.w += dv.w + b.w;
+        sd.x += dv.x; sd.y += dv.y; sd.z += dv.z; sd.w += dv.w;
+    }
+    part[((size_t)ch * 3 + 0) * pl4 + j] = s1;
+    part[((size_t)ch * 3 + 1) * pl4 + j] = s3;
+    part[((size_t)ch * 3 + 2) * pl4 + j] = sd;
+}
+
+// v1 = sum(d+g1)/N, v2 = sum(d+g3)/N, dmean = sum(d)/N;  G3 = projection2box!(v2)
+// (cdl_kernels.jl:37-51); P_D = 1 on rows l < filter_len.
+__global__ void k_dfinish(const float* __restrict__ part, float* __restrict__ v1,
+                          float* __restrict__ G3, float* __restrict__ dmean, size_t pl,
+                          int Lg, int flen, int N, int nchunk) {
+    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= pl) return;
+    double s1 = 0, s3 = 0, sd = 0;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        s1 += part[((size_t)ch * 3 + 0) * pl + j];
+        s3 += part[((size_t)ch * 3 + 1) * pl + j];
+        sd += part[((size_t)ch * 3 + 2) * pl + j];
+    }
+    float a = (float)(s1 / N), b = (float)(s3 / N);
+    v1[j] = a;
+    dmean[j] = (float)(sd / N);
+    int l = (int)(j % Lg);
+    bool sup = l < flen;
+    G3[j] = b >= 1.f ? (sup ? 1.f : 0.f) : (b <= 0.f ? 0.f : (sup ? b : 0.f));
+}
+
+// prox_simplex_zeros! (cdl_kernels.jl:53-66), group index as in the reference: for
+// 1-based row l the group is rows i+1..i+4 with i = 4*floor(l/4).
+__global__ void k_dprox(const float* __restrict__ v1, float* __restrict__ G1, int Lg, int M,
+                        int flen) {
+    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= (size_t)Lg * M) return;
+    int l0 = (int)(j % Lg);
+    size_t col = j - l0;
+    float out = 0.f;
+    if (l0 < flen) {
+        int i = 4 * ((l0 + 1) / 4);
+        const float* v = v1 + col;
+        double grp = (double)v[i] + v[i + 1] + v[i + 2] + v[i + 3];
+        out = (float)((double)v[l0] - 0.25 * (grp - 1.0));
+    }
+    G1[j] = out;
+}
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    __syncthreads();
+    return t;
+}
+
+__global__ void k_abssum(const float4* __restrict__ X, size_t n4, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = X[i];
+        acc += (double)((fabsf(v.x) + fabsf(v.y)) + (fabsf(v.z) + fabsf(v.w)));
+    }
+    acc = block_sum_d(acc, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = acc;
+}
+
+// sum over the data window of (DX - S)^2  (||W*DX - S||^2)
+__global__ void k_fit(const float* __restrict__ DX, const float* __restrict__ S, int Lg, int L4,
+                      int gamma, size_t n, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        size_t nn = i / L4;
+        int j = (int)(i - nn * L4);
+        double r = (double)DX[nn * Lg + gamma + j] - (double)S[i];
+        acc += r * r;
+    }
+    acc = block_sum_d(acc, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = acc;
+}
+
+// out[0] = 0.5 * sum(part[nb1..nb1+nb2)) + lam * sum(part[0..nb1))
+__global__ void k_obj_final(const double* __restrict__ part, int nb1, int nb2, double lam,
+                            double* __restrict__ out) {
+    __shared__ double sh[32];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < nb1; i += blockDim.x) a += part[i];
+    for (int i = threadIdx.x; i < nb2; i += blockDim.x) b += part[nb1 + i];
+    a = block_sum_d(a, sh);
+    b = block_sum_d(b, sh);
+    if (threadIdx.x == 0) out[0] = 0.5 * b + lam * a;
+}
+
+// std of the positive entries: pass 1 count + sum, pass 2 sum of squared deviations
+__global__ void k_pos_stats(const float4* __restrict__ X, size_t n4, const double* __restrict__ mu,
+                            double* __restrict__ out) {
+    __shared__ double sh[32];
+    double c = 0.0, s = 0.0;
+    double m = mu ? mu[0] : 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = X[i];
+        float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (e[k] > 0.f) {
+                if (mu) { double t = (double)e[k] - m; s += t * t; }
+                else { c += 1.0; s += (double)e[k]; }
+            }
+    }
+    c = block_sum_d(c, sh);
+    s = block_sum_d(s, sh);
+    if (threadIdx.x == 0) {
+        out[2 * blockIdx.x] = c;
+        out[2 * blockIdx.x + 1] = s;
+    }
+}
+
+__global__ void k_pos_final(const double* __restrict__ part, int nb, double* __restrict__ out,
+                            int second) {
+    __shared__ double sh[32];
+    double c = 0.0, s = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        c += part[2 * i];
+        s += part[2 * i + 1];
+    }
+    c = block_sum_d(c, sh);
+    s = block_sum_d(s, sh);
+    if (threadIdx.x == 0) {
+        if (!second) { out[0] = c; out[1] = c > 0 ? s / c : 0.0; }
+        else out[2] = out[0] > 1 ? sqrt(s / (out[0] - 1.0)) : nan("");
+    }
+}
+
+// host-side seeded normal (used for D0 when none is given)
+double host_normal(uint64_t seed, uint64_t i) {
+    uint64_t h = splitmix64(seed * 0x2545F4914F6CDD1Dull ^ (i + 0x9E37ull));
+    double u1 = ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    uint64_t h2 = splitmix64(h);
+    double u2 = ((double)(h2 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
+}
+double host_uniform(uint64_t seed, uint64_t i) {
+    uint64_t h = splitmix64(seed * 0x9E3779B97F4A7C15ull ^ (i + 0x51ull));
+    return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+int make_plans(cdlgb_ctx* c) {
+    long long n[1] = {c->Lg};
+    long long in_r[1] = {c->Lg}, in_c[1] = {c->F};
+    size_t ws = 0;
+    long long bLMN = (long long)c->M * c->N, bLN = c->N, bLM = c->M;
+    FFT_TRY(c, cufftCreate(&c->pR2C_LMN));
+    FFT_TRY(c, cufftMakePlanMany64(c->pR2C_LMN, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, bLMN, &ws));
+    FFT_TRY(c, cufftCreate(&c->pC2R_LMN));
+    FFT_TRY(c, cufftMakePlanMany64(c->pC2R_LMN, 1, n, in_c, 1, c->F, in_r, 1, c->Lg, CUFFT_C2R, bLMN, &ws));
+    FFT_TRY(c, cufftCreate(&c->pR2C_LN));
+    FFT_TRY(c, cufftMakePlanMany64(c->pR2C_LN, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, bLN, &ws));
+    FFT_TRY(c, cufftCreate(&c->pC2R_LN));
+    FFT_TRY(c, cufftMakePlanMany64(c->pC2R_LN, 1, n, in_c, 1, c->F, in_r, 1, c->Lg, CUFFT_C2R, bLN, &ws));
+    FFT_TRY(c, cufftCreate(&c->pR2C_LM));
+    FFT_TRY(c, cufftMakePlanMany64(c->pR2C_LM, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, bLM, &ws));
+    c->plans = true;
+    return CDLGB_OK;
+}
+
+int set_plan_streams(cdlgb_ctx* c) {
+    if (!c->plans) return CDLGB_OK;
+    FFT_TRY(c, cufftSetStream(c->pR2C_LMN, c->stream));
+    FFT_TRY(c, cufftSetStream(c->pC2R_LMN, c->stream));
+    FFT_TRY(c, cufftSetStream(c->pR2C_LN, c->stream));
+    FFT_TRY(c, cufftSetStream(c->pC2R_LN, c->stream));
+    FFT_TRY(c, cufftSetStream(c->pR2C_LM, c->stream));
+    return CDLGB_OK;
+}
+
+int r2c(cdlgb_ctx* c, cufftHandle p, float* in, float2* out) {
+    FFT_TRY(c, cufftExecR2C(p, (cufftReal*)in, (cufftComplex*)out));
+    c->fft_calls++;
+    return CDLGB_OK;
+}
+int c2r(cdlgb_ctx* c, cufftHandle p, float2* in, float* out) {
+    FFT_TRY(c, cufftExecC2R(p, (cufftComplex*)in, (cufftReal*)out));
+    c->fft_calls++;
+    return CDLGB_OK;
+}
+
+// G1h = rfft(G1) and A = sum_m |G1h|^2
+int refresh_G1h(cdlgb_ctx* c) {
+    ST_TRY(r2c(c, c->pR2C_LM, c->G1, c->G1h));
+    k_colnorm<<<(c->F + 127) / 128, 128, 0, c->stream>>>(c->G1h, c->Ah, c->F, c->M);
+    LAUNCH_CHECK(c, "k_colnorm");
+    return CDLGB_OK;
+}
+
+float* cur_X(cdlgb_ctx* c) { return c->Xb[c->xcur]; }
+
+}  // namespace
+
+// ============================================================================ API-level
+size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
+    size_t gamma = 4 * (size_t)p->filter_size, Lg = L4 + 2 * gamma, F = Lg / 2 + 1;
+    size_t M = p->M, LMN = Lg * M * N, LN = Lg * N, LM = Lg * M;
+    size_t b = 0;
+    b += (size_t)N * L4 * 4;                    // data
+    b += 7 * LMN * 4;                           // X x2, y2, y3, d, g1, g3
+    b += 8 * LN * 4;                            // Y1 y1 DX Td G2 g2 + 2 scratch
+    b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
+    b += 2 * N * F * 8;                         // LN spectra
+    if (fused) {
+        b += fused_scratch_bytes((int)Lg, (int)M, N);
+    } else {
+        b += 2 * LMN * 4 + 3 * (size_t)N * M * F * 8;   // cuFFT-path scratch
+        b += LMN * 4 / 2;                               // cuFFT work area (estimate)
+    }
+    b += 64ull * 3 * LM * 4;                    // D-step partials
+    b += (64u << 20);                           // reductions, scan scratch, slack
+    return b;
+}
+
+int admm_alloc(cdlgb_ctx* c) {
+    const size_t LMN = c->LMN, LN = c->LN, LM = c->LM;
+    auto A = [&](void** p, size_t bytes) -> int {
+        CU_TRY(c, cudaMalloc(p, bytes));
+        return CDLGB_OK;
+    };
+    ST_TRY(A((void**)&c->Xb[0], LMN * 4));
+    ST_TRY(A((void**)&c->Xb[1], LMN * 4));
+    ST_TRY(A((void**)&c->y2, LMN * 4));
+    ST_TRY(A((void**)&c->y3, LMN * 4));
+    ST_TRY(A((void**)&c->d, LMN * 4));
+    ST_TRY(A((void**)&c->g1, LMN * 4));
+    ST_TRY(A((void**)&c->g3, LMN * 4));
+    ST_TRY(A((void**)&c->Y1, LN * 4));
+    ST_TRY(A((void**)&c->y1, LN * 4));
+    ST_TRY(A((void**)&c->DX, LN * 4));
+    ST_TRY(A((void**)&c->Td, LN * 4));
+    ST_TRY(A((void**)&c->G2, LN * 4));
+    ST_TRY(A((void**)&c->g2, LN * 4));
+    ST_TRY(A((void**)&c->sU, LN * 4));
+    ST_TRY(A((void**)&c->G1, LM * 4));
+    ST_TRY(A((void**)&c->G3, LM * 4));
+    ST_TRY(A((void**)&c->dsum, LM * 4));
+    ST_TRY(A((void**)&c->Dbest, LM * 4));
+    ST_TRY(A((void**)&c->vbar, LM * 4));
+    ST_TRY(A((void**)&c->G1h, (size_t)c->M * c->F * 8));
+    ST_TRY(A((void**)&c->Ah, (size_t)c->F * 4));
+    ST_TRY(A((void**)&c->sUh, (size_t)c->N * c->F * 8));
+    ST_TRY(A((void**)&c->sVh, (size_t)c->N * c->F * 8));
+    // spectra of the whole dataset are needed at init (DX) and by the cuFFT path
+    ST_TRY(A((void**)&c->sA, LMN * 4));
+    ST_TRY(A((void**)&c->sAh, (size_t)c->N * c->M * c->F * 8));
+    if (!c->fused) {
+        ST_TRY(A((void**)&c->sB, LMN * 4));
+        ST_TRY(A((void**)&c->sBh, (size_t)c->N * c->M * c->F * 8));
+        ST_TRY(A((void**)&c->sCh, (size_t)c->N * c->M * c->F * 8));
+    }
+    c->nchunk = std::max(1, std::min(64, c->N));
+    ST_TRY(A((void**)&c->part, (size_t)c->nchunk * 3 * LM * 4));
+    c->nred = 152 * 4;
+    ST_TRY(A((void**)&c->dred, (size_t)c->nred * 4 * sizeof(double)));
+    ST_TRY(A((void**)&c->dscalar, 8 * sizeof(double)));
+    CU_TRY(c, cudaMallocHost((void**)&c->hscalar, 8 * sizeof(double)));
+    ST_TRY(make_plans(c));
+    ST_TRY(set_plan_streams(c));
+    return CDLGB_OK;
+}
+
+void admm_free(cdlgb_ctx* c) {
+    float** fl[] = {&c->Xb[0], &c->Xb[1], &c->y2, &c->y3, &c->d, &c->g1, &c->g3, &c->Y1,
+                    &c->y1, &c->DX, &c->Td, &c->G2, &c->g2, &c->sU, &c->G1, &c->G3,
+                    &c->dsum, &c->Dbest, &c->vbar, &c->Ah, &c->sA, &c->sB, &c->part};
+    for (auto p : fl) { if (*p) cudaFree(*p); *p = nullptr; }
+    float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh};
+    for (auto p : cl) { if (*p) cudaFree(*p); *p = nullptr; }
+    if (c->dred) cudaFree(c->dred);
+    if (c->dscalar) cudaFree(c->dscalar);
+    if (c->hscalar) cudaFreeHost(c->hscalar);
+    c->dred = nullptr; c->dscalar = nullptr; c->hscalar = nullptr;
+    if (c->plans) {
+        cufftDestroy(c->pR2C_LMN); cufftDestroy(c->pC2R_LMN); cufftDestroy(c->pR2C_LN);
+        cufftDestroy(c->pC2R_LN); cufftDestroy(c->pR2C_LM);
+        c->plans = false;
+    }
+}
+
+int cdlgb_set_plan_streams(cdlgb_ctx* c) { return set_plan_streams(c); }
+
+int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
+    cudaStream_t s = c->stream;
+    const int Lg = c->Lg, M = c->M, N = c->N, flen = 4 * c->p.filter_size;
+    const size_t LMN = c->LMN, LN = c->LN, LM = c->LM;
+    c->xcur = 0;
+    c->best_is_cur = 1;
+    float* X = c->Xb[0];
+    // X0 (CDL_setup.jl:191-192): given, or standard normal; then masked to the 4-stride
+    if (X0) {
+        CU_TRY(c, cudaMemcpyAsync(X, X0, LMN * 4, cudaMemcpyHostToDevice, s));
+    } else {
+        k_randn_masked<<<grid_for(LMN, kBlock), kBlock, 0, s>>>(X, LMN, Lg, seed);
+        LAUNCH_CHECK(c, "k_randn_masked");
+    }
+    k_mask4<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)X, LMN / 4);
+    LAUNCH_CHECK(c, "k_mask4");
+    // D0 (CDL_setup.jl:182-183), masked by P_D
+    std::vector<float> D(LM, 0.f);
+    if (D0) {
+        for (int m = 0; m < M; ++m)
+            for (int l = 0; l < flen; ++l) D[(size_t)m * Lg + l] = D0[(size_t)m * Lg + l];
+    } else if (c->p.init_mode == 1) {
+        // the reference's draw: per 4-row group a uniform point on the simplex
+        uint64_t ctr = 0;
+        for (int m = 0; m < M; ++m)
+            for (int g = 0; g < flen / 4; ++g) {
+                double u[3];
+                for (int k = 0; k < 3; ++k) u[k] = host_uniform(seed, ctr++);
+                std::sort(u, u + 3);
+                double w[5] = {0, u[0], u[1], u[2], 1};
+                for (int k = 0; k < 4; ++k) D[(size_t)m * Lg + 4 * g + k] = (float)(w[k + 1] - w[k]);
+            }
+    } else {
+        uint64_t ctr = 0;
+        for (int m = 0; m < M; ++m) {
+            double nrm = 0;
+            std::vector<double> v(flen);
+            for (int l = 0; l < flen; ++l) { v[l] = host_normal(seed, ctr++); nrm += v[l] * v[l]; }
+            nrm = sqrt(nrm);
+            for (int l = 0; l < flen; ++l) D[(size_t)m * Lg + l] = (float)(v[l] / nrm);
+        }
+    }
+    CU_TRY(c, cudaMemcpyAsync(c->G1, D.data(), LM * 4, cudaMemcpyHostToDevice, s));
+    CU_TRY(c, cudaMemcpyAsync(c->G3, c->G1, LM * 4, cudaMemcpyDeviceToDevice, s));
+    CU_TRY(c, cudaMemcpyAsync(c->Dbest, c->G1, LM * 4, cudaMemcpyDeviceToDevice, s));
+    CU_TRY(c, cudaMemcpyAsync(c->dsum, c->G1, LM * 4, cudaMemcpyDeviceToDevice, s));
+    // d = real(ifft(d-hat)) with d-hat = D-hat broadcast (CDL_setup.jl:207-210)
+    k_bcast_plane<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)c->d, (const float4*)c->G1,
+                                                                 LM / 4, LMN / 4);
+    LAUNCH_CHECK(c, "k_bcast_plane");
+    // duals and Y1 start at zero (CDL_setup.jl:220-230)
+    CU_TRY(c, cudaMemsetAsync(c->y2, 0, LMN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->y3, 0, LMN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->g1, 0, LMN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->g3, 0, LMN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->Y1, 0, LN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->y1, 0, LN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->g2, 0, LN * 4, s));
+    CU_TRY(c, cudaMemsetAsync(c->Td, 0, LN * 4, s));
+    ST_TRY(refresh_G1h(c));
+    // DX = real(ifft(sum_m D-hat .* X-hat)) (CDL_setup.jl:197-203); G2 = DX
+    ST_TRY(r2c(c, c->pR2C_LMN, X, c->sAh));
+    size_t FN = (size_t)c->F * N;
+    k_spec_dot<<<(unsigned)((FN + 255) / 256), 256, 0, s>>>(c->sAh, c->G1h, c->sVh, c->F, M, N,
+                                                          1.f / (float)Lg);
+    LAUNCH_CHECK(c, "k_spec_dot");
+    ST_TRY(c2r(c, c->pC2R_LN, c->sVh, c->DX));
+    CU_TRY(c, cudaMemcpyAsync(c->G2, c->DX, LN * 4, cudaMemcpyDeviceToDevice, s));
+    c->initialized = true;
+    double obj = 0;
+    ST_TRY(admm_objective(c, &obj));
+    c->obj_best = obj;
+    return CDLGB_OK;
+}
+
+int admm_code_update(cdlgb_ctx* c, int iters) {
+    cudaStream_t s = c->stream;
+    const size_t LMN = c->LMN, LN = c->LN;
+    const int F = c->F, M = c->M, N = c->N;
+    for (int it = 0; it < iters; ++it) {
+        cdlgb_phase_begin(c, PH_XSTEP);
+        // X_best aliases the current buffer: write the new X into the other one
+        float* Xin = cur_X(c);
+        float* Xout = c->best_is_cur ? c->Xb[1 - c->xcur] : Xin;
+        if (c->fused) {
+            ST_TRY(fused_xstep(c, Xin, Xout, 0));
+        } else {
+            k_xprep<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>(
+                (const float4*)Xin, (float4*)c->y2, (float4*)c->y3, (float4*)c->sA, LMN / 4,
+                c->p.lambda);
+            LAUNCH_CHECK(c, "k_xprep");
+            k_xprep_ln<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->y1, c->DX, c->Y1, c->sU, LN);
+            LAUNCH_CHECK(c, "k_xprep_ln");
+            ST_TRY(r2c(c, c->pR2C_LMN, c->sA, c->sAh));
+            ST_TRY(r2c(c, c->pR2C_LN, c->sU, c->sUh));
+            int nfb = (F + 127) / 128;
+            k_xsolve<<<(unsigned)((size_t)nfb * N), 128, 0, s>>>(c->sAh, c->sUh, c->G1h, c->Ah,
+                                                                 c->sVh, F, M, nfb,
+                                                                 c->p.sherman_const_csc,
+                                                                 1.f / (float)c->Lg);
+            LAUNCH_CHECK(c, "k_xsolve");
+            ST_TRY(c2r(c, c->pC2R_LMN, c->sAh, Xout));
+            ST_TRY(c2r(c, c->pC2R_LN, c->sVh, c->DX));
+            k_mask_update<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Y1, c->DX, c->y1, c->S, c->Lg,
+                                                                 c->L4, c->gamma, LN, c->p.rho);
+            LAUNCH_CHECK(c, "k_mask_update");
+        }
+        if (Xout != Xin) {
+            c->xcur = 1 - c->xcur;
+            c->best_is_cur = 0;
+        }
+        cdlgb_phase_end(c, PH_XSTEP);
+    }
+    return CDLGB_OK;
+}
+
+int admm_dict_update(cdlgb_ctx* c, int iters) {
+    cudaStream_t s = c->stream;
+    const size_t LMN = c->LMN, LN = c->LN, LM = c->LM;
+    const int F = c->F, M = c->M, N = c->N, Lg = c->Lg;
+    for (int it = 0; it < iters; ++it) {
+        cdlgb_phase_begin(c, PH_DSTEP);
+        if (c->fused) {
+            ST_TRY(fused_dstep(c));
+        } else {
+            k_dprep<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>(
+                (const float4*)cur_X(c), (const float4*)c->y3, (const float4*)c->g1,
+                (const float4*)c->g3, (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA,
+                (float4*)c->sB, LMN / 4, LM / 4);
+            LAUNCH_CHECK(c, "k_dprep");
+            k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
+            LAUNCH_CHECK(c, "k_sub");
+            ST_TRY(r2c(c, c->pR2C_LMN, c->sA, c->sAh));
+            ST_TRY(r2c(c, c->pR2C_LMN, c->sB, c->sBh));
+            ST_TRY(r2c(c, c->pR2C_LMN, c->d, c->sCh));
+            ST_TRY(r2c(c, c->pR2C_LN, c->sU, c->sUh));
+            int nfb = (F + 127) / 128;
+            k_dsolve<<<(unsigned)((size_t)nfb * N), 128, 0, s>>>(c->sAh, c->sBh, c->sCh, c->sUh,
+                                                                 c->sVh, F, M, nfb,
+                                                                 c->p.sherman_const_cdl,
+                                                                 1.f / (float)Lg);
+            LAUNCH_CHECK(c, "k_dsolve");
+            ST_TRY(c2r(c, c->pC2R_LMN, c->sBh, c->d));
+            ST_TRY(c2r(c, c->pC2R_LN, c->sVh, c->Td));
+            k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
+                                                         c->gamma, LN, c->p.sigma);
+            LAUNCH_CHECK(c, "k_dg2");
+            size_t pl4 = LM / 4;
+            dim3 g((unsigned)((pl4 + 255) / 256), (unsigned)c->nchunk);
+            k_dcons<<<g, 256, 0, s>>>((const float4*)c->d, (float4*)c->g1, (float4*)c->g3,
+                                      (const float4*)c->G1, (const float4*)c->G3,
+                                      (float4*)c->part, pl4, N, c->nchunk);
+            LAUNCH_CHECK(c, "k_dcons");
+        }
+        int flen = 4 * c->p.filter_size;
+        k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
+                                                               LM, Lg, flen, N, c->nchunk);
+        LAUNCH_CHECK(c, "k_dfinish");
+        k_dprox<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->vbar, c->G1, Lg, M, flen);
+        LAUNCH_CHECK(c, "k_dprox");
+        ST_TRY(refresh_G1h(c));
+        cdlgb_phase_end(c, PH_DSTEP);
+    }
+    return CDLGB_OK;
+}
+
+// objective into c->dscalar[0] (device), no host sync
+static int objective_async(cdlgb_ctx* c) {
+    cudaStream_t s = c->stream;
+    int nb1 = 152 * 2, nb2 = 152;
+    k_abssum<<<nb1, kBlock, 0, s>>>((const float4*)cur_X(c), c->LMN / 4, c->dred);
+    LAUNCH_CHECK(c, "k_abssum");
+    k_fit<<<nb2, kBlock, 0, s>>>(c->DX, c->S, c->Lg, c->L4, c->gamma, (size_t)c->N * c->L4,
+                                 c->dred + nb1);
+    LAUNCH_CHECK(c, "k_fit");
+    k_obj_final<<<1, kBlock, 0, s>>>(c->dred, nb1, nb2, (double)c->p.lambda, c->dscalar);
+    LAUNCH_CHECK(c, "k_obj_final");
+    return CDLGB_OK;
+}
+
+int admm_objective(cdlgb_ctx* c, double* obj) {
+    cdlgb_phase_begin(c, PH_OBJ);
+    ST_TRY(objective_async(c));
+    CU_TRY(c, cudaMemcpyAsync(c->hscalar, c->dscalar, sizeof(double), cudaMemcpyDeviceToHost,
+                              c->stream));
+    cdlgb_phase_end(c, PH_OBJ);
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    *obj = c->hscalar[0];
+    return CDLGB_OK;
+}
+
+int admm_update_best(cdlgb_ctx* c, double* obj, int* improved) {
+    double o = 0;
+    ST_TRY(admm_objective(c, &o));
+    int imp = o < c->obj_best;
+    if (imp) {
+        c->obj_best = o;
+        // D_best = sum(d, dims=3) / N (train.jl:95), kept up to date by the D-step;
+        // X_best = copy(X) (:96) becomes an alias of the current X buffer.
+        CU_TRY(c, cudaMemcpyAsync(c->Dbest, c->dsum, c->LM * 4, cudaMemcpyDeviceToDevice,
+                                  c->stream));
+        c->best_is_cur = 1;
+    }
+    if (obj) *obj = o;
+    if (improved) *improved = imp;
+    return CDLGB_OK;
+}
+
+int admm_code_threshold(cdlgb_ctx* c, double* thr) {
+    cudaStream_t s = c->stream;
+    const float* Xbest = c->best_is_cur ? c->Xb[c->xcur] : c->Xb[1 - c->xcur];
+    int nb = 152 * 2;
+    k_pos_stats<<<nb, kBlock, 0, s>>>((const float4*)Xbest, c->LMN / 4, nullptr, c->dred);
+    LAUNCH_CHECK(c, "k_pos_stats");
+    k_pos_final<<<1, kBlock, 0, s>>>(c->dred, nb, c->dscalar, 0);
+    LAUNCH_CHECK(c, "k_pos_final");
+    k_pos_stats<<<nb, kBlock, 0, s>>>((const float4*)Xbest, c->LMN / 4, c->dscalar + 1, c->dred);
+    LAUNCH_CHECK(c, "k_pos_stats");
+    k_pos_final<<<1, kBlock, 0, s>>>(c->dred, nb, c->dscalar, 1);
+    LAUNCH_CHECK(c, "k_pos_final");
+    CU_TRY(c, cudaMemcpyAsync(c->hscalar, c->dscalar, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CU_TRY(c, cudaStreamSynchronize(s));
+    *thr = c->hscalar[2] * (double)c->p.std_threshold_multiplier;
+    return CDLGB_OK;
+}

@@ -1,0 +1,409 @@
+// C ABI entry points of libcdlgb (declared in include/cdlgb.h).
+#include "cdlgb_internal.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+int cdlgb_seterr(cdlgb_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c->err, sizeof(c->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+int cdlgb_after_launch(cdlgb_ctx* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cdlgb_seterr(c, CDLGB_ECUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+    c->launches++;
+    return CDLGB_OK;
+}
+
+// ---- phase timers: a ring of event pairs, read back (and synchronised) on demand
+namespace {
+constexpr int kRing = 4096;
+struct Ring {
+    cudaEvent_t ev[2 * kRing];
+    int ph[kRing];
+    int used = 0;
+    int open[PH_COUNT];
+};
+}  // namespace
+
+static void ring_collect(cdlgb_ctx* c) {
+    Ring* r = (Ring*)c->ring;
+    if (!r) return;
+    cudaStreamSynchronize(c->stream);
+    for (int k = 0; k < r->used; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r->ev[2 * k], r->ev[2 * k + 1]) == cudaSuccess) {
+            c->ph_ms[r->ph[k]] += ms;
+            c->ph_n[r->ph[k]] += 1;
+        }
+    }
+    r->used = 0;
+}
+
+void cdlgb_phase_begin(cdlgb_ctx* c, int ph) {
+    Ring* r = (Ring*)c->ring;
+    if (!c->profile || !r) return;
+    if (r->used >= kRing) ring_collect(c);
+    int k = r->used++;
+    r->ph[k] = ph;
+    r->open[ph] = k;
+    cudaEventRecord(r->ev[2 * k], c->stream);
+}
+
+void cdlgb_phase_end(cdlgb_ctx* c, int ph) {
+    Ring* r = (Ring*)c->ring;
+    if (!c->profile || !r) return;
+    int k = r->open[ph];
+    if (k < 0 || k >= r->used) return;
+    cudaEventRecord(r->ev[2 * k + 1], c->stream);
+    r->open[ph] = -1;
+}
+
+extern "C" {
+
+int cdlgb_params_default(cdlgb_params* p) {
+    if (!p) return CDLGB_EINVAL;
+    memset(p, 0, sizeof(*p));
+    p->M = 10;
+    p->filter_size = 4;
+    p->rho = 100.f;
+    p->sigma = 100.f;
+    p->lambda = 0.01f;
+    p->csc_iter_num = 15;
+    p->cdl_iter_num = 1;
+    p->iter_num = 10;
+    p->std_threshold_multiplier = 1.f;
+    p->sherman_const_csc = 2.f;
+    p->sherman_const_cdl = 2.f;
+    p->device = 0;
+    p->init_mode = 0;
+    p->fft_mode = 0;
+    p->hbm_budget_bytes = 0;
+    return CDLGB_OK;
+}
+
+static int check_params(cdlgb_ctx* c, const cdlgb_params* p) {
+    if (p->M < 1 || p->M > 4096) return cdlgb_seterr(c, CDLGB_EINVAL, "M=%d out of range", p->M);
+    if (p->filter_size < 1 || p->filter_size > 1024)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "filter_size=%d out of range", p->filter_size);
+    if (!(p->rho > 0) || !(p->sigma > 0) || !(p->lambda >= 0))
+        return cdlgb_seterr(c, CDLGB_EINVAL, "rho, sigma must be > 0 and lambda >= 0");
+    if (!(p->sherman_const_csc > 0) || !(p->sherman_const_cdl > 0))
+        return cdlgb_seterr(c, CDLGB_EINVAL, "sherman constants must be > 0");
+    if (p->fft_mode < 0 || p->fft_mode > 2)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "fft_mode=%d (0 auto, 1 cuFFT, 2 fused)", p->fft_mode);
+    return CDLGB_OK;
+}
+
+int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out) {
+    if (!p || !out) return CDLGB_EINVAL;
+    *out = nullptr;
+    cdlgb_ctx* c = new (std::nothrow) cdlgb_ctx();
+    if (!c) return CDLGB_EINVAL;
+    c->err[0] = 0;
+    c->p = *p;
+    int st = check_params(c, p);
+    if (st) { fprintf(stderr, "cdlgb_create: %s\n", c->err); delete c; return st; }
+    c->dev = p->device;
+    cudaError_t e = cudaSetDevice(c->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "cdlgb_create: %s\n", cudaGetErrorString(e));
+        delete c;
+        return CDLGB_ECUDA;
+    }
+    c->own_stream = true;
+    Ring* r = new (std::nothrow) Ring();
+    if (r) {
+        bool ok = true;
+        for (int i = 0; i < 2 * kRing && ok; ++i) ok = cudaEventCreate(&r->ev[i]) == cudaSuccess;
+        for (int i = 0; i < PH_COUNT; ++i) r->open[i] = -1;
+        if (!ok) { delete r; r = nullptr; }
+    }
+    c->ring = r;
+    *out = c;
+    return CDLGB_OK;
+}
+
+int cdlgb_destroy(cdlgb_ctx* c) {
+    if (!c) return CDLGB_OK;
+    cudaSetDevice(c->dev);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    admm_free(c);
+    fused_free(c);
+    scan_free(c);
+    if (c->S) cudaFree(c->S);
+    Ring* r = (Ring*)c->ring;
+    if (r) {
+        for (int i = 0; i < 2 * kRing; ++i) cudaEventDestroy(r->ev[i]);
+        delete r;
+    }
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return CDLGB_OK;
+}
+
+const char* cdlgb_last_error(const cdlgb_ctx* c) { return c ? c->err : "null context"; }
+
+static int pick_fused(const cdlgb_params* p, int Lg) {
+    if (p->fft_mode == 1) return 0;
+    int ok = fused_supported(Lg, p->M);
+    if (p->fft_mode == 2) return ok ? 1 : -1;
+    return ok;
+}
+
+int cdlgb_footprint(const cdlgb_params* p, int32_t L, int32_t N, uint64_t* bytes) {
+    if (!p || !bytes || L <= 0 || N <= 0) return CDLGB_EINVAL;
+    int L4 = 4 * L, Lg = L4 + 8 * p->filter_size;
+    int f = pick_fused(p, Lg);
+    *bytes = admm_footprint(p, L4, N, f > 0);
+    return CDLGB_OK;
+}
+
+int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
+    if (!c) return CDLGB_EINVAL;
+    if (!onehot || L4 <= 0 || N <= 0)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "load_data: null data or bad size (4L=%d, N=%d)", L4, N);
+    // CDL_setup.jl:174
+    if (L4 % 4) return cdlgb_seterr(c, CDLGB_EINVAL, "first dimension of dat must be multiple of 4s (got %d)", L4);
+    CU_TRY(c, cudaSetDevice(c->dev));
+    if (c->loaded) {
+        CU_TRY(c, cudaStreamSynchronize(c->stream));
+        admm_free(c);
+        fused_free(c);
+        if (c->S) cudaFree(c->S);
+        c->S = nullptr;
+        c->loaded = c->initialized = false;
+    }
+    const cdlgb_params& p = c->p;
+    c->L4 = L4;
+    c->N = N;
+    c->M = p.M;
+    c->gamma = 4 * p.filter_size;
+    c->Lg = L4 + 2 * c->gamma;
+    c->F = c->Lg / 2 + 1;
+    c->LMN = (size_t)c->Lg * c->M * N;
+    c->LN = (size_t)c->Lg * N;
+    c->LM = (size_t)c->Lg * c->M;
+    int f = pick_fused(&p, c->Lg);
+    if (f < 0)
+        return cdlgb_seterr(c, CDLGB_ENOTSUP, "fused path does not support Lg=%d, M=%d", c->Lg, c->M);
+    c->fused = f;
+    // admission by HBM footprint
+    size_t need = admm_footprint(&p, L4, N, c->fused);
+    size_t freeb = 0, total = 0;
+    CU_TRY(c, cudaMemGetInfo(&freeb, &total));
+    size_t budget = p.hbm_budget_bytes ? (size_t)p.hbm_budget_bytes
+                                       : (freeb > (1ull << 30) ? freeb - (1ull << 30) : 0);
+    if (need > budget)
+        return cdlgb_seterr(c, CDLGB_ENOMEM_BUDGET,
+                            "dataset needs %.2f GB of device memory, budget is %.2f GB (N=%d, 4L=%d, M=%d)",
+                            need / 1e9, budget / 1e9, N, L4, c->M);
+    // validate one-hot 0/1 entries (needed for the integer count kernels)
+    size_t n = (size_t)L4 * N;
+    int exact = 1;
+    for (size_t i = 0; i < n && exact; ++i) exact = onehot[i] == 0.f || onehot[i] == 1.f;
+    c->onehot_exact = exact;
+    CU_TRY(c, cudaMalloc((void**)&c->S, n * 4));
+    CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
+    int st = admm_alloc(c);
+    if (st == CDLGB_OK && c->fused) st = fused_setup(c);
+    if (st != CDLGB_OK) {
+        std::string msg = c->err;
+        cudaGetLastError();
+        admm_free(c);
+        fused_free(c);
+        cudaFree(c->S);
+        c->S = nullptr;
+        return cdlgb_seterr(c, st, "%s", msg.c_str());
+    }
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    c->loaded = true;
+    return CDLGB_OK;
+}
+
+int cdlgb_dims(const cdlgb_ctx* c, int32_t* L4, int32_t* N, int32_t* M, int32_t* gamma, int32_t* Lg) {
+    if (!c || !c->loaded) return CDLGB_ESTATE;
+    if (L4) *L4 = c->L4;
+    if (N) *N = c->N;
+    if (M) *M = c->M;
+    if (gamma) *gamma = c->gamma;
+    if (Lg) *Lg = c->Lg;
+    return CDLGB_OK;
+}
+
+#define NEED_LOADED(c)                                                                   \
+    do {                                                                                 \
+        if (!(c)) return CDLGB_EINVAL;                                                   \
+        if (!(c)->loaded) return cdlgb_seterr((c), CDLGB_ESTATE, "no data loaded");      \
+        CU_TRY((c), cudaSetDevice((c)->dev));                                            \
+    } while (0)
+#define NEED_INIT(c)                                                                     \
+    do {                                                                                 \
+        NEED_LOADED(c);                                                                  \
+        if (!(c)->initialized) return cdlgb_seterr((c), CDLGB_ESTATE, "state not initialised"); \
+    } while (0)
+
+int cdlgb_init_state(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
+    NEED_LOADED(c);
+    c->initialized = false;
+    return admm_init(c, X0, D0, seed);
+}
+
+int cdlgb_code_update(cdlgb_ctx* c, int32_t num_iter) {
+    NEED_INIT(c);
+    if (num_iter < 0) return cdlgb_seterr(c, CDLGB_EINVAL, "num_iter < 0");
+    return admm_code_update(c, num_iter);
+}
+
+int cdlgb_dict_update(cdlgb_ctx* c, int32_t num_iter) {
+    NEED_INIT(c);
+    if (num_iter < 0) return cdlgb_seterr(c, CDLGB_EINVAL, "num_iter < 0");
+    return admm_dict_update(c, num_iter);
+}
+
+int cdlgb_objective(cdlgb_ctx* c, double* obj) {
+    NEED_INIT(c);
+    if (!obj) return cdlgb_seterr(c, CDLGB_EINVAL, "obj is NULL");
+    return admm_objective(c, obj);
+}
+
+int cdlgb_update_best(cdlgb_ctx* c, double* obj, int32_t* improved) {
+    NEED_INIT(c);
+    int imp = 0;
+    ST_TRY(admm_update_best(c, obj, &imp));
+    if (improved) *improved = imp;
+    return CDLGB_OK;
+}
+
+int cdlgb_run_outer(cdlgb_ctx* c, int32_t iter_num, double* objs) {
+    NEED_INIT(c);
+    if (iter_num < 0) return cdlgb_seterr(c, CDLGB_EINVAL, "iter_num < 0");
+    for (int it = 0; it < iter_num; ++it) {
+        ST_TRY(admm_code_update(c, c->p.csc_iter_num));
+        double o = 0;
+        int imp = 0;
+        ST_TRY(admm_update_best(c, &o, &imp));
+        ST_TRY(admm_dict_update(c, c->p.cdl_iter_num));
+        if (objs) objs[it] = o;
+    }
+    return CDLGB_OK;
+}
+
+int cdlgb_code_threshold(cdlgb_ctx* c, double* thresh) {
+    NEED_INIT(c);
+    if (!thresh) return cdlgb_seterr(c, CDLGB_EINVAL, "thresh is NULL");
+    return admm_code_threshold(c, thresh);
+}
+
+int cdlgb_get(cdlgb_ctx* c, int32_t field, void* dst, size_t bytes) {
+    NEED_INIT(c);
+    if (!dst) return cdlgb_seterr(c, CDLGB_EINVAL, "dst is NULL");
+    const void* src = nullptr;
+    size_t want = 0;
+    const size_t LMN = c->LMN * 4, LN = c->LN * 4, LM = c->LM * 4;
+    switch (field) {
+        case CDLGB_FIELD_X: src = c->Xb[c->xcur]; want = LMN; break;
+        case CDLGB_FIELD_X_BEST: src = c->best_is_cur ? c->Xb[c->xcur] : c->Xb[1 - c->xcur]; want = LMN; break;
+        case CDLGB_FIELD_D: src = c->d; want = LMN; break;
+        case CDLGB_FIELD_D_BEST: src = c->Dbest; want = LM; break;
+        case CDLGB_FIELD_G1: src = c->G1; want = LM; break;
+        case CDLGB_FIELD_G3: src = c->G3; want = LM; break;
+        case CDLGB_FIELD_DX: src = c->DX; want = LN; break;
+        case CDLGB_FIELD_Y1: src = c->Y1; want = LN; break;
+        case CDLGB_FIELD_Y2_DUAL: src = c->y2; want = LMN; break;
+        case CDLGB_FIELD_Y3_DUAL: src = c->y3; want = LMN; break;
+        case CDLGB_FIELD_G1_DUAL: src = c->g1; want = LMN; break;
+        case CDLGB_FIELD_G3_DUAL: src = c->g3; want = LMN; break;
+        case CDLGB_FIELD_TD: src = c->Td; want = LN; break;
+        case CDLGB_FIELD_G2: src = c->G2; want = LN; break;
+        case CDLGB_FIELD_G2_DUAL: src = c->g2; want = LN; break;
+        case CDLGB_FIELD_Y1_DUAL: src = c->y1; want = LN; break;
+        case CDLGB_FIELD_OBJ_BEST:
+            if (bytes != sizeof(double)) return cdlgb_seterr(c, CDLGB_EINVAL, "obj_best is one float64");
+            *(double*)dst = c->obj_best;
+            return CDLGB_OK;
+        default: return cdlgb_seterr(c, CDLGB_EINVAL, "unknown field %d", field);
+    }
+    if (bytes != want)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "field %d is %zu bytes, got %zu", field, want, bytes);
+    CU_TRY(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    return CDLGB_OK;
+}
+
+int cdlgb_scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
+                   int32_t K, int32_t maxlen, int32_t* pos_out) {
+    NEED_LOADED(c);
+    if (!pos_out) return cdlgb_seterr(c, CDLGB_EINVAL, "pos_out is NULL");
+    return scan_fwd(c, pwms, lens, thresh, K, maxlen, pos_out);
+}
+
+int cdlgb_scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
+                    int32_t K, int32_t maxlen, int32_t* pos_out, float* score_out,
+                    uint8_t* use_comp_out) {
+    NEED_LOADED(c);
+    return scan_both(c, pwms, lens, thresh, K, maxlen, pos_out, score_out, use_comp_out);
+}
+
+int cdlgb_count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp,
+                     const int32_t* lens, int32_t K, int32_t maxlen, int32_t* counts_out,
+                     int32_t* nseq_out) {
+    NEED_LOADED(c);
+    return count_pfms(c, pos, use_comp, lens, K, maxlen, counts_out, nseq_out);
+}
+
+// ------------------------------------------------------------------ instrumentation
+int cdlgb_set_stream(cdlgb_ctx* c, void* stream) {
+    if (!c) return CDLGB_EINVAL;
+    CU_TRY(c, cudaSetDevice(c->dev));
+    if (c->stream) CU_TRY(c, cudaStreamSynchronize(c->stream));
+    if (stream) {
+        if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+        c->own_stream = false;
+        c->stream = (cudaStream_t)stream;
+    } else if (!c->own_stream) {
+        CU_TRY(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    return cdlgb_set_plan_streams(c);
+}
+
+int cdlgb_profile(cdlgb_ctx* c, int32_t enable) {
+    if (!c) return CDLGB_EINVAL;
+    if (!c->ring) return cdlgb_seterr(c, CDLGB_ECUDA, "no timing events available");
+    ring_collect(c);
+    c->profile = enable ? 1 : 0;
+    return CDLGB_OK;
+}
+
+int cdlgb_profile_read(cdlgb_ctx* c, double* ms, int64_t* counts, int64_t* launches,
+                       int64_t* fft_calls, int32_t reset) {
+    if (!c) return CDLGB_EINVAL;
+    ring_collect(c);
+    for (int i = 0; i < PH_COUNT; ++i) {
+        if (ms) ms[i] = c->ph_ms[i];
+        if (counts) counts[i] = c->ph_n[i];
+    }
+    if (launches) *launches = c->launches;
+    if (fft_calls) *fft_calls = c->fft_calls;
+    if (reset) {
+        for (int i = 0; i < PH_COUNT; ++i) { c->ph_ms[i] = 0; c->ph_n[i] = 0; }
+        c->launches = 0;
+        c->fft_calls = 0;
+    }
+    return CDLGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,153 @@
+// Internal declarations shared by the libcdlgb translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "cdlgb.h"
+
+// Per-phase timers (CUDA events on the context's stream), enabled on demand.
+enum cdlgb_phase {
+    PH_XSTEP = 0,     // one whole X-step iteration
+    PH_DSTEP,         // one whole D-step iteration
+    PH_OBJ,           // objective / update_best
+    PH_XFUSED,        // the fused X-step kernel alone
+    PH_DFUSED_A,      // fused D-step kernel, pass A
+    PH_DFUSED_B,      // fused D-step kernel, pass B
+    PH_SCAN,
+    PH_COUNT
+};
+
+struct cdlgb_ctx {
+    cdlgb_params p;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    char err[1024];
+
+    bool loaded = false, initialized = false;
+    int L4 = 0, N = 0, M = 0, gamma = 0, Lg = 0, F = 0;
+    size_t LMN = 0, LN = 0, LM = 0;
+    int fused = 0;                  // 1 when the fused in-kernel-FFT path is used
+
+    // one-hot data, (N, L4) == Julia (4L, N)
+    float* S = nullptr;
+    int onehot_exact = 0;
+
+    // LMN state
+    float* Xb[2] = {nullptr, nullptr};
+    int xcur = 0;                   // Xb[xcur] holds X
+    int best_is_cur = 1;            // X_best aliases Xb[xcur] (else Xb[1-xcur])
+    float *y2 = nullptr, *y3 = nullptr, *d = nullptr, *g1 = nullptr, *g3 = nullptr;
+    // LN state
+    float *Y1 = nullptr, *y1 = nullptr, *DX = nullptr, *Td = nullptr, *G2 = nullptr, *g2 = nullptr;
+    // LM state
+    float *G1 = nullptr, *G3 = nullptr, *dsum = nullptr, *Dbest = nullptr, *vbar = nullptr;
+    float2* G1h = nullptr;          // (M, F) rfft of G1
+    float* Ah = nullptr;            // (F) sum_m |G1h|^2
+
+    // scratch (cuFFT path)
+    float *sA = nullptr, *sB = nullptr;              // LMN real
+    float2 *sAh = nullptr, *sBh = nullptr, *sCh = nullptr;   // (N, M, F) spectra
+    float* sU = nullptr;                              // LN real
+    float2 *sUh = nullptr, *sVh = nullptr;            // (N, F)
+    float* part = nullptr;                            // D-step partial sums
+    int nchunk = 0;
+    double* dred = nullptr;                           // reduction partials (float64)
+    int nred = 0;
+    double* dscalar = nullptr;                        // device scalars
+    double* hscalar = nullptr;                        // pinned host mirror
+    double obj_best = 0.0;
+
+    // fused path twiddles / plan
+    void* fplan = nullptr;
+
+    cufftHandle pR2C_LMN = 0, pC2R_LMN = 0, pR2C_LN = 0, pC2R_LN = 0, pR2C_LM = 0;
+    bool plans = false;
+
+    // scan scratch
+    int32_t* scan_i = nullptr; size_t scan_i_cap = 0;
+    float* scan_f = nullptr; size_t scan_f_cap = 0;
+    uint8_t* scan_u = nullptr; size_t scan_u_cap = 0;
+
+    // instrumentation
+    int profile = 0;
+    void* ring = nullptr;           // event ring for the phase timers
+    double ph_ms[PH_COUNT] = {};
+    int64_t ph_n[PH_COUNT] = {};
+    int64_t launches = 0;           // our own kernel launches
+    int64_t fft_calls = 0;          // cuFFT exec calls
+};
+
+int cdlgb_seterr(cdlgb_ctx* c, int code, const char* fmt, ...);
+
+#define CU_TRY(c, call)                                                                 \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return cdlgb_seterr((c), CDLGB_ECUDA, "%s failed: %s (%s:%d)", #call,        \
+                                cudaGetErrorString(e_), __FILE__, __LINE__);            \
+    } while (0)
+
+#define FFT_TRY(c, call)                                                                \
+    do {                                                                                \
+        cufftResult r_ = (call);                                                        \
+        if (r_ != CUFFT_SUCCESS)                                                        \
+            return cdlgb_seterr((c), CDLGB_ECUDA, "%s failed: cufft status %d (%s:%d)",  \
+                                #call, (int)r_, __FILE__, __LINE__);                    \
+    } while (0)
+
+#define ST_TRY(call)                                                                    \
+    do {                                                                                \
+        int s_ = (call);                                                                \
+        if (s_ != CDLGB_OK) return s_;                                                  \
+    } while (0)
+
+// launch bookkeeping: checks the launch error of the kernel just issued
+int cdlgb_after_launch(cdlgb_ctx* c, const char* what);
+#define LAUNCH_CHECK(c, what) ST_TRY(cdlgb_after_launch((c), (what)))
+
+// phase timers
+void cdlgb_phase_begin(cdlgb_ctx* c, int ph);
+void cdlgb_phase_end(cdlgb_ctx* c, int ph);
+
+// ---- admm.cu ----
+int admm_alloc(cdlgb_ctx* c);
+void admm_free(cdlgb_ctx* c);
+int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed);
+int admm_code_update(cdlgb_ctx* c, int iters);
+int admm_dict_update(cdlgb_ctx* c, int iters);
+int admm_objective(cdlgb_ctx* c, double* obj);      // synchronous: result on host
+int admm_update_best(cdlgb_ctx* c, double* obj, int* improved);
+int admm_code_threshold(cdlgb_ctx* c, double* thr);
+size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused);
+int cdlgb_set_plan_streams(cdlgb_ctx* c);
+
+// ---- fused.cu ----
+int fused_supported(int Lg, int M);
+int fused_setup(cdlgb_ctx* c);
+void fused_free(cdlgb_ctx* c);
+int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs);
+int fused_dstep(cdlgb_ctx* c);
+size_t fused_scratch_bytes(int Lg, int M, int N);
+
+// ---- scan.cu ----
+int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
+             int K, int maxlen, int32_t* pos_out);
+int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
+              int K, int maxlen, int32_t* pos_out, float* score_out, uint8_t* comp_out);
+int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp,
+               const int32_t* lens, int K, int maxlen, int32_t* counts_out, int32_t* nseq_out);
+void scan_free(cdlgb_ctx* c);
+
+static inline unsigned grid_for(size_t n, int block, unsigned cap = 152u * 32u) {
+    size_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}

@@ -1,0 +1,295 @@
+// PWM scan and count kernels (src/SEARCH/scan.jl, src/SEARCH/helpers.jl).
+//
+// Scores are summed in float32 with one rounded multiply and one rounded add per
+// term (__fmul_rn / __fadd_rn: no FMA contraction), in the order of the reference
+// path being replaced, so positions and scores are bit-identical to it:
+//   greedy_search! (scan.jl:223-239): position-major, ind outer, nucleotide inner;
+//   scan_n (scan.jl:10-21):           nucleotide-major, j outer, k inner.
+#include "cdlgb_internal.h"
+
+#include <math.h>
+#include <vector>
+
+namespace {
+
+constexpr int kScanThreads = 256;
+
+// order-preserving reduction of (value, index): larger value wins, ties -> lower index
+struct VI { float v; int i; };
+__device__ __forceinline__ VI vi_best(VI a, VI b) {
+    bool take_b = (b.v > a.v) || (b.v == a.v && b.i < a.i);
+    return take_b ? b : a;
+}
+__device__ VI block_argmax(VI x, VI* sh) {
+    for (int o = 16; o > 0; o >>= 1) {
+        VI y;
+        y.v = __shfl_xor_sync(0xffffffffu, x.v, o);
+        y.i = __shfl_xor_sync(0xffffffffu, x.i, o);
+        x = vi_best(x, y);
+    }
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        x = lane < (int)(blockDim.x >> 5) ? sh[lane] : VI{-INFINITY, 0x7fffffff};
+        for (int o = 16; o > 0; o >>= 1) {
+            VI y;
+            y.v = __shfl_xor_sync(0xffffffffu, x.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, x.i, o);
+            x = vi_best(x, y);
+        }
+        if (lane == 0) sh[0] = x;
+    }
+    __syncthreads();
+    VI r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// one block per sequence n; loops over motifs k; threads over positions.
+// pwms: (K, 4, maxlen) col-major; out pos: (K, N) col-major.
+__global__ void k_scan_fwd(const float* __restrict__ data, const float* __restrict__ pwms,
+                           const int32_t* __restrict__ lens, const float* __restrict__ thresh,
+                           int K, int maxlen, int L, int32_t* __restrict__ pos) {
+    extern __shared__ float xs[];      // one-hot column, 4L floats
+    __shared__ VI red[32];
+    const int n = blockIdx.x;
+    const float* col = data + (size_t)n * 4 * L;
+    for (int i = threadIdx.x; i < 4 * L; i += blockDim.x) xs[i] = col[i];
+    __syncthreads();
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        const float th = thresh[k];
+        VI best{-INFINITY, 0x7fffffff};
+        for (int l = threadIdx.x; l < L; l += blockDim.x) {
+            float v = 0.f;
+            if (l <= L - w) {
+                float s = 0.f;
+                for (int ind = 0; ind < w; ++ind)
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+                        s = __fadd_rn(s, __fmul_rn(pwms[k + K * (a + 4 * ind)], xs[(l + ind) * 4 + a]));
+                v = s > th ? s : 0.f;
+            }
+            best = vi_best(best, VI{v, l});
+        }
+        VI r = block_argmax(best, red);
+        if (threadIdx.x == 0) pos[k + (size_t)K * n] = (r.i == 0) ? 0 : r.i + 1;
+    }
+}
+
+// scan_n on both strands; complement pwm_c[j, kk] = pwm[3-j, w-1-kk] (reverse of the
+// matrix).  Strict '>' from -Inf: NaN and -Inf never become the maximum.
+__global__ void k_scan_both(const float* __restrict__ data, const float* __restrict__ pwms,
+                            const int32_t* __restrict__ lens, const float* __restrict__ thresh,
+                            int K, int maxlen, int L, int32_t* __restrict__ pos,
+                            float* __restrict__ score, uint8_t* __restrict__ comp) {
+    extern __shared__ float xs[];
+    __shared__ VI red[32];
+    const int n = blockIdx.x;
+    const float* col = data + (size_t)n * 4 * L;
+    for (int i = threadIdx.x; i < 4 * L; i += blockDim.x) xs[i] = col[i];
+    __syncthreads();
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        VI bf{-INFINITY, 0x7fffffff}, bc{-INFINITY, 0x7fffffff};
+        for (int l = threadIdx.x; l <= L - w; l += blockDim.x) {
+            float sf = 0.f, sc = 0.f;
+            for (int j = 0; j < 4; ++j)
+                for (int kk = 0; kk < w; ++kk) {
+                    float x = xs[(l + kk) * 4 + j];
+                    sf = __fadd_rn(sf, __fmul_rn(pwms[k + K * (j + 4 * kk)], x));
+                    sc = __fadd_rn(sc, __fmul_rn(pwms[k + K * ((3 - j) + 4 * (w - 1 - kk))], x));
+                }
+            if (sf > -INFINITY) bf = vi_best(bf, VI{sf, l});
+            if (sc > -INFINITY) bc = vi_best(bc, VI{sc, l});
+        }
+        VI rf = block_argmax(bf, red);
+        VI rc = block_argmax(bc, red);
+        if (threadIdx.x == 0) {
+            // no candidate -> (-1, -Inf) as scan_n returns
+            float sF = rf.i == 0x7fffffff ? -INFINITY : rf.v;
+            float sC = rc.i == 0x7fffffff ? -INFINITY : rc.v;
+            int iF = rf.i == 0x7fffffff ? -1 : rf.i + 1;
+            int iC = rc.i == 0x7fffffff ? -1 : rc.i + 1;
+            bool fwd = sF >= sC;
+            float s = fwd ? sF : sC;
+            bool keep = s > thresh[k];
+            size_t o = k + (size_t)K * n;
+            if (pos) pos[o] = keep ? (fwd ? iF : iC) : 0;
+            if (score) score[o] = keep ? s : 0.f;
+            if (comp) comp[o] = (keep && !fwd) ? 1 : 0;
+        }
+    }
+}
+
+// integer count matrices: grid (K, chunks); counts (4, maxlen, K) col-major
+__global__ void k_count(const float* __restrict__ data, const int32_t* __restrict__ pos,
+                        const uint8_t* __restrict__ comp, const int32_t* __restrict__ lens, int K,
+                        int maxlen, int L, int N, int32_t* __restrict__ counts,
+                        int32_t* __restrict__ nseq) {
+    extern __shared__ int cnt[];       // 4*maxlen + 1
+    const int k = blockIdx.x;
+    const int w = lens[k];
+    for (int i = threadIdx.x; i < 4 * maxlen + 1; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    int per = (N + gridDim.y - 1) / gridDim.y;
+    int n0 = blockIdx.y * per, n1 = min(N, n0 + per);
+    for (int n = n0 + threadIdx.x; n < n1; n += blockDim.x) {
+        int p = pos[k + (size_t)K * n];
+        if (p <= 0) continue;
+        bool rc = comp && comp[k + (size_t)K * n];
+        const float* x = data + (size_t)n * 4 * L + (size_t)(p - 1) * 4;
+        for (int i = 0; i < w; ++i)
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+                int v = (int)(rc ? x[(w - 1 - i) * 4 + (3 - a)] : x[i * 4 + a]);
+                if (v) atomicAdd(&cnt[a + 4 * i], v);
+            }
+        atomicAdd(&cnt[4 * maxlen], 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * maxlen; i += blockDim.x)
+        if (cnt[i]) atomicAdd(&counts[i + (size_t)4 * maxlen * k], cnt[i]);
+    if (threadIdx.x == 0 && cnt[4 * maxlen]) atomicAdd(&nseq[k], cnt[4 * maxlen]);
+}
+
+template <typename T>
+int ensure(cdlgb_ctx* c, T** p, size_t* cap, size_t n) {
+    if (*cap >= n) return CDLGB_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    CU_TRY(c, cudaMalloc((void**)p, n * sizeof(T)));
+    *cap = n;
+    return CDLGB_OK;
+}
+
+int check_pwm_args(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
+                   int K, int maxlen) {
+    if (!c->loaded) return cdlgb_seterr(c, CDLGB_ESTATE, "no data loaded");
+    if (K <= 0 || maxlen <= 0 || !pwms || !lens || !thresh)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "scan: bad K=%d / maxlen=%d / null input", K, maxlen);
+    for (int k = 0; k < K; ++k)
+        if (lens[k] < 1 || lens[k] > maxlen)
+            return cdlgb_seterr(c, CDLGB_EINVAL, "scan: lens[%d]=%d outside 1..maxlen=%d", k,
+                                lens[k], maxlen);
+    return CDLGB_OK;
+}
+
+// device scratch layout: [pwms K*4*maxlen f32][thresh K f32] and [lens K i32][pos K*N i32]
+int upload_pwms(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh, int K,
+                int maxlen, size_t extra_i) {
+    size_t nf = (size_t)K * 4 * maxlen + K;
+    ST_TRY(ensure(c, &c->scan_f, &c->scan_f_cap, nf + (size_t)K * c->N));
+    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, (size_t)K + extra_i));
+    CU_TRY(c, cudaMemcpyAsync(c->scan_f, pwms, (size_t)K * 4 * maxlen * 4, cudaMemcpyHostToDevice,
+                              c->stream));
+    CU_TRY(c, cudaMemcpyAsync(c->scan_f + (size_t)K * 4 * maxlen, thresh, (size_t)K * 4,
+                              cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(c->scan_i, lens, (size_t)K * 4, cudaMemcpyHostToDevice, c->stream));
+    return CDLGB_OK;
+}
+
+}  // namespace
+
+int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh, int K,
+             int maxlen, int32_t* pos_out) {
+    ST_TRY(check_pwm_args(c, pwms, lens, thresh, K, maxlen));
+    const int N = c->N, L = c->L4 / 4;
+    cdlgb_phase_begin(c, PH_SCAN);
+    ST_TRY(upload_pwms(c, pwms, lens, thresh, K, maxlen, (size_t)K * N));
+    int32_t* dpos = c->scan_i + K;
+    size_t shm = (size_t)4 * L * sizeof(float);
+    if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
+    if (shm > 48 * 1024)
+        CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    k_scan_fwd<<<N, kScanThreads, shm, c->stream>>>(c->S, c->scan_f, c->scan_i,
+                                                     c->scan_f + (size_t)K * 4 * maxlen, K, maxlen,
+                                                     L, dpos);
+    LAUNCH_CHECK(c, "k_scan_fwd");
+    CU_TRY(c, cudaMemcpyAsync(pos_out, dpos, (size_t)K * N * 4, cudaMemcpyDeviceToHost, c->stream));
+    cdlgb_phase_end(c, PH_SCAN);
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    return CDLGB_OK;
+}
+
+int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh, int K,
+              int maxlen, int32_t* pos_out, float* score_out, uint8_t* comp_out) {
+    ST_TRY(check_pwm_args(c, pwms, lens, thresh, K, maxlen));
+    const int N = c->N, L = c->L4 / 4;
+    cdlgb_phase_begin(c, PH_SCAN);
+    ST_TRY(upload_pwms(c, pwms, lens, thresh, K, maxlen, (size_t)K * N));
+    ST_TRY(ensure(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));
+    int32_t* dpos = c->scan_i + K;
+    float* dscore = c->scan_f + (size_t)K * 4 * maxlen + K;
+    size_t shm = (size_t)4 * L * sizeof(float);
+    if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
+    if (shm > 48 * 1024)
+        CU_TRY(c, cudaFuncSetAttribute(k_scan_both, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    k_scan_both<<<N, kScanThreads, shm, c->stream>>>(c->S, c->scan_f, c->scan_i,
+                                                      c->scan_f + (size_t)K * 4 * maxlen, K,
+                                                      maxlen, L, dpos, dscore, c->scan_u);
+    LAUNCH_CHECK(c, "k_scan_both");
+    if (pos_out)
+        CU_TRY(c, cudaMemcpyAsync(pos_out, dpos, (size_t)K * N * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (score_out)
+        CU_TRY(c, cudaMemcpyAsync(score_out, dscore, (size_t)K * N * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (comp_out)
+        CU_TRY(c, cudaMemcpyAsync(comp_out, c->scan_u, (size_t)K * N, cudaMemcpyDeviceToHost, c->stream));
+    cdlgb_phase_end(c, PH_SCAN);
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    return CDLGB_OK;
+}
+
+int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp, const int32_t* lens,
+               int K, int maxlen, int32_t* counts_out, int32_t* nseq_out) {
+    if (!c->loaded) return cdlgb_seterr(c, CDLGB_ESTATE, "no data loaded");
+    if (!c->onehot_exact)
+        return cdlgb_seterr(c, CDLGB_ENOTSUP, "count_pfms needs 0/1 one-hot data");
+    if (K <= 0 || maxlen <= 0 || !pos || !lens || !counts_out)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "count_pfms: bad arguments");
+    const int N = c->N, L = c->L4 / 4;
+    for (int k = 0; k < K; ++k) {
+        if (lens[k] < 1 || lens[k] > maxlen)
+            return cdlgb_seterr(c, CDLGB_EINVAL, "count_pfms: lens[%d]=%d", k, lens[k]);
+        for (int n = 0; n < N; ++n) {
+            int p = pos[k + (size_t)K * n];
+            if (p < 0 || (p > 0 && p - 1 + lens[k] > L))
+                return cdlgb_seterr(c, CDLGB_EINVAL,
+                                    "count_pfms: window at pos[%d,%d]=%d (len %d) leaves the sequence (L=%d)",
+                                    k, n, p, lens[k], L);
+        }
+    }
+    size_t ncnt = (size_t)4 * maxlen * K;
+    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, (size_t)K + (size_t)K * N + ncnt + K));
+    ST_TRY(ensure(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));
+    int32_t* dlens = c->scan_i;
+    int32_t* dpos = c->scan_i + K;
+    int32_t* dcnt = dpos + (size_t)K * N;
+    int32_t* dnseq = dcnt + ncnt;
+    CU_TRY(c, cudaMemcpyAsync(dlens, lens, (size_t)K * 4, cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(dpos, pos, (size_t)K * N * 4, cudaMemcpyHostToDevice, c->stream));
+    if (use_comp)
+        CU_TRY(c, cudaMemcpyAsync(c->scan_u, use_comp, (size_t)K * N, cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, cudaMemsetAsync(dcnt, 0, (ncnt + K) * 4, c->stream));
+    int chunks = (N + 1023) / 1024;
+    if (chunks > 64) chunks = 64;
+    size_t shm = (size_t)(4 * maxlen + 1) * 4;
+    k_count<<<dim3(K, chunks), 256, shm, c->stream>>>(c->S, dpos, use_comp ? c->scan_u : nullptr,
+                                                      dlens, K, maxlen, L, N, dcnt, dnseq);
+    LAUNCH_CHECK(c, "k_count");
+    CU_TRY(c, cudaMemcpyAsync(counts_out, dcnt, ncnt * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (nseq_out)
+        CU_TRY(c, cudaMemcpyAsync(nseq_out, dnseq, (size_t)K * 4, cudaMemcpyDeviceToHost, c->stream));
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    return CDLGB_OK;
+}
+
+void scan_free(cdlgb_ctx* c) {
+    if (c->scan_i) cudaFree(c->scan_i);
+    if (c->scan_f) cudaFree(c->scan_f);
+    if (c->scan_u) cudaFree(c->scan_u);
+    c->scan_i = nullptr; c->scan_f = nullptr; c->scan_u = nullptr;
+    c->scan_i_cap = c->scan_f_cap = c->scan_u_cap = 0;
+}

@@ -1,0 +1,206 @@
+/*
+ * cdlgb.h -- C ABI of libcdlgb, the GB300 (sm_103a) implementation of the
+ * CDLmotif.jl convolutional-dictionary-learning hot path: the Fourier-domain ADMM
+ * (sparse-coding X-step, consensus dictionary D-step, best-iterate tracking) and
+ * the PWM scan / count stage that follows it.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Host arrays are caller-owned and use the
+ *     reference's Julia column-major layouts, so a Julia `ccall` can pass its
+ *     arrays as they are: "(a, b, c) col-major" means element (i, j, k) (0-based)
+ *     sits at i + a*(j + b*k).
+ *   - Device memory is owned by the library (one context = one dataset's ADMM
+ *     state, resident in HBM until cdlgb_destroy).
+ *   - Every call returns a cdlgb_status; 0 = OK, negative = error, with the
+ *     message available from cdlgb_last_error(ctx).  No call aborts the process
+ *     and no kernel traps.
+ *   - A context is used by one host thread at a time and owns its own CUDA stream.
+ *
+ * Reference interfaces replaced (paths within kchu25/CDLmotif.jl):
+ *   cdl ctor / init_cdl ............ src/SETUP/CDL_setup.jl:165-283
+ *   code_update! ................... src/CDL/train.jl:1-44
+ *   dict_update! ................... src/CDL/train.jl:46-89
+ *   update_best! ................... src/CDL/train.jl:91-98
+ *   objective ...................... src/SETUP/CDL_setup.jl:286
+ *   cdl_optimize inner loop ........ src/WRAPPER/wrap.jl:6-11
+ *   std(X_best[X_best .> 0]) ....... src/WRAPPER/wrap.jl:12
+ *   scan_w_gpu! / greedy_search! ... src/SEARCH/scan.jl:176-239
+ *   overlapping_scan! / scan_n ..... src/SEARCH/scan.jl:10-21, 89-121
+ *   posdicts2pfms (counts) ......... src/SEARCH/helpers.jl:59-96
+ *   save_pfms_as_transfac .......... src/SAVE/save_learned_results.jl:184-217
+ */
+#ifndef CDLGB_H
+#define CDLGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cdlgb_ctx cdlgb_ctx;
+
+typedef enum {
+    CDLGB_OK = 0,
+    CDLGB_EINVAL = -1,          /* bad argument or size */
+    CDLGB_ENOMEM_BUDGET = -2,   /* dataset does not fit the HBM budget (admission) */
+    CDLGB_ECUDA = -3,           /* a CUDA / cuFFT call failed */
+    CDLGB_ETIMEOUT = -4,        /* a bounded device wait gave up */
+    CDLGB_ESTATE = -5,          /* call out of order (e.g. no data loaded) */
+    CDLGB_ENOTSUP = -6          /* size or option not supported by this build */
+} cdlgb_status;
+
+/* Hyper-parameters: the fields of CDL_setup (src/SETUP/WRAPPER_setup.jl:1-13). */
+typedef struct {
+    int32_t M;                  /* number of filters (default 10) */
+    int32_t filter_size;        /* bases per filter; filter length = 4*filter_size (default 4) */
+    float rho;                  /* CSC penalty (default 100) */
+    float sigma;                /* CDL penalty (default 100) */
+    float lambda;               /* sparsity weight (default 0.01) */
+    int32_t csc_iter_num;       /* X-steps per outer iteration (default 15) */
+    int32_t cdl_iter_num;       /* D-steps per outer iteration (default 1) */
+    int32_t iter_num;           /* outer iterations (default 10) */
+    float std_threshold_multiplier; /* code threshold = multiplier * std (default 1) */
+    float sherman_const_csc;    /* code_update! keyword (default 2) */
+    float sherman_const_cdl;    /* dict_update! keyword (default 2) */
+    int32_t device;             /* CUDA device ordinal (default 0) */
+    int32_t init_mode;          /* D0 == NULL: 0 = random normal, unit norm per filter;
+                                   1 = the reference's simplex-per-base draw */
+    int32_t fft_mode;           /* 0 = auto (fused in-kernel FFT path where the size is
+                                   supported, else cuFFT transforms), 1 = cuFFT, 2 = fused */
+    uint64_t hbm_budget_bytes;  /* 0 = free device memory minus a 1 GiB margin */
+} cdlgb_params;
+
+/* Fields readable with cdlgb_get (sizes in elements; all float32 unless noted). */
+typedef enum {
+    CDLGB_FIELD_X = 0,          /* (Lg, M, N) col-major */
+    CDLGB_FIELD_X_BEST = 1,     /* (Lg, M, N) */
+    CDLGB_FIELD_D = 2,          /* consensus copies d, (Lg, M, N) */
+    CDLGB_FIELD_D_BEST = 3,     /* (Lg, M) */
+    CDLGB_FIELD_G1 = 4,         /* (Lg, M) */
+    CDLGB_FIELD_G3 = 5,         /* (Lg, M) */
+    CDLGB_FIELD_DX = 6,         /* (Lg, N) */
+    CDLGB_FIELD_Y1 = 7,         /* (Lg, N) */
+    CDLGB_FIELD_Y2_DUAL = 8,    /* y2, (Lg, M, N) */
+    CDLGB_FIELD_Y3_DUAL = 9,    /* y3, (Lg, M, N) */
+    CDLGB_FIELD_G1_DUAL = 10,   /* g1, (Lg, M, N) */
+    CDLGB_FIELD_G3_DUAL = 11,   /* g3, (Lg, M, N) */
+    CDLGB_FIELD_TD = 12,        /* (Lg, N) */
+    CDLGB_FIELD_G2 = 13,        /* (Lg, N) */
+    CDLGB_FIELD_G2_DUAL = 14,   /* g2, (Lg, N) */
+    CDLGB_FIELD_Y1_DUAL = 15,   /* y1, (Lg, N) */
+    CDLGB_FIELD_OBJ_BEST = 16   /* one float64 */
+} cdlgb_field;
+
+/* Fill *p with the CDL_setup defaults. */
+int cdlgb_params_default(cdlgb_params* p);
+
+/* Create a context on p->device.  Replaces nothing by itself: the reference has no
+ * handle; its state is the `cdl` struct built by init_cdl. */
+int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out);
+int cdlgb_destroy(cdlgb_ctx* ctx);
+const char* cdlgb_last_error(const cdlgb_ctx* ctx);
+
+/* Device memory a dataset of N sequences x L bases needs, for admission control. */
+int cdlgb_footprint(const cdlgb_params* p, int32_t L, int32_t N, uint64_t* bytes);
+
+/* Upload the one-hot data matrix (4L, N) col-major (dna2dummy layout,
+ * src/LOAD/to_dummy.jl:29-38; the reference's data_matrix_gpu).  Allocates the ADMM
+ * state; fails with CDLGB_ENOMEM_BUDGET if it does not fit. */
+int cdlgb_load_data(cdlgb_ctx* ctx, const float* onehot, int32_t L4, int32_t N);
+
+/* Dimensions of the loaded problem: L4 = 4L, gamma = 4*filter_size, Lg = L4 + 2*gamma. */
+int cdlgb_dims(const cdlgb_ctx* ctx, int32_t* L4, int32_t* N, int32_t* M,
+               int32_t* gamma, int32_t* Lg);
+
+/* init_cdl (src/SETUP/CDL_setup.jl:165-283).  X0: (Lg, M, N) col-major or NULL
+ * (standard normal from `seed`); D0: (Lg, M) or NULL (per init_mode, from `seed`).
+ * X0 is masked to rows (l-1) % 4 == 0 and D0 to the filter support, as the
+ * constructor does.  Computes DX, the auxiliaries and obj_best. */
+int cdlgb_init_state(cdlgb_ctx* ctx, const float* X0, const float* D0, uint64_t seed);
+
+/* code_update!(c, num_iter) -- src/CDL/train.jl:1-44. */
+int cdlgb_code_update(cdlgb_ctx* ctx, int32_t num_iter);
+
+/* dict_update!(c, num_iter) -- src/CDL/train.jl:46-89. */
+int cdlgb_dict_update(cdlgb_ctx* ctx, int32_t num_iter);
+
+/* objective(c, S) -- src/SETUP/CDL_setup.jl:286, accumulated in float64 on the GPU. */
+int cdlgb_objective(cdlgb_ctx* ctx, double* obj);
+
+/* update_best!(c, S) -- src/CDL/train.jl:91-98.  *improved (may be NULL) = 1 when
+ * X_best / D_best were replaced. */
+int cdlgb_update_best(cdlgb_ctx* ctx, double* obj, int32_t* improved);
+
+/* iter_num passes of cdl_optimize's loop body (src/WRAPPER/wrap.jl:6-11):
+ * code_update!(csc_iter_num); update_best!; dict_update!(cdl_iter_num).
+ * objs (may be NULL) receives the iter_num objective values. */
+int cdlgb_run_outer(cdlgb_ctx* ctx, int32_t iter_num, double* objs);
+
+/* std(X_best[X_best .> 0]) * multiplier -- src/WRAPPER/wrap.jl:12 (float64 on the GPU). */
+int cdlgb_code_threshold(cdlgb_ctx* ctx, double* thresh);
+
+/* Copy a state field to host memory; bytes must equal the field's size. */
+int cdlgb_get(cdlgb_ctx* ctx, int32_t field, void* host_dst, size_t bytes);
+
+/* scan_w_gpu! + greedy_search! (src/SEARCH/scan.jl:176-239) on the loaded data.
+ * pwms: (K, 4, maxlen) col-major, zero-padded past lens[k]; thresh: K.
+ * pos_out: (K, N) col-major, int32, 1-based argmax position of the thresholded
+ * forward-strand score, 0 = not found (a best hit at position 1 also reads 0,
+ * as in the reference).  Scores are summed in float32 in the reference's order. */
+int cdlgb_scan_fwd(cdlgb_ctx* ctx, const float* pwms, const int32_t* lens,
+                   const float* thresh, int32_t K, int32_t maxlen, int32_t* pos_out);
+
+/* overlapping_scan! (src/SEARCH/scan.jl:89-121, scan_n :10-21): both strands, the
+ * complement being `reverse(pwm)`.  pwms as above.  Outputs (K, N) col-major:
+ * pos_out 1-based (0 = no score above thresh[k]), score_out, use_comp_out (1 when
+ * the reverse complement won).  Any output pointer may be NULL. */
+int cdlgb_scan_both(cdlgb_ctx* ctx, const float* pwms, const int32_t* lens,
+                    const float* thresh, int32_t K, int32_t maxlen, int32_t* pos_out,
+                    float* score_out, uint8_t* use_comp_out);
+
+/* The count matrices behind posdicts2pfms (src/SEARCH/helpers.jl:59-96): for each
+ * motif k, the sum of the one-hot windows of length lens[k] at pos[k,n] (1-based,
+ * 0 = none), reverse-complemented where use_comp[k,n] != 0 (use_comp may be NULL).
+ * counts_out: (4, maxlen, K) col-major int32; nseq_out: K int32 (may be NULL). */
+int cdlgb_count_pfms(cdlgb_ctx* ctx, const int32_t* pos, const uint8_t* use_comp,
+                     const int32_t* lens, int32_t K, int32_t maxlen,
+                     int32_t* counts_out, int32_t* nseq_out);
+
+/* posdicts2pfms's normalisation (src/SEARCH/helpers.jl:66,87-88) in float32:
+ * ps = pseudocounts_r*n when smoothing, else (less_pseudocount ? 0.1 : pseudo_count);
+ * pfm = (count + ps) / (n + 4 ps).  pfm_out: (4, maxlen, K) col-major. Host only. */
+int cdlgb_counts_to_pfms(const int32_t* counts, const int32_t* nseq, const int32_t* lens,
+                         int32_t K, int32_t maxlen, float pseudocounts_r,
+                         float pseudo_count, int32_t smoothing, int32_t less_pseudocount,
+                         float* pfm_out);
+
+/* One transfac file body as save_pfms_as_transfac writes it
+ * (src/SAVE/save_learned_results.jl:186-196): pfm (4, w) col-major, values printed
+ * as pfm*1000 in Julia's shortest Float32 form.  reverse_complement != 0 writes the
+ * `_c` variant (reverse(pfm)).  Returns the byte count needed (excluding the NUL);
+ * writes at most cap bytes including a NUL.  Host only. */
+int64_t cdlgb_transfac_format(const float* pfm, int32_t w, int32_t reverse_complement,
+                              char* out, size_t cap);
+
+/* ---- Instrumentation and stream control.  No counterpart in the reference, which
+ * times phases with `@time` only (src/WRAPPER/wrap.jl:30,52,54,67,80,100,137). ---- */
+
+/* Run the context's work on an existing CUDA stream (cudaStream_t passed as void*),
+ * e.g. CUDA.jl's task stream; NULL returns to a stream owned by the context. */
+int cdlgb_set_stream(cdlgb_ctx* ctx, void* cuda_stream);
+
+/* Enable per-phase CUDA-event timers (X-step, D-step, objective, fused kernels, scan). */
+int cdlgb_profile(cdlgb_ctx* ctx, int32_t enable);
+
+/* Read the accumulated phase times: ms[8], counts[8] (order: X-step, D-step,
+ * objective, fused X kernel, fused D kernel pass A, pass B, scan, reserved),
+ * the number of this library's kernel launches and of cuFFT executions. */
+int cdlgb_profile_read(cdlgb_ctx* ctx, double* ms, int64_t* counts, int64_t* launches,
+                       int64_t* fft_calls, int32_t reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CDLGB_H */

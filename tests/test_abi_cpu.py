@@ -1,0 +1,85 @@
+"""CPU tests of the C ABI library: it loads, exports every symbol include/cdlgb.h
+declares, and its host-only functions (no GPU needed) match the oracle."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import search_oracle as SO
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "cdlgb.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(cdlgb_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    syms = header_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(built_lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(pkg, built_lib):
+    from cdlmotif_gb300 import _lib
+    assert set(header_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_params_default_match_cdl_setup(pkg, built_lib):
+    import ctypes as C
+    from cdlmotif_gb300._lib import CdlgbParams
+    p = CdlgbParams()
+    assert built_lib.cdlgb_params_default(C.byref(p)) == 0
+    # src/SETUP/WRAPPER_setup.jl:1-13
+    assert (p.M, p.filter_size, p.csc_iter_num, p.cdl_iter_num, p.iter_num) == (10, 4, 15, 1, 10)
+    assert (p.rho, p.sigma) == (100.0, 100.0)
+    assert p.lambda_ == pytest.approx(0.01)
+    assert (p.sherman_const_csc, p.sherman_const_cdl) == (2.0, 2.0)
+
+
+def test_transfac_c_matches_oracle(pkg, built_lib):
+    rng = np.random.default_rng(0)
+    for t in range(300):
+        w = int(rng.integers(1, 25))
+        pfm = rng.dirichlet(np.ones(4) * 0.7, size=w).T.astype(np.float32)
+        assert pkg.transfac_text(pfm) == SO.transfac_text(pfm)
+        assert pkg.transfac_text(pfm, True) == SO.transfac_text(SO.pwm_complement(pfm))
+
+
+def test_transfac_file_writer(pkg, built_lib, tmp_path):
+    pfms = [np.array([[0.25, 0.5], [0.25, 0.25], [0.25, 0.125], [0.25, 0.125]], np.float32),
+            np.array([[0.7], [0.1], [0.1], [0.1]], np.float32)]
+    pkg.save_pfms_as_transfac(str(tmp_path), pfms, [2, 1])
+    assert (tmp_path / "d1.transfac").read_text() == SO.transfac_text(pfms[1])
+    assert (tmp_path / "d2_c.transfac").read_text() == SO.transfac_text(SO.pwm_complement(pfms[0]))
+
+
+def test_counts_to_pfms_c_matches_oracle(pkg, built_lib):
+    import ctypes as C
+    from cdlmotif_gb300._lib import ptr
+    rng = np.random.default_rng(1)
+    K, maxlen = 5, 9
+    lens = rng.integers(3, maxlen + 1, K).astype(np.int32)
+    nseq = rng.integers(1, 5000, K).astype(np.int32)
+    counts = np.zeros((K, maxlen, 4), np.int32)
+    for k in range(K):
+        for i in range(lens[k]):
+            counts[k, i] = rng.multinomial(nseq[k], [0.25] * 4)
+    for smoothing, less in [(True, False), (False, False), (False, True)]:
+        out = np.zeros((K, maxlen, 4), np.float32)
+        st = built_lib.cdlgb_counts_to_pfms(ptr(counts, C.c_int32), ptr(nseq, C.c_int32),
+                                            ptr(lens, C.c_int32), K, maxlen, 0.0295, 5.0,
+                                            int(smoothing), int(less), ptr(out, C.c_float))
+        assert st == 0
+        ref = SO.counts_to_pfms(counts, nseq, lens, smoothing=smoothing, less_pseudocount=less)
+        for k in range(K):
+            np.testing.assert_array_equal(out[k, : lens[k]].T, ref[k])
+
+
+def test_golden_scan_pfms_from_counts(pkg, built_lib):
+    g = np.load(os.path.join(ROOT, "tests", "golden", "scan_small.npz"))
+    assert SO.transfac_text(g["pfms"][0, :, : g["lens"][0]]) == str(g["transfac"])

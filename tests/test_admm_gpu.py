@@ -1,0 +1,185 @@
+"""GPU parity of the ADMM (X-step, D-step, objective, best-iterate) against the
+FP64 oracle, through the C ABI.
+
+Tolerance (stated for the FP32-complex GPU path against the all-FP64 oracle after a
+fixed iteration count): X and d relative L2 <= 1e-4, objective relative <= 1e-5."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import cdl_oracle as O
+
+from conftest import random_onehot, rel
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL_X = 1e-4
+TOL_OBJ = 1e-5
+MODES = [1, 2]      # 1 = cuFFT transforms, 2 = fused in-kernel FFTs
+
+
+def _setup(pkg, M, fs, lam, rho, sigma, csc=15, cdl=1):
+    return pkg.CDLSetup(M=int(M), filter_size=int(fs), lambda_=float(lam), rho=float(rho),
+                        sigma=float(sigma), csc_iter_num=int(csc), cdl_iter_num=int(cdl))
+
+
+def _init(pkg, g, mode):
+    M, fs, lam, rho, sigma, outer, csc, cdl = g["params"]
+    setup = _setup(pkg, M, fs, lam, rho, sigma, csc, cdl)
+    try:
+        return pkg.init_cdl(setup, g["S"], X0=g["X0"], D0=g["D0"], fft_mode=mode), int(outer)
+    except pkg.CDLGBError as e:
+        if mode == 2 and e.status == -6:
+            pytest.skip("fused path does not cover this size")
+        raise
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("name", ["admm_tiny", "admm_small", "admm_refdefaults"])
+def test_golden_outer_iterations(pkg, built_lib, name, mode):
+    g = np.load(os.path.join(GOLD, name + ".npz"))
+    c, outer = _init(pkg, g, mode)
+    with c:
+        assert c.obj_best == pytest.approx(float(g["obj0"]), rel=TOL_OBJ)
+        objs = pkg.run_outer(c, outer)
+        np.testing.assert_allclose(objs, g["objs"], rtol=TOL_OBJ)
+        assert rel(c.X, g["X"]) < TOL_X
+        assert rel(c.d, g["d"]) < TOL_X
+        assert rel(c.G1, g["G1"]) < TOL_X
+        assert rel(c.DX, g["DX"]) < TOL_X
+        assert rel(c.X_best, g["X_best"]) < TOL_X
+        assert rel(c.D_best, g["D_best"]) < TOL_X
+        assert c.obj_best == pytest.approx(float(g["obj_best"]), rel=TOL_OBJ)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_steps_separately_against_oracle(pkg, built_lib, mode):
+    """code_update!, update_best! and dict_update! one at a time, every field."""
+    rng = np.random.default_rng(7)
+    N, L, M, fs = 20, 30, 5, 3
+    S, _ = random_onehot(rng, N, L)
+    Lg = 4 * L + 8 * fs
+    X0 = rng.standard_normal((N, M, Lg)).astype(np.float32)
+    D0 = rng.standard_normal((M, Lg)).astype(np.float32)
+    ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    setup = _setup(pkg, M, fs, 0.1, 1.0, 100.0)
+    try:
+        c = pkg.init_cdl(setup, S, X0=X0, D0=D0, fft_mode=mode)
+    except pkg.CDLGBError as e:
+        if mode == 2 and e.status == -6:
+            pytest.skip("fused path does not cover this size")
+        raise
+    with c:
+        assert rel(c.X, ref.X) < 1e-6 and rel(c.DX, ref.DX) < 1e-5 and rel(c.d, ref.d) < 1e-6
+        for step in range(3):
+            O.code_update(ref, 5)
+            pkg.code_update(c, 5)
+            for f in ("X", "y2", "y3", "y1", "Y1", "DX"):
+                assert rel(getattr(c, f), getattr(ref, f)) < TOL_X, f
+            o_ref, imp_ref = O.update_best(ref)
+            o, imp = pkg.update_best(c)
+            assert o == pytest.approx(o_ref, rel=TOL_OBJ) and imp == imp_ref
+            O.dict_update(ref, 1)
+            pkg.dict_update(c, 1)
+            for f in ("d", "g1", "g3", "G1", "G3", "Td", "G2", "g2"):
+                assert rel(getattr(c, f), getattr(ref, f)) < TOL_X, f
+        assert pkg.objective(c) == pytest.approx(O.objective(ref), rel=TOL_OBJ)
+        assert pkg.code_threshold(c) == pytest.approx(O.code_threshold(ref.X_best), rel=1e-4)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_config1_shape_parity(pkg, built_lib, mode):
+    """The N=1000/L=100/K=16/W=12 workload's shapes (Lg = 496 = 2^4 * 31) on 48
+    sequences with planted motifs, lambda 0.1, rho 1, 3 outer iterations."""
+    synth = pkg.synth
+    bases, _, _ = synth.plant_dataset(3, 48, 100, [10, 10], [0.3, 0.3])
+    S = synth.onehot(bases)
+    M, fs = 16, 12
+    Lg = 400 + 8 * fs
+    X0 = synth.init_X0(1, 48, M, Lg)
+    D0 = synth.init_D0_unit_norm(1, M, Lg, 4 * fs)
+    ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    objs_ref = O.run_outer(ref, 3)
+    try:
+        c = pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=mode)
+    except pkg.CDLGBError as e:
+        if mode == 2 and e.status == -6:
+            pytest.skip("fused path does not cover this size")
+        raise
+    with c:
+        objs = pkg.run_outer(c, 3)
+        np.testing.assert_allclose(objs, objs_ref, rtol=TOL_OBJ)
+        assert rel(c.X, ref.X) < TOL_X and rel(c.d, ref.d) < TOL_X
+        assert rel(c.D_best, ref.D_best) < TOL_X
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_deterministic(pkg, built_lib, mode):
+    rng = np.random.default_rng(9)
+    S, _ = random_onehot(rng, 33, 21)
+    setup = _setup(pkg, 7, 2, 0.1, 1.0, 100.0)
+    outs = []
+    for _ in range(2):
+        try:
+            c = pkg.init_cdl(setup, S, seed=123, fft_mode=mode)
+        except pkg.CDLGBError as e:
+            if mode == 2 and e.status == -6:
+                pytest.skip("fused path does not cover this size")
+            raise
+        with c:
+            pkg.run_outer(c, 2)
+            outs.append((c.X, c.d, c.G1))
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_modes_agree(pkg, built_lib):
+    rng = np.random.default_rng(10)
+    S, _ = random_onehot(rng, 40, 50)
+    setup = _setup(pkg, 8, 4, 0.1, 1.0, 100.0)
+    res = {}
+    for mode in MODES:
+        try:
+            c = pkg.init_cdl(setup, S, seed=5, fft_mode=mode)
+        except pkg.CDLGBError as e:
+            if mode == 2 and e.status == -6:
+                pytest.skip("fused path does not cover this size")
+            raise
+        with c:
+            pkg.run_outer(c, 2)
+            res[mode] = (c.X, c.d)
+    assert rel(res[1][0], res[2][0]) < TOL_X and rel(res[1][1], res[2][1]) < TOL_X
+
+
+def test_errors_are_reported(pkg, built_lib):
+    setup = _setup(pkg, 4, 2, 0.1, 1.0, 100.0)
+    c = pkg.CDL(setup)
+    with c:
+        with pytest.raises(pkg.CDLGBError) as e:
+            pkg.code_update(c, 1)          # nothing loaded
+        assert e.value.status == -5
+        with pytest.raises(pkg.CDLGBError) as e:
+            c.load_data(np.zeros((3, 10), np.float32))   # 4L not a multiple of 4
+        assert e.value.status == -1
+    # admission by HBM footprint
+    tiny = pkg.CDL(setup, hbm_budget_bytes=1024)
+    with tiny:
+        with pytest.raises(pkg.CDLGBError) as e:
+            tiny.load_data(np.zeros((10, 40), np.float32))
+        assert e.value.status == -2
+
+
+def test_profile_counts_launches(pkg, built_lib):
+    rng = np.random.default_rng(12)
+    S, _ = random_onehot(rng, 16, 20)
+    c = pkg.init_cdl(_setup(pkg, 4, 2, 0.1, 1.0, 100.0), S, seed=1)
+    with c:
+        c.profile(True)
+        c.profile_read(reset=True)
+        pkg.code_update(c, 3)
+        pkg.dict_update(c, 1)
+        pr = c.profile_read()
+        assert pr["xstep"][1] == 3 and pr["dstep"][1] == 1
+        assert pr["launches"] > 0 and pr["xstep"][0] > 0

@@ -1,0 +1,131 @@
+"""GPU parity of the PWM scans and count matrices: bit-exact against the oracle
+(same PWMs and thresholds -> identical positions, float32 scores, strands, integer
+counts and PFMs)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import search_oracle as SO
+
+from conftest import random_onehot
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _ctx(pkg, S):
+    c = pkg.CDL(pkg.CDLSetup(M=2, filter_size=2))
+    c.load_data(S)
+    return c
+
+
+def _random_pwms(rng, K, lo, hi):
+    lens = rng.integers(lo, hi, K).astype(np.int32)
+    pwms = []
+    for w in lens:
+        pfm = rng.dirichlet(0.4 * np.ones(4), size=int(w)).T
+        pfm = (pfm + 0.02) / 1.08
+        pwms.append(np.log2(pfm / 0.25).astype(np.float32))
+    thresh = np.array([0.3 * np.sum(np.max(p, axis=0)) for p in pwms], np.float32)
+    return pwms, lens, thresh
+
+
+def _pad(pwms, lens):
+    K, maxlen = len(lens), int(max(lens))
+    pw = np.zeros((K, 4, maxlen), np.float32)
+    for k in range(K):
+        pw[k, :, : lens[k]] = pwms[k][:, : lens[k]]
+    return pw
+
+
+def test_golden_scan(pkg, built_lib):
+    g = np.load(os.path.join(GOLD, "scan_small.npz"))
+    lens = g["lens"]
+    pwms = [g["pwms"][k, :, : lens[k]] for k in range(len(lens))]
+    with _ctx(pkg, g["S"]) as c:
+        pos_fwd = pkg.scan_w_gpu(c, pwms, g["thresh"])
+        np.testing.assert_array_equal(pos_fwd.T, g["pos_fwd"])
+        pos, score, comp = pkg.overlapping_scan(c, pwms, g["thresh"])
+        np.testing.assert_array_equal(pos.T, g["pos"])
+        np.testing.assert_array_equal(score.T, g["score"])
+        np.testing.assert_array_equal(comp.T, g["comp"])
+        counts, nseq = pkg.count_matrices(c, pos, lens, comp)
+        np.testing.assert_array_equal(counts, g["counts"])
+        np.testing.assert_array_equal(nseq, g["nseq"])
+        pfms = pkg.posdicts2pfms(c, pos, lens, comp)
+        for k in range(len(lens)):
+            np.testing.assert_array_equal(pfms[k], g["pfms"][k, :, : lens[k]])
+
+
+@pytest.mark.parametrize("N,L,K", [(300, 200, 8), (64, 100, 20), (7, 31, 3)])
+def test_scans_bit_exact_random(pkg, built_lib, N, L, K):
+    rng = np.random.default_rng(N + L + K)
+    S, _ = random_onehot(rng, N, L)
+    pwms, lens, thresh = _random_pwms(rng, K, 4, 21)
+    with _ctx(pkg, S) as c:
+        pos_fwd = pkg.scan_w_gpu(c, pwms, thresh)
+        ref_fwd = SO.scan_w_gpu_positions(_pad(pwms, lens), S, lens, thresh)
+        np.testing.assert_array_equal(pos_fwd.T, ref_fwd)
+        pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+        rp, rs, rc = SO.overlapping_scan(S, pwms, lens, thresh)
+        np.testing.assert_array_equal(pos.T, rp)
+        np.testing.assert_array_equal(score.T, rs)
+        np.testing.assert_array_equal(comp.T, rc)
+        counts, nseq = pkg.count_matrices(c, pos, lens, comp)
+        rcnt, rn = SO.count_matrices(S, rp, rc, lens)
+        np.testing.assert_array_equal(counts, rcnt)
+        np.testing.assert_array_equal(nseq, rn)
+
+
+def test_scan_edge_cases(pkg, built_lib):
+    rng = np.random.default_rng(3)
+    N, L = 12, 9
+    S, _ = random_onehot(rng, N, L)
+    pwms = [np.log2(rng.dirichlet(np.ones(4), size=w).T / 0.25 + 1e-3).astype(np.float32)
+            for w in (12, 9, 1, 4)]                      # longer than L, == L, width 1
+    lens = np.array([12, 9, 1, 4], np.int32)
+    for thresh in (np.array([0, 0, 0, 0], np.float32), np.array([-50, -50, -50, -50], np.float32),
+                   np.array([1e9] * 4, np.float32)):
+        with _ctx(pkg, S) as c:
+            pos_fwd = pkg.scan_w_gpu(c, pwms, thresh)
+            np.testing.assert_array_equal(pos_fwd.T, SO.scan_w_gpu_positions(_pad(pwms, lens), S, lens, thresh))
+            pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+            rp, rs, rc = SO.overlapping_scan(S, pwms, lens, thresh)
+            np.testing.assert_array_equal(pos.T, rp)
+            np.testing.assert_array_equal(score.T, rs)
+            np.testing.assert_array_equal(comp.T, rc)
+
+
+def test_scan_ties_first_position(pkg, built_lib):
+    """Repeated motif occurrences: equal scores resolve to the first position, and a
+    best hit at position 1 reads 0 in scan_w_gpu (scan.jl:197)."""
+    L = 20
+    seq = "ACGTACGTACGTACGTACGT"
+    S = np.zeros((2, 4 * L), np.float32)
+    for i, ch in enumerate(seq):
+        S[0, 4 * i + "ACGT".index(ch)] = 1
+    for i, ch in enumerate("TT" + seq[:-2]):
+        S[1, 4 * i + "ACGT".index(ch)] = 1
+    pwm = np.full((4, 4), -1.0, np.float32)
+    for i, ch in enumerate("ACGT"):
+        pwm["ACGT".index(ch), i] = 1.0
+    th = np.array([0.5], np.float32)
+    with _ctx(pkg, S) as c:
+        pos = pkg.scan_w_gpu(c, [pwm], th)
+        assert pos[0, 0] == 0 and pos[1, 0] == 3
+        p2, s2, c2 = pkg.overlapping_scan(c, [pwm], th)
+        rp, rs, rc = SO.overlapping_scan(S, [pwm], [4], th)
+        np.testing.assert_array_equal(p2.T, rp)
+        assert p2[0, 0] == 1
+
+
+def test_count_rejects_out_of_range_window(pkg, built_lib):
+    rng = np.random.default_rng(4)
+    S, _ = random_onehot(rng, 3, 10)
+    with _ctx(pkg, S) as c:
+        pos = np.array([[8], [1], [0]], np.int32)     # window of 4 at base 8 leaves L=10
+        with pytest.raises(pkg.CDLGBError) as e:
+            pkg.count_matrices(c, pos, [4])
+        assert e.value.status == -1

@@ -1,0 +1,364 @@
+"""Benchmark: outer ADMM iterations/s of CDLmotif's CDL hot path on one GB300.
+
+Workload (the headline configuration): N = 20000 sequences of L = 200 bases,
+one-hot float32 (4 channels), 5 planted motifs of widths 8..20 (Dirichlet(0.1)
+columns, 10..40 % occupancy, random strand), K = M = 64 filters of 16 bases
+(Lg = 4L + 8W = 928), lambda 0.1, rho 1, sigma 100.  One step = one outer ADMM
+iteration of cdl_optimize (src/WRAPPER/wrap.jl:6-11): 15 X-steps, update_best!,
+1 D-step.
+
+  value  device-resident: state and data already in HBM.
+  e2e    through the public C ABI with host buffers: every step uploads the one-hot
+         data from pinned host memory (cdlgb_load_data), initialises the state
+         (cdlgb_init_state), runs E outer iterations (cdlgb_run_outer) and reads the
+         objectives and D_best back; the unit is the same (outer iterations/s).
+
+``--impl reference`` times the CPU restatement of the reference (the oracle: an
+FP64 NumPy port of src/CDL/train.jl, the reference having no host path of its own
+and Julia being absent) with a process per host core, each on its own slice of
+the sequences, and reports the same metric scaled to the full N.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="plain_n20000_l200_k64", N=20000, L=200, M=64, filter_size=16,
+                widths=[8, 11, 14, 17, 20], occ=[0.1, 0.175, 0.25, 0.325, 0.4],
+                lam=0.1, rho=1.0, sigma=100.0, csc_iter=15, cdl_iter=1, seed=2024)
+METRIC = "ADMM outer iterations/s at N=20k, L=200, K=64 (15 X-steps + update_best + 1 D-step)"
+UNIT = "outer_iter/s"
+
+
+def _pkg():
+    import __graft_entry__ as ge
+    return ge._pkg()
+
+
+def dataset(wl=WORKLOAD, N=None):
+    from importlib import import_module  # noqa: F401
+    pkg = _pkg()
+    n = wl["N"] if N is None else N
+    bases, _, _ = pkg.synth.plant_dataset(wl["seed"], wl["N"], wl["L"], wl["widths"], wl["occ"])
+    return bases[:n]
+
+
+def algorithmic_bytes(wl=WORKLOAD):
+    """Minimum HBM traffic per outer iteration and per X-step / D-step (state read
+    and written once per step, FP32): X-step 24 B per (l,m,n) + 28 B per (l,n);
+    D-step 32 B per (l,m,n) + 24 B per (l,n); objective 4 B per (l,m,n) + 4 per (l,n)."""
+    Lg = 4 * wl["L"] + 8 * wl["filter_size"]
+    LMN = Lg * wl["M"] * wl["N"]
+    LN = Lg * wl["N"]
+    bx = 24 * LMN + 28 * LN
+    bd = 32 * LMN + 24 * LN
+    bo = 4 * LMN + 4 * LN
+    return dict(Lg=Lg, LMN=LMN, LN=LN, xstep=bx, dstep=bd, obj=bo,
+                outer=wl["csc_iter"] * bx + wl["cdl_iter"] * bd + bo)
+
+
+# ------------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+# ------------------------------------------------------------------------ CPU leg
+def _cpu_worker(args):
+    """Run the oracle on a slice of sequences: W + K outer iterations, each between
+    two barrier waits so the parent can time the step across all workers."""
+    bases, wl, barrier, steps, warmup = args
+    from oracle import cdl_oracle as O
+    N, L = bases.shape
+    S = np.zeros((N, L, 4), np.float32)
+    S[np.arange(N)[:, None], np.arange(L)[None], bases] = 1
+    S = S.reshape(N, 4 * L)
+    Lg = 4 * L + 8 * wl["filter_size"]
+    rng = np.random.default_rng(1)
+    X0 = rng.standard_normal((N, wl["M"], Lg)).astype(np.float32)
+    D0 = rng.standard_normal((wl["M"], Lg)).astype(np.float32)
+    c = O.init_cdl(S, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"], X0=X0, D0=D0)
+    for _ in range(warmup + steps):
+        if barrier is not None:
+            barrier.wait()
+        O.code_update(c, wl["csc_iter"])
+        O.update_best(c)
+        O.dict_update(c, wl["cdl_iter"])
+        if barrier is not None:
+            barrier.wait()
+    return True
+
+
+def cpu_reference(steps: int, warmup: int, procs: int, per_proc: int):
+    """Times the oracle with `procs` processes of `per_proc` sequences each; returns
+    (outer iterations/s scaled to the full N, ms per sample step, sample text)."""
+    wl = WORKLOAD
+    bases = dataset(wl, N=procs * per_proc)
+    if procs == 1:
+        from oracle import cdl_oracle  # noqa: F401
+        times = []
+        import threading  # noqa: F401
+
+        class _B:
+            def wait(self):
+                times.append(time.perf_counter())
+        _cpu_worker((bases, wl, _B(), steps, warmup))
+        t = np.diff(np.array(times))[0::2][warmup:]
+    else:
+        ctx = mp.get_context("spawn")
+        barrier = ctx.Manager().Barrier(procs + 1)
+        with ctx.Pool(procs) as pool:
+            res = pool.map_async(_cpu_worker, [(bases[i * per_proc:(i + 1) * per_proc], wl, barrier,
+                                                steps, warmup) for i in range(procs)])
+            t = []
+            for s in range(warmup + steps):
+                barrier.wait()
+                t0 = time.perf_counter()
+                barrier.wait()
+                if s >= warmup:
+                    t.append(time.perf_counter() - t0)
+            res.get()
+        t = np.array(t)
+    sec = float(np.mean(t))
+    seqs = procs * per_proc
+    rate = 1.0 / (sec * wl["N"] / seqs)
+    sample = (f"{seqs} of {wl['N']} sequences ({procs} process(es) x {per_proc}), one outer "
+              f"iteration per step, FP64 NumPy oracle; rate scaled by N/{seqs}")
+    return rate, sec * 1e3, sample
+
+
+# ------------------------------------------------------------------------ GPU leg
+def run_gpu(args, rank: int, world: int):
+    import torch
+    pkg = _pkg()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = WORKLOAD
+    bases = dataset(wl)
+    S = pkg.synth.onehot(bases)
+    setup = pkg.CDLSetup(M=wl["M"], filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
+                         sigma=wl["sigma"], csc_iter_num=wl["csc_iter"], cdl_iter_num=wl["cdl_iter"])
+    stream = torch.cuda.current_stream(dev)
+    c = pkg.CDL(setup, device=dev, fft_mode=args.fft_mode)
+    c.set_stream(stream.cuda_stream)
+    # pinned host copy of the inputs for the end-to-end leg
+    S_pin_t = torch.empty(S.shape, dtype=torch.float32, pin_memory=True)
+    S_pin = S_pin_t.numpy()
+    S_pin[...] = S
+    c.load_data(S_pin)
+    c.init_state(seed=wl["seed"])
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- device-resident leg
+    for _ in range(args.warmup):
+        pkg.run_outer(c, 1)
+    c.profile(True)
+    c.profile_read(reset=True)
+    sampler = ClockSampler(dev)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        pkg.run_outer(c, 1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    prof = c.profile_read(reset=True)
+    c.profile(False)
+    ms_t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{dev}")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # ---- end-to-end leg through the C ABI with host buffers
+    E = args.e2e_outer
+    for _ in range(max(1, args.warmup // 2)):
+        c.load_data(S_pin)
+        c.init_state(seed=wl["seed"])
+        pkg.run_outer(c, E)
+        c.get("D_best")
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_steps = max(2, args.steps // 2)
+    for _ in range(e_steps):
+        c.load_data(S_pin)                   # H2D of the step's inputs
+        c.init_state(seed=wl["seed"])
+        pkg.run_outer(c, E)                  # objectives come back to the host
+        Db = c.get("D_best")                 # D2H of the learned filters
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    te = torch.tensor([t_e2e], dtype=torch.float64, device=f"cuda:{dev}")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * e_steps * E / float(te.item())
+    h2d = S.nbytes
+    d2h = Db.nbytes + 8 * E
+    fused = bool(c._p.fft_mode != 1) and prof["xfused"][1] > 0
+    c.close()
+    return dict(value=value, ms=ms_max, clocks=clocks, prof=prof, e2e=e2e_value, h2d=h2d, d2h=d2h,
+                fused=fused)
+
+
+def roofline(prof, steps, fused):
+    """Roofline of the dominant kernel, from the phase timers recorded (CUDA events on
+    the launching stream) during the timed region."""
+    ab = algorithmic_bytes()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not peak:
+        peak, peak_src = 6800.0, "fallback"
+    if fused and prof["xfused"][1] > 0:
+        ms_avg = prof["xfused"][0] / prof["xfused"][1]
+        kernel = "fused X-step kernel (k_xstep_fused)"
+    else:
+        ms_avg = prof["xstep"][0] / max(prof["xstep"][1], 1)
+        kernel = "X-step (cuFFT path: k_xprep + R2C + k_xsolve + C2R + k_mask_update)"
+    achieved = ab["xstep"] / (ms_avg / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
+            "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "traffic": None, "algorithmic_bytes_per_launch": ab["xstep"],
+            "avg_launch_ms": round(ms_avg, 4)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--fft-mode", type=int, default=0, help="0 auto, 1 cuFFT, 2 fused")
+    ap.add_argument("--e2e-outer", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    wl = WORKLOAD
+    config = {"workload": wl["name"], "N": wl["N"], "L": wl["L"], "K": wl["M"],
+              "filter_size": wl["filter_size"], "Lg": algorithmic_bytes()["Lg"], "lambda": wl["lam"],
+              "rho": wl["rho"], "sigma": wl["sigma"], "csc_iter_num": wl["csc_iter"],
+              "cdl_iter_num": wl["cdl_iter"], "parallelism": f"replicas{world}",
+              "l2": "inputs larger than L2 (ADMM state ~28 GB per replica)"}
+
+    if args.impl == "reference":
+        if world > 1 and rank != 0:
+            return
+        procs = os.cpu_count() or 1
+        rate, ms, sample = cpu_reference(args.steps, args.warmup, procs, per_proc=2)
+        line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / rate,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded planted motifs)", "config": config, "impl": "reference",
+                "cpu_baseline": {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
+                                 "sample": sample, "sample_ms_per_step": ms},
+                "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    # the CPU baseline runs before any GPU call, single process, bounded sample
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        per = 2
+        r1, ms1, _ = cpu_reference(1, 0, 1, per)
+        k = max(1, int(args.cpu_seconds / max(ms1 / 1e3, 1e-3)))
+        rate, ms, sample = cpu_reference(min(k, 20), 0, 1, per)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+    r = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    prof = r["prof"]
+    launches = prof["launches"]
+    line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded planted motifs, Dirichlet(0.1) PWMs)", "config": config,
+            "clocks": r["clocks"],
+            "e2e": {"value": r["e2e"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"], "outer_iterations_per_step": args.e2e_outer},
+            "gpu_launches": launches,
+            "library_calls": {"cufft_exec": prof["fft_calls"]},
+            "roofline": roofline(prof, args.steps, r["fused"]),
+            "phases_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in prof.items()
+                                   if isinstance(v, tuple) and v[1]},
+            "path": "fused" if r["fused"] else "cufft",
+            "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -70,6 +70,31 @@ void cdlgb_phase_end(cdlgb_ctx* c, int ph) {
     r->open[ph] = -1;
 }
 
+// one-hot validation on the device: every entry must be 0 or 1 (the integer count
+// kernels rely on it).  Sets c->onehot_exact; synchronises the stream.
+__global__ void k_check_onehot(const float4* __restrict__ S, size_t n4, int* __restrict__ bad) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = S[i];
+        bool ok = (v.x == 0.f || v.x == 1.f) && (v.y == 0.f || v.y == 1.f) &&
+                  (v.z == 0.f || v.z == 1.f) && (v.w == 0.f || v.w == 1.f);
+        if (!ok) *bad = 1;
+    }
+}
+
+static int check_onehot(cdlgb_ctx* c) {
+    int* flag = (int*)c->dscalar;      // 8 doubles of device scratch, first int used here
+    CU_TRY(c, cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
+    size_t n4 = (size_t)c->L4 * c->N / 4;
+    k_check_onehot<<<grid_for(n4, 256), 256, 0, c->stream>>>((const float4*)c->S, n4, flag);
+    LAUNCH_CHECK(c, "k_check_onehot");
+    int hbad = 0;
+    CU_TRY(c, cudaMemcpyAsync(&hbad, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    c->onehot_exact = hbad == 0;
+    return CDLGB_OK;
+}
+
 extern "C" {
 
 int cdlgb_params_default(cdlgb_params* p) {
@@ -178,6 +203,13 @@ int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
     // CDL_setup.jl:174
     if (L4 % 4) return cdlgb_seterr(c, CDLGB_EINVAL, "first dimension of dat must be multiple of 4s (got %d)", L4);
     CU_TRY(c, cudaSetDevice(c->dev));
+    if (c->loaded && c->L4 == L4 && c->N == N) {
+        // same shape as the resident dataset: keep every buffer and plan, replace the data
+        size_t n = (size_t)L4 * N;
+        CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
+        c->initialized = false;
+        return check_onehot(c);
+    }
     if (c->loaded) {
         CU_TRY(c, cudaStreamSynchronize(c->stream));
         admm_free(c);
@@ -210,11 +242,7 @@ int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
         return cdlgb_seterr(c, CDLGB_ENOMEM_BUDGET,
                             "dataset needs %.2f GB of device memory, budget is %.2f GB (N=%d, 4L=%d, M=%d)",
                             need / 1e9, budget / 1e9, N, L4, c->M);
-    // validate one-hot 0/1 entries (needed for the integer count kernels)
     size_t n = (size_t)L4 * N;
-    int exact = 1;
-    for (size_t i = 0; i < n && exact; ++i) exact = onehot[i] == 0.f || onehot[i] == 1.f;
-    c->onehot_exact = exact;
     CU_TRY(c, cudaMalloc((void**)&c->S, n * 4));
     CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
     int st = admm_alloc(c);
@@ -228,9 +256,8 @@ int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
         c->S = nullptr;
         return cdlgb_seterr(c, st, "%s", msg.c_str());
     }
-    CU_TRY(c, cudaStreamSynchronize(c->stream));
     c->loaded = true;
-    return CDLGB_OK;
+    return check_onehot(c);
 }
 
 int cdlgb_dims(const cdlgb_ctx* c, int32_t* L4, int32_t* N, int32_t* M, int32_t* gamma, int32_t* Lg) {

@@ -358,13 +358,13 @@ __global__ void k_fit(const float* __restrict__ DX, const float* __restrict__ S,
     if (threadIdx.x == 0) out[blockIdx.x] = acc;
 }
 
-// out[0] = 0.5 * sum(part[nb1..nb1+nb2)) + lam * sum(part[0..nb1))
-__global__ void k_obj_final(const double* __restrict__ part, int nb1, int nb2, double lam,
-                            double* __restrict__ out) {
+// out[0] = 0.5 * sum(pb[0..nb2)) + lam * sum(pa[0..nb1))
+__global__ void k_obj_final(const double* __restrict__ pa, int nb1, const double* __restrict__ pb,
+                            int nb2, double lam, double* __restrict__ out) {
     __shared__ double sh[32];
     double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < nb1; i += blockDim.x) a += part[i];
-    for (int i = threadIdx.x; i < nb2; i += blockDim.x) b += part[nb1 + i];
+    for (int i = threadIdx.x; i < nb1; i += blockDim.x) a += pa[i];
+    for (int i = threadIdx.x; i < nb2; i += blockDim.x) b += pb[i];
     a = block_sum_d(a, sh);
     b = block_sum_d(b, sh);
     if (threadIdx.x == 0) out[0] = 0.5 * b + lam * a;
@@ -486,12 +486,9 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     b += 8 * LN * 4;                            // Y1 y1 DX Td G2 g2 + 2 scratch
     b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
     b += 2 * N * F * 8;                         // LN spectra
-    if (fused) {
-        b += fused_scratch_bytes((int)Lg, (int)M, N);
-    } else {
-        b += 2 * LMN * 4 + 3 * (size_t)N * M * F * 8;   // cuFFT-path scratch
-        b += LMN * 4 / 2;                               // cuFFT work area (estimate)
-    }
+    if (fused) b += fused_scratch_bytes((int)Lg, (int)M, N);
+    b += 2 * LMN * 4 + 3 * (size_t)N * M * F * 8;       // cuFFT-path scratch (D-step)
+    b += LMN * 4 / 2;                                   // cuFFT work area (estimate)
     b += 64ull * 3 * LM * 4;                    // D-step partials
     b += (64u << 20);                           // reductions, scan scratch, slack
     return b;
@@ -529,11 +526,9 @@ int admm_alloc(cdlgb_ctx* c) {
     // spectra of the whole dataset are needed at init (DX) and by the cuFFT path
     ST_TRY(A((void**)&c->sA, LMN * 4));
     ST_TRY(A((void**)&c->sAh, (size_t)c->N * c->M * c->F * 8));
-    if (!c->fused) {
-        ST_TRY(A((void**)&c->sB, LMN * 4));
-        ST_TRY(A((void**)&c->sBh, (size_t)c->N * c->M * c->F * 8));
-        ST_TRY(A((void**)&c->sCh, (size_t)c->N * c->M * c->F * 8));
-    }
+    ST_TRY(A((void**)&c->sB, LMN * 4));
+    ST_TRY(A((void**)&c->sBh, (size_t)c->N * c->M * c->F * 8));
+    ST_TRY(A((void**)&c->sCh, (size_t)c->N * c->M * c->F * 8));
     c->nchunk = std::max(1, std::min(64, c->N));
     ST_TRY(A((void**)&c->part, (size_t)c->nchunk * 3 * LM * 4));
     c->nred = 152 * 4;
@@ -571,6 +566,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     const size_t LMN = c->LMN, LN = c->LN, LM = c->LM;
     c->xcur = 0;
     c->best_is_cur = 1;
+    c->absx_fused = 0;
     float* X = c->Xb[0];
     // X0 (CDL_setup.jl:191-192): given, or standard normal; then masked to the 4-stride
     if (X0) {
@@ -651,7 +647,9 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
         float* Xout = c->best_is_cur ? c->Xb[1 - c->xcur] : Xin;
         if (c->fused) {
             ST_TRY(fused_xstep(c, Xin, Xout, 0));
+            c->absx_fused = 1;
         } else {
+            c->absx_fused = 0;
             k_xprep<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>(
                 (const float4*)Xin, (float4*)c->y2, (float4*)c->y3, (float4*)c->sA, LMN / 4,
                 c->p.lambda);
@@ -687,9 +685,7 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
     const int F = c->F, M = c->M, N = c->N, Lg = c->Lg;
     for (int it = 0; it < iters; ++it) {
         cdlgb_phase_begin(c, PH_DSTEP);
-        if (c->fused) {
-            ST_TRY(fused_dstep(c));
-        } else {
+        {
             k_dprep<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>(
                 (const float4*)cur_X(c), (const float4*)c->y3, (const float4*)c->g1,
                 (const float4*)c->g3, (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA,
@@ -735,12 +731,22 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
 static int objective_async(cdlgb_ctx* c) {
     cudaStream_t s = c->stream;
     int nb1 = 152 * 2, nb2 = 152;
-    k_abssum<<<nb1, kBlock, 0, s>>>((const float4*)cur_X(c), c->LMN / 4, c->dred);
-    LAUNCH_CHECK(c, "k_abssum");
+    const double* pa = c->dred;
+    const double* fp = nullptr;
+    int nf = 0;
+    if (c->absx_fused && fused_absx(c, &fp, &nf)) {
+        // sum |X| came with the last fused X-step
+        pa = fp;
+        nb1 = nf;
+    } else {
+        k_abssum<<<nb1, kBlock, 0, s>>>((const float4*)cur_X(c), c->LMN / 4, c->dred);
+        LAUNCH_CHECK(c, "k_abssum");
+    }
     k_fit<<<nb2, kBlock, 0, s>>>(c->DX, c->S, c->Lg, c->L4, c->gamma, (size_t)c->N * c->L4,
-                                 c->dred + nb1);
+                                 c->dred + 152 * 2);
     LAUNCH_CHECK(c, "k_fit");
-    k_obj_final<<<1, kBlock, 0, s>>>(c->dred, nb1, nb2, (double)c->p.lambda, c->dscalar);
+    k_obj_final<<<1, kBlock, 0, s>>>(pa, nb1, c->dred + 152 * 2, nb2, (double)c->p.lambda,
+                                     c->dscalar);
     LAUNCH_CHECK(c, "k_obj_final");
     return CDLGB_OK;
 }

@@ -33,7 +33,8 @@ struct cdlgb_ctx {
     bool loaded = false, initialized = false;
     int L4 = 0, N = 0, M = 0, gamma = 0, Lg = 0, F = 0;
     size_t LMN = 0, LN = 0, LM = 0;
-    int fused = 0;                  // 1 when the fused in-kernel-FFT path is used
+    int fused = 0;                  // 1 when the fused in-kernel-FFT X-step is used
+    int absx_fused = 0;             // sum |X| partials of the last fused X-step are current
 
     // one-hot data, (N, L4) == Julia (4L, N)
     float* S = nullptr;
@@ -134,6 +135,7 @@ int fused_setup(cdlgb_ctx* c);
 void fused_free(cdlgb_ctx* c);
 int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs);
 int fused_dstep(cdlgb_ctx* c);
+int fused_absx(cdlgb_ctx* c, const double** part, int* n);
 size_t fused_scratch_bytes(int Lg, int M, int N);
 
 // ---- scan.cu ----

@@ -50,7 +50,7 @@ def dataset(wl=WORKLOAD, N=None):
     from importlib import import_module  # noqa: F401
     pkg = _pkg()
     n = wl["N"] if N is None else N
-    bases, _, _ = pkg.synth.plant_dataset(wl["seed"], wl["N"], wl["L"], wl["widths"], wl["occ"])
+    bases, _, _ = pkg.synth.plant_dataset(wl["seed"], n, wl["L"], wl["widths"], wl["occ"])
     return bases[:n]
 
 
@@ -236,6 +236,10 @@ def run_gpu(args, rank: int, world: int):
 
     # ---- end-to-end leg through the C ABI with host buffers
     E = args.e2e_outer
+    if args.skip_e2e:
+        c.close()
+        return dict(value=value, ms=ms_max, clocks=clocks, prof=prof, e2e=None, h2d=0, d2h=0,
+                    fused=prof["xfused"][1] > 0)
     for _ in range(max(1, args.warmup // 2)):
         c.load_data(S_pin)
         c.init_state(seed=wl["seed"])
@@ -301,8 +305,13 @@ def main():
     ap.add_argument("--e2e-outer", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=0, help="override N (small cases for profiling)")
+    ap.add_argument("--skip-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.n:
+        WORKLOAD["N"] = args.n
+        WORKLOAD["name"] = f"plain_n{args.n}_l{WORKLOAD['L']}_k{WORKLOAD['M']}"
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     wl = WORKLOAD

@@ -42,6 +42,13 @@ __host__ __device__ constexpr int trig_off(int p) {
 }
 const int kPrimes[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
 
+// register-FFT variant (xwarp.cu)
+void* warp_plan_create(cdlgb_ctx* c, int* status);
+void warp_plan_free(void* p);
+int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout);
+int warp_absx(void* p, const double** part, int* n);
+int warp_variant_exists(int Lg, int M);
+
 struct FusedPlan {
     int Lg, F;
     int nfac;
@@ -51,6 +58,7 @@ struct FusedPlan {
     int grid;               // CTAs (multiple of CS)
     float2* tw;             // Lg twiddles exp(-2 pi i t / Lg), device
     double* absx_part;      // one partial sum of |X| per CTA
+    void* warp;             // register-FFT variant (xwarp.cu) when Lg has one
 };
 
 struct XArgs {
@@ -533,6 +541,7 @@ bool choose_cluster(int Lg, int M, int* CS, int* Mc) {
 
 int fused_supported(int Lg, int M) {
     int fac[kMaxFactors], nf = 0, cs = 0, mc = 0;
+    if (warp_variant_exists(Lg, M)) return 1;
     if (Lg % 4) return 0;
     if (!factorize(Lg, fac, &nf)) return 0;
     if (!choose_cluster(Lg, M, &cs, &mc)) return 0;
@@ -549,6 +558,12 @@ int fused_setup(cdlgb_ctx* c) {
     c->fplan = P;
     P->Lg = c->Lg;
     P->F = c->F;
+    if (!getenv("CDLGB_GENERIC_FFT")) {
+        int st = CDLGB_OK;
+        P->warp = warp_plan_create(c, &st);
+        if (st != CDLGB_OK) return st;
+        if (P->warp) return CDLGB_OK;
+    }
     if (!factorize(c->Lg, P->fac, &P->nfac) || !choose_cluster(c->Lg, c->M, &P->CS, &P->Mc))
         return cdlgb_seterr(c, CDLGB_ENOTSUP, "fused path: unsupported Lg=%d / M=%d", c->Lg, c->M);
     for (int t = P->nfac; t < kMaxFactors; ++t) P->fac[t] = 1;
@@ -595,6 +610,7 @@ void fused_free(cdlgb_ctx* c) {
     if (!P) return;
     if (P->tw) cudaFree(P->tw);
     if (P->absx_part) cudaFree(P->absx_part);
+    warp_plan_free(P->warp);
     delete P;
     c->fplan = nullptr;
 }
@@ -602,6 +618,7 @@ void fused_free(cdlgb_ctx* c) {
 int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs) {
     (void)accum_abs;
     FusedPlan* P = (FusedPlan*)c->fplan;
+    if (P->warp) return warp_xstep(c, P->warp, Xin, Xout);
     XArgs a;
     a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
     a.Y1 = c->Y1; a.y1 = c->y1; a.DX = c->DX; a.S = c->S;
@@ -635,6 +652,7 @@ int fused_dstep(cdlgb_ctx* c) { return cdlgb_seterr(c, CDLGB_ENOTSUP, "fused D-s
 int fused_absx(cdlgb_ctx* c, const double** part, int* n) {
     FusedPlan* P = (FusedPlan*)c->fplan;
     if (!P) return 0;
+    if (P->warp) return warp_absx(P->warp, part, n);
     *part = P->absx_part;
     *n = P->grid;
     return 1;

@@ -1,0 +1,646 @@
+// Fused X-step with register-resident four-step FFTs (Lg = N1 * P, N1 in {16, 32}
+// lanes, P an odd prime).  Same algebra and cluster structure as the generic fused
+// kernel (fused.cu), but each packed column pair (and the U / DX slot) is owned by a
+// group of N1 lanes that transforms it without block-wide barriers:
+//   forward  x[n1 + N1 n2] (lane n1 holds n2 = 0..P-1)
+//     1. DFT-P over n2 in registers (pairwise-symmetric form), twiddle w_Lg^(n1 k2),
+//        write T[k2][n1] (row stride N1+1: conflict-free both ways);
+//     2. lane j takes rows r = j + N1 q: DFT-N1 in registers (radix-2 DIF) gives
+//        X[r + P k1], written in natural order into the same buffer.
+//   inverse  the same steps backwards (inverse DFT-N1 per row, conjugate twiddles,
+//     transpose, inverse DFT-P per lane, results streamed to HBM).
+// The block-wide phases between the transforms (split of the packed spectra,
+// cross-filter sums, Sherman-Morrison combine) read and write the spectra in shared
+// memory; the cross-filter sum over the cluster goes through distributed shared
+// memory in fixed rank order.
+#include "cdlgb_internal.h"
+
+#include <cooperative_groups.h>
+#include <math.h>
+#include <stdlib.h>
+#include <vector>
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+constexpr int kMaxThreads = 160;
+constexpr size_t kWarpSmemCap = 72 * 1024;   // three CTAs per SM
+
+// cos/sin(2 pi m / p) for the odd primes 3..31, concatenated; exp(-2 pi i j / 32)
+__constant__ float2 c_trigw[3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31];
+__constant__ float2 c_w32[32];
+
+__host__ __device__ constexpr int toff(int p) {
+    return p == 3 ? 0 : p == 5 ? 3 : p == 7 ? 8 : p == 11 ? 15 : p == 13 ? 26 : p == 17 ? 39
+         : p == 19 ? 56 : p == 23 ? 75 : p == 29 ? 98 : p == 31 ? 127 : -1;
+}
+const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
+
+__host__ __device__ constexpr int brev(int k, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; ++b) r |= ((k >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return f2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return f2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
+    return f2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+    return f2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {  // conj(a)*b + c
+    return f2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, c.y)));
+}
+template <int SIGN>
+__device__ __forceinline__ float2 mul_i(float2 a) {  // SIGN * i * a
+    return SIGN > 0 ? f2(-a.y, a.x) : f2(a.y, -a.x);
+}
+
+// in-register radix-2 DIF DFT of length N (16 or 32); X[k] ends in x[brev(k)]
+template <int N, int SIGN>
+__device__ __forceinline__ void dft_reg(float2 (&x)[N]) {
+    constexpr int LOG = ilog2c(N);
+#pragma unroll
+    for (int st = 0; st < LOG; ++st) {
+        const int span = N >> (st + 1);
+#pragma unroll
+        for (int blk = 0; blk < N; blk += 2 * span) {
+#pragma unroll
+            for (int j = 0; j < span; ++j) {
+                float2 a = x[blk + j], b = x[blk + j + span];
+                x[blk + j] = cadd(a, b);
+                float2 t = csub(a, b);
+                if (j == 0) {
+                    x[blk + j + span] = t;
+                } else if (4 * j == 2 * span) {          // w = SIGN * i
+                    x[blk + j + span] = mul_i<SIGN>(t);
+                } else {
+                    float2 w = c_w32[j * (32 / (2 * span))];
+                    x[blk + j + span] = SIGN < 0 ? cmul(t, w) : cmulc(t, w);
+                }
+            }
+        }
+    }
+}
+
+// Forward step 1, in place on this lane's column of the group buffer: inputs
+// z[n2] at T[n2][n1], DFT-P over n2, twiddle by w_Lg^(n1 k2), outputs at T[k2][n1].
+template <int N1, int P>
+__device__ __forceinline__ void fwd_step1(float2* __restrict__ T, int n1,
+                                          const float2* __restrict__ tw2) {
+    constexpr int H = (P - 1) / 2;
+    constexpr int OFF = toff(P);
+    constexpr int RS = N1 + 1;
+    float2 x0 = T[n1];
+    float2 s[H], d[H];
+    float2 y0 = x0;
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+        float2 a = T[j * RS + n1], b = T[(P - j) * RS + n1];
+        s[j - 1] = cadd(a, b);
+        d[j - 1] = csub(a, b);
+        y0 = cadd(y0, s[j - 1]);
+    }
+    T[n1] = y0;
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+        float2 A = x0, B = f2(0.f, 0.f);
+#pragma unroll
+        for (int j = 1; j <= H; ++j) {
+            const float2 cs = c_trigw[OFF + (j * k) % P];
+            A.x = fmaf(s[j - 1].x, cs.x, A.x);
+            A.y = fmaf(s[j - 1].y, cs.x, A.y);
+            B.x = fmaf(d[j - 1].x, cs.y, B.x);
+            B.y = fmaf(d[j - 1].y, cs.y, B.y);
+        }
+        float2 ib = mul_i<-1>(B);
+        T[k * RS + n1] = cmul(cadd(A, ib), tw2[k * N1 + n1]);
+        T[(P - k) * RS + n1] = cmul(csub(A, ib), tw2[(P - k) * N1 + n1]);
+    }
+}
+
+// Inverse step 1: inputs T[k2][n1] (already twiddled), inverse DFT-P, put(n2, x).
+template <int N1, int P, class Put>
+__device__ __forceinline__ void inv_step1(const float2* __restrict__ T, int n1, Put&& put) {
+    constexpr int H = (P - 1) / 2;
+    constexpr int OFF = toff(P);
+    constexpr int RS = N1 + 1;
+    float2 x0 = T[n1];
+    float2 s[H], d[H];
+    float2 y0 = x0;
+#pragma unroll
+    for (int j = 1; j <= H; ++j) {
+        float2 a = T[j * RS + n1], b = T[(P - j) * RS + n1];
+        s[j - 1] = cadd(a, b);
+        d[j - 1] = csub(a, b);
+        y0 = cadd(y0, s[j - 1]);
+    }
+    put(0, y0);
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+        float2 A = x0, B = f2(0.f, 0.f);
+#pragma unroll
+        for (int j = 1; j <= H; ++j) {
+            const float2 cs = c_trigw[OFF + (j * k) % P];
+            A.x = fmaf(s[j - 1].x, cs.x, A.x);
+            A.y = fmaf(s[j - 1].y, cs.x, A.y);
+            B.x = fmaf(d[j - 1].x, cs.y, B.x);
+            B.y = fmaf(d[j - 1].y, cs.y, B.y);
+        }
+        float2 ib = mul_i<1>(B);
+        put(k, cadd(A, ib));
+        put(P - k, csub(A, ib));
+    }
+}
+
+// Forward step 2: rows of T -> DFT-N1 -> natural-order spectrum Z (same buffer).
+template <int N1, int P>
+__device__ __forceinline__ void fwd_step2(float2* __restrict__ buf, int j, bool active) {
+    constexpr int RQ = (P + N1 - 1) / N1;
+    constexpr int RS = N1 + 1;
+    constexpr int LB = ilog2c(N1);
+    float2 v[RQ][N1];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+        int r = j + N1 * q;
+        if (active && r < P) {
+#pragma unroll
+            for (int t = 0; t < N1; ++t) v[q][t] = buf[r * RS + t];
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+        int r = j + N1 * q;
+        if (active && r < P) {
+            dft_reg<N1, -1>(v[q]);
+#pragma unroll
+            for (int i = 0; i < N1; ++i) buf[r + P * brev(i, LB)] = v[q][i];   // X[k1] is v[brev(k1)]
+        }
+    }
+    __syncwarp();
+}
+
+// Inverse step 2: natural-order spectrum -> inverse DFT-N1 per row -> conj twiddle -> T.
+template <int N1, int P>
+__device__ __forceinline__ void inv_step2(float2* __restrict__ buf, int j, bool active,
+                                          const float2* __restrict__ tw2) {
+    constexpr int RQ = (P + N1 - 1) / N1;
+    constexpr int RS = N1 + 1;
+    constexpr int LB = ilog2c(N1);
+    float2 v[RQ][N1];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+        int r = j + N1 * q;
+        if (active && r < P) {
+#pragma unroll
+            for (int k1 = 0; k1 < N1; ++k1) v[q][k1] = buf[r + P * k1];
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) {
+        int r = j + N1 * q;
+        if (active && r < P) {
+            dft_reg<N1, 1>(v[q]);
+#pragma unroll
+            for (int i = 0; i < N1; ++i) {
+                const int n1 = brev(i, LB);
+                buf[r * RS + n1] = cmulc(v[q][i], tw2[r * N1 + n1]);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+struct WArgs {
+    const float* Xin;
+    float* Xout;
+    float* y2;
+    float* y3;
+    float* Y1;
+    float* y1;
+    float* DX;
+    const float* S;
+    const float2* G1h;
+    const float* Ah;
+    const float2* tw2;      // [P][N1] exp(-2 pi i n1 k2 / Lg)
+    double* absx_part;
+    int N, M, F, L4, gamma;
+    float lam, rho, kc;
+    int Mc, B;
+};
+
+__device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
+                                       float& na, float& nb, float& v) {
+    float t = x + a;                                        // X + y2
+    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);    // shrink!  (csc_kernels.jl:53-64)
+    float Y3 = keep ? x + b : 0.f;                          // projectionX! (:68-82)
+    na = (a + x) - Y2;                                      // train.jl:13
+    nb = (b + x) - Y3;                                      // train.jl:14
+    v = (Y2 - na) + (Y3 - nb);
+}
+
+// streamed input of the forward transform: element l = n1 + N1 n2 of a packed column
+// pair (X, y2, y3 read, y2', y3' written back) or of the U slot
+template <int N1, int Lg>
+struct GetXT {
+    const float* __restrict__ Xin;
+    float* __restrict__ y2;
+    float* __restrict__ y3;
+    const float* __restrict__ Y1;
+    const float* __restrict__ y1;
+    const float* __restrict__ DX;
+    size_t ba, bn;
+    int gl;
+    float lam;
+    bool is_pair, is_u, hasb;
+    float* y1s;
+    __device__ __forceinline__ float2 operator()(int n2) const {
+        const int l = gl + N1 * n2;
+        const bool keep = (l & 3) == 0;
+        if (is_pair) {
+            float xa = Xin[ba + l], aa = y2[ba + l], ca = y3[ba + l];
+            float na, nb, va, vb = 0.f;
+            xprep1(xa, aa, ca, lam, keep, na, nb, va);
+            y2[ba + l] = na;
+            y3[ba + l] = nb;
+            if (hasb) {
+                float xb = Xin[ba + Lg + l], ab = y2[ba + Lg + l], cb = y3[ba + Lg + l];
+                xprep1(xb, ab, cb, lam, keep, na, nb, vb);
+                y2[ba + Lg + l] = na;
+                y3[ba + Lg + l] = nb;
+            }
+            return f2(va, vb);
+        } else if (is_u) {
+            float Yv = Y1[bn + l];
+            float yn = (y1[bn + l] + DX[bn + l]) - Yv;   // train.jl:12
+            y1s[l] = yn;
+            return f2(Yv - yn, 0.f);
+        }
+        return f2(0.f, 0.f);
+    }
+};
+
+// streamed output of the inverse transform: X of a column pair, or DX / y1' / Y1
+template <int N1, int Lg>
+struct PutXT {
+    float* __restrict__ Xout;
+    float* __restrict__ DX;
+    float* __restrict__ y1;
+    float* __restrict__ Y1;
+    const float* __restrict__ S;
+    size_t ba, bn, sn;
+    int gl, gamma, L4;
+    float rho;
+    bool is_pair, is_dx, hasb;
+    const float* y1s;
+    float acc;
+    __device__ __forceinline__ void operator()(int n2, float2 v) {
+        const int l = gl + N1 * n2;
+        if (is_pair) {
+            Xout[ba + l] = v.x;
+            acc += fabsf(v.x);
+            if (hasb) {
+                Xout[ba + Lg + l] = v.y;
+                acc += fabsf(v.y);
+            }
+        } else if (is_dx) {
+            // Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!, csc_kernels.jl:86-95)
+            const bool in = l >= gamma && l < gamma + L4;
+            const float wts = in ? S[sn + (l - gamma)] : 0.f;
+            const float dg = in ? 1.f : 0.f;
+            const float yn = y1s[l];
+            DX[bn + l] = v.x;
+            y1[bn + l] = yn;
+            Y1[bn + l] = (wts + rho * (v.x + yn)) / (dg + rho);
+        }
+    }
+};
+
+template <int N1, int P>
+__global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
+    constexpr int Lg = N1 * P;
+    constexpr int G = 32 / N1;                  // lane groups per warp
+    constexpr int BUF = P * (N1 + 1);           // complex entries per group buffer
+    constexpr int half = Lg / 2;
+    constexpr int F = Lg / 2 + 1;
+    constexpr int Fp = (F + 1) & ~1;
+    extern __shared__ float4 smem4[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CS = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int cid = blockIdx.x / CS;
+    const int nclusters = gridDim.x / CS;
+    const int B = A.B, Mc = A.Mc, M = A.M;
+    const int NG = (blockDim.x >> 5) * G;
+
+    float2* tw2 = reinterpret_cast<float2*>(smem4);
+    float2* bufs = tw2 + P * N1;
+    float2* Ppart = bufs + (size_t)NG * BUF;
+    float2* Wv = Ppart + 2 * Fp;
+    float* y1s = reinterpret_cast<float*>(Wv + Fp);
+    __shared__ double red[kMaxThreads / 32];
+
+    for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int grp = (threadIdx.x >> 5) * G + lane / N1;   // slot handled by this lane group
+    const int gl = lane % N1;                             // lane within the group
+    float2* gbuf = bufs + (size_t)grp * BUF;
+    const int m0 = rank * Mc;
+    const float sc = 1.f / (A.kc * (float)Lg);
+    const float lam = A.lam;
+    double absacc = 0.0;
+    int it = 0;
+
+    for (int n = cid; n < A.N; n += nclusters, ++it) {
+        // ---------------- forward transforms (one slot per lane group)
+        {
+            const bool is_pair = grp < B;
+            const bool is_u = grp == B;
+            const int ma = m0 + 2 * grp;
+            const bool hasb = is_pair && (2 * grp + 1 < Mc);
+            const size_t ba = ((size_t)n * M + ma) * Lg;
+            const size_t bn = (size_t)n * Lg;
+            GetXT<N1, Lg> get{A.Xin, A.y2, A.y3, A.Y1, A.y1, A.DX, ba, bn, gl, lam, is_pair, is_u, hasb, y1s};
+            if (grp <= B) {
+#pragma unroll 4
+                for (int n2 = 0; n2 < P; ++n2) gbuf[n2 * (N1 + 1) + gl] = get(n2);
+                fwd_step1<N1, P>(gbuf, gl, tw2);
+            }
+            __syncwarp();
+            fwd_step2<N1, P>(gbuf, gl, grp <= B);
+        }
+        __syncthreads();
+
+        // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
+        float2* Pp = Ppart + (it & 1) * Fp;
+        for (int f = threadIdx.x; f < F; f += blockDim.x) {
+            float2 P_ = f2(0.f, 0.f);
+            const bool edge = (f == 0) || (f == half);
+            const int fr = edge ? f : Lg - f;
+            for (int s = 0; s < B; ++s) {
+                const float2* Z = bufs + (size_t)s * BUF;
+                float2 z1 = Z[f], z2 = Z[fr];
+                float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+                float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+                const int ma = m0 + 2 * s;
+                P_ = cfma(A.G1h[(size_t)ma * F + f], va, P_);
+                if (2 * s + 1 < Mc) P_ = cfma(A.G1h[(size_t)(ma + 1) * F + f], vb, P_);
+            }
+            Pp[f] = P_;
+        }
+        cluster.sync();
+
+        // ---------------- P over the cluster, alpha, W; rank 0 packs DXh
+        {
+            float2* ZU = bufs + (size_t)B * BUF;
+            for (int f = threadIdx.x; f < F; f += blockDim.x) {
+                float2 P_ = f2(0.f, 0.f);
+                for (int r = 0; r < CS; ++r) P_ = cadd(P_, cluster.map_shared_rank(Pp, r)[f]);
+                const float Av = A.Ah[f];
+                const float2 U = ZU[f];
+                const float inv_s = 1.f / (Av + A.kc);
+                float2 alpha = f2(fmaf(Av, U.x, P_.x) * inv_s, fmaf(Av, U.y, P_.y) * inv_s);
+                float2 W = csub(U, alpha);
+                Wv[f] = W;
+                if (rank == 0) {
+                    float2 D = f2(fmaf(Av, W.x, P_.x) * sc, fmaf(Av, W.y, P_.y) * sc);
+                    if (f == 0 || f == half) {
+                        ZU[f] = f2(D.x, 0.f);
+                    } else {
+                        ZU[f] = D;
+                        ZU[Lg - f] = f2(D.x, -D.y);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---------------- Xh = (Vh + conj(G1h) W)/(k Lg), repacked in place
+        for (int idx = threadIdx.x; idx < B * F; idx += blockDim.x) {
+            const int s = idx / F;
+            const int f = idx - s * F;
+            float2* Z = bufs + (size_t)s * BUF;
+            const bool edge = (f == 0) || (f == half);
+            const int ma = m0 + 2 * s;
+            const bool hasb = 2 * s + 1 < Mc;
+            const float2 W = Wv[f];
+            float2 z1 = Z[f], z2 = Z[edge ? f : Lg - f];
+            float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+            float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+            float2 xa = cjfma(A.G1h[(size_t)ma * F + f], W, va);
+            float2 xb = hasb ? cjfma(A.G1h[(size_t)(ma + 1) * F + f], W, vb) : f2(0.f, 0.f);
+            xa = f2(xa.x * sc, xa.y * sc);
+            xb = f2(xb.x * sc, xb.y * sc);
+            if (edge) {
+                Z[f] = f2(xa.x, xb.x);
+            } else {
+                Z[f] = f2(xa.x - xb.y, xa.y + xb.x);
+                Z[Lg - f] = f2(xa.x + xb.y, xb.x - xa.y);
+            }
+        }
+        __syncthreads();
+
+        // ---------------- inverse transforms and stores
+        {
+            const bool is_pair = grp < B;
+            const bool is_dx = (grp == B) && (rank == 0);
+            const int ma = m0 + 2 * grp;
+            const bool hasb = is_pair && (2 * grp + 1 < Mc);
+            const size_t ba = ((size_t)n * M + ma) * Lg;
+            const size_t bn = (size_t)n * Lg;
+            inv_step2<N1, P>(gbuf, gl, is_pair || is_dx, tw2);
+            PutXT<N1, Lg> put{A.Xout, A.DX, A.y1, A.Y1, A.S, ba, bn, (size_t)n * A.L4, gl, A.gamma, A.L4, A.rho, is_pair, is_dx, hasb, y1s, 0.f};
+            if (is_pair || is_dx) inv_step1<N1, P>(gbuf, gl, put);
+            absacc += (double)put.acc;
+        }
+        __syncthreads();
+    }
+    cluster.sync();
+
+    for (int o = 16; o > 0; o >>= 1) absacc += __shfl_xor_sync(0xffffffffu, absacc, o);
+    if (lane == 0) red[threadIdx.x >> 5] = absacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        A.absx_part[blockIdx.x] = t;
+    }
+}
+
+// ------------------------------------------------------------------ dispatch
+typedef void (*kern_t)(WArgs);
+struct Variant { int N1, P; kern_t k; };
+const Variant kVariants[] = {
+    {32, 29, k_xstep_warp<32, 29>},
+    {16, 31, k_xstep_warp<16, 31>},
+};
+
+const Variant* find_variant(int Lg) {
+    for (const Variant& v : kVariants)
+        if (v.N1 * v.P == Lg) return &v;
+    return nullptr;
+}
+
+size_t warp_smem(int N1, int P, int NG) {
+    int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
+    return ((size_t)P * N1 + (size_t)NG * P * (N1 + 1) + 3 * (size_t)Fp) * sizeof(float2) +
+           (size_t)Lg * sizeof(float);
+}
+
+}  // namespace
+
+int warp_variant_exists(int Lg, int M) {
+    const Variant* v = find_variant(Lg);
+    if (!v) return 0;
+    for (int cs : {1, 2, 4, 8}) {
+        if (M % cs) continue;
+        int B = (M / cs + 1) / 2, G = 32 / v->N1, warps = (B + 1 + G - 1) / G;
+        if (warps * 32 <= kMaxThreads && warp_smem(v->N1, v->P, warps * G) <= kWarpSmemCap) return 1;
+    }
+    return 0;
+}
+
+struct WarpPlan {
+    const Variant* v;
+    int CS, Mc, B, threads;
+    size_t smem;
+    int grid;
+    float2* tw2;
+    double* absx_part;
+};
+
+// Picks the smallest cluster whose CTA fits 3 per SM; returns nullptr when the size
+// has no register-FFT variant.
+void* warp_plan_create(cdlgb_ctx* c, int* status) {
+    *status = CDLGB_OK;
+    const Variant* v = find_variant(c->Lg);
+    if (!v) return nullptr;
+    int want_cs = 0;
+    if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
+    WarpPlan* P = nullptr;
+    for (int cs : {1, 2, 4, 8}) {
+        if (c->M % cs) continue;
+        if (want_cs && cs != want_cs) continue;
+        int mc = c->M / cs;
+        int B = (mc + 1) / 2;
+        int G = 32 / v->N1;
+        int warps = (B + 1 + G - 1) / G;
+        int threads = warps * 32;
+        if (threads > kMaxThreads) continue;
+        size_t sm = warp_smem(v->N1, v->P, warps * G);
+        if (sm > kWarpSmemCap) continue;
+        P = new WarpPlan();
+        P->v = v; P->CS = cs; P->Mc = mc; P->B = B; P->threads = threads; P->smem = sm;
+        break;
+    }
+    if (!P) return nullptr;
+    // tables
+    std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31);
+    for (int p : kPrimesW)
+        for (int m = 0; m < p; ++m)
+            trig[toff(p) + m] = make_float2((float)cos(2.0 * M_PI * m / p), (float)sin(2.0 * M_PI * m / p));
+    std::vector<float2> w32(32);
+    for (int j = 0; j < 32; ++j) w32[j] = make_float2((float)cos(2.0 * M_PI * j / 32), (float)-sin(2.0 * M_PI * j / 32));
+    int N1 = v->N1, Pp = v->P, Lg = N1 * Pp;
+    std::vector<float2> tw2((size_t)Pp * N1);
+    for (int k2 = 0; k2 < Pp; ++k2)
+        for (int n1 = 0; n1 < N1; ++n1) {
+            double a = 2.0 * M_PI * (double)((n1 * k2) % Lg) / Lg;
+            tw2[(size_t)k2 * N1 + n1] = make_float2((float)cos(a), (float)-sin(a));
+        }
+    cudaError_t e = cudaMemcpyToSymbol(c_trigw, trig.data(), trig.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_w32, w32.data(), 32 * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(v->k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem);
+    int nclusters = 0;
+    if (e == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = P->CS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(P->CS * 152 * 4, 1, 1);
+        cfg.blockDim = dim3(P->threads, 1, 1);
+        cfg.dynamicSmemBytes = P->smem;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)v->k, &cfg);
+    }
+    if (e != cudaSuccess || nclusters < 1) {
+        *status = cdlgb_seterr(c, CDLGB_ECUDA, "register-FFT X-step setup failed: %s",
+                               e != cudaSuccess ? cudaGetErrorString(e) : "no cluster fits");
+        if (P->tw2) cudaFree(P->tw2);
+        delete P;
+        return nullptr;
+    }
+    if (nclusters > c->N) nclusters = c->N;
+    P->grid = nclusters * P->CS;
+    e = cudaMalloc((void**)&P->absx_part, (size_t)P->grid * sizeof(double));
+    if (e != cudaSuccess) {
+        *status = cdlgb_seterr(c, CDLGB_ECUDA, "cudaMalloc: %s", cudaGetErrorString(e));
+        cudaFree(P->tw2);
+        delete P;
+        return nullptr;
+    }
+    return P;
+}
+
+void warp_plan_free(void* p) {
+    WarpPlan* P = (WarpPlan*)p;
+    if (!P) return;
+    if (P->tw2) cudaFree(P->tw2);
+    if (P->absx_part) cudaFree(P->absx_part);
+    delete P;
+}
+
+int warp_plan_cluster(void* p) { return p ? ((WarpPlan*)p)->CS : 0; }
+
+int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout) {
+    WarpPlan* P = (WarpPlan*)p;
+    WArgs a;
+    a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
+    a.Y1 = c->Y1; a.y1 = c->y1; a.DX = c->DX; a.S = c->S;
+    a.G1h = c->G1h; a.Ah = c->Ah; a.tw2 = P->tw2; a.absx_part = P->absx_part;
+    a.N = c->N; a.M = c->M; a.F = c->F; a.L4 = c->L4; a.gamma = c->gamma;
+    a.lam = c->p.lambda; a.rho = c->p.rho; a.kc = c->p.sherman_const_csc;
+    a.Mc = P->Mc; a.B = P->B;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = P->CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(P->grid, 1, 1);
+    cfg.blockDim = dim3(P->threads, 1, 1);
+    cfg.dynamicSmemBytes = P->smem;
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cdlgb_phase_begin(c, PH_XFUSED);
+    CU_TRY(c, cudaLaunchKernelEx(&cfg, P->v->k, a));
+    LAUNCH_CHECK(c, "k_xstep_warp");
+    cdlgb_phase_end(c, PH_XFUSED);
+    return CDLGB_OK;
+}
+
+int warp_absx(void* p, const double** part, int* n) {
+    WarpPlan* P = (WarpPlan*)p;
+    if (!P) return 0;
+    *part = P->absx_part;
+    *n = P->grid;
+    return 1;
+}

@@ -138,6 +138,13 @@ int fused_dstep(cdlgb_ctx* c);
 int fused_absx(cdlgb_ctx* c, const double** part, int* n);
 size_t fused_scratch_bytes(int Lg, int M, int N);
 
+// ---- xwarp.cu (register-FFT variant of the fused X-step) ----
+void* warp_plan_create(cdlgb_ctx* c, int* status);
+void warp_plan_free(void* p);
+int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout);
+int warp_absx(void* p, const double** part, int* n);
+int warp_variant_exists(int Lg, int M);
+
 // ---- scan.cu ----
 int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
              int K, int maxlen, int32_t* pos_out);

@@ -42,13 +42,6 @@ __host__ __device__ constexpr int trig_off(int p) {
 }
 const int kPrimes[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
 
-// register-FFT variant (xwarp.cu)
-void* warp_plan_create(cdlgb_ctx* c, int* status);
-void warp_plan_free(void* p);
-int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout);
-int warp_absx(void* p, const double** part, int* n);
-int warp_variant_exists(int Lg, int M);
-
 struct FusedPlan {
     int Lg, F;
     int nfac;

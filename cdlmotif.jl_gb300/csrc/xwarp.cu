@@ -45,8 +45,31 @@ __host__ __device__ constexpr int brev(int k, int bits) {
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return f2(a.x - b.x, a.y - b.y); }
+// Blackwell packed FP32x2 arithmetic (one instruction for both halves, IEEE-identical
+// to the two scalar operations); the pairs are formed inside the asm so that the
+// register allocator can keep them as adjacent registers
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+// a * (c, c) + b  for a complex a and a real c
+__device__ __forceinline__ float2 rfma(float2 a, float c, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pc, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pc, {%4, %4};\n\t"
+        "mov.b64 pb, {%5, %6};\n\tfma.rn.f32x2 pd, pa, pc, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(c), "f"(b.x), "f"(b.y));
+    return r;
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return f2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
@@ -116,10 +139,8 @@ __device__ __forceinline__ void fwd_step1(float2* __restrict__ T, int n1,
 #pragma unroll
         for (int j = 1; j <= H; ++j) {
             const float2 cs = c_trigw[OFF + (j * k) % P];
-            A.x = fmaf(s[j - 1].x, cs.x, A.x);
-            A.y = fmaf(s[j - 1].y, cs.x, A.y);
-            B.x = fmaf(d[j - 1].x, cs.y, B.x);
-            B.y = fmaf(d[j - 1].y, cs.y, B.y);
+            A = rfma(s[j - 1], cs.x, A);
+            B = rfma(d[j - 1], cs.y, B);
         }
         float2 ib = mul_i<-1>(B);
         T[k * RS + n1] = cmul(cadd(A, ib), tw2[k * N1 + n1]);
@@ -127,9 +148,10 @@ __device__ __forceinline__ void fwd_step1(float2* __restrict__ T, int n1,
     }
 }
 
-// Inverse step 1: inputs T[k2][n1] (already twiddled), inverse DFT-P, put(n2, x).
-template <int N1, int P, class Put>
-__device__ __forceinline__ void inv_step1(const float2* __restrict__ T, int n1, Put&& put) {
+// Inverse step 1, in place on this lane's column: inputs T[k2][n1] (already
+// twiddled), inverse DFT-P over k2, outputs x[n1 + N1 n2] at T[n2][n1].
+template <int N1, int P>
+__device__ __forceinline__ void inv_step1(float2* __restrict__ T, int n1) {
     constexpr int H = (P - 1) / 2;
     constexpr int OFF = toff(P);
     constexpr int RS = N1 + 1;
@@ -143,21 +165,19 @@ __device__ __forceinline__ void inv_step1(const float2* __restrict__ T, int n1, 
         d[j - 1] = csub(a, b);
         y0 = cadd(y0, s[j - 1]);
     }
-    put(0, y0);
+    T[n1] = y0;
 #pragma unroll
     for (int k = 1; k <= H; ++k) {
         float2 A = x0, B = f2(0.f, 0.f);
 #pragma unroll
         for (int j = 1; j <= H; ++j) {
             const float2 cs = c_trigw[OFF + (j * k) % P];
-            A.x = fmaf(s[j - 1].x, cs.x, A.x);
-            A.y = fmaf(s[j - 1].y, cs.x, A.y);
-            B.x = fmaf(d[j - 1].x, cs.y, B.x);
-            B.y = fmaf(d[j - 1].y, cs.y, B.y);
+            A = rfma(s[j - 1], cs.x, A);
+            B = rfma(d[j - 1], cs.y, B);
         }
         float2 ib = mul_i<1>(B);
-        put(k, cadd(A, ib));
-        put(P - k, csub(A, ib));
+        T[k * RS + n1] = cadd(A, ib);
+        T[(P - k) * RS + n1] = csub(A, ib);
     }
 }
 
@@ -249,88 +269,13 @@ __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, boo
     v = (Y2 - na) + (Y3 - nb);
 }
 
-// streamed input of the forward transform: element l = n1 + N1 n2 of a packed column
-// pair (X, y2, y3 read, y2', y3' written back) or of the U slot
-template <int N1, int Lg>
-struct GetXT {
-    const float* __restrict__ Xin;
-    float* __restrict__ y2;
-    float* __restrict__ y3;
-    const float* __restrict__ Y1;
-    const float* __restrict__ y1;
-    const float* __restrict__ DX;
-    size_t ba, bn;
-    int gl;
-    float lam;
-    bool is_pair, is_u, hasb;
-    float* y1s;
-    __device__ __forceinline__ float2 operator()(int n2) const {
-        const int l = gl + N1 * n2;
-        const bool keep = (l & 3) == 0;
-        if (is_pair) {
-            float xa = Xin[ba + l], aa = y2[ba + l], ca = y3[ba + l];
-            float na, nb, va, vb = 0.f;
-            xprep1(xa, aa, ca, lam, keep, na, nb, va);
-            y2[ba + l] = na;
-            y3[ba + l] = nb;
-            if (hasb) {
-                float xb = Xin[ba + Lg + l], ab = y2[ba + Lg + l], cb = y3[ba + Lg + l];
-                xprep1(xb, ab, cb, lam, keep, na, nb, vb);
-                y2[ba + Lg + l] = na;
-                y3[ba + Lg + l] = nb;
-            }
-            return f2(va, vb);
-        } else if (is_u) {
-            float Yv = Y1[bn + l];
-            float yn = (y1[bn + l] + DX[bn + l]) - Yv;   // train.jl:12
-            y1s[l] = yn;
-            return f2(Yv - yn, 0.f);
-        }
-        return f2(0.f, 0.f);
-    }
-};
-
-// streamed output of the inverse transform: X of a column pair, or DX / y1' / Y1
-template <int N1, int Lg>
-struct PutXT {
-    float* __restrict__ Xout;
-    float* __restrict__ DX;
-    float* __restrict__ y1;
-    float* __restrict__ Y1;
-    const float* __restrict__ S;
-    size_t ba, bn, sn;
-    int gl, gamma, L4;
-    float rho;
-    bool is_pair, is_dx, hasb;
-    const float* y1s;
-    float acc;
-    __device__ __forceinline__ void operator()(int n2, float2 v) {
-        const int l = gl + N1 * n2;
-        if (is_pair) {
-            Xout[ba + l] = v.x;
-            acc += fabsf(v.x);
-            if (hasb) {
-                Xout[ba + Lg + l] = v.y;
-                acc += fabsf(v.y);
-            }
-        } else if (is_dx) {
-            // Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!, csc_kernels.jl:86-95)
-            const bool in = l >= gamma && l < gamma + L4;
-            const float wts = in ? S[sn + (l - gamma)] : 0.f;
-            const float dg = in ? 1.f : 0.f;
-            const float yn = y1s[l];
-            DX[bn + l] = v.x;
-            y1[bn + l] = yn;
-            Y1[bn + l] = (wts + rho * (v.x + yn)) / (dg + rho);
-        }
-    }
-};
-
 template <int N1, int P>
 __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
     constexpr int Lg = N1 * P;
+    constexpr int Lg4 = Lg / 4;
     constexpr int G = 32 / N1;                  // lane groups per warp
-    constexpr int BUF = P * (N1 + 1);           // complex entries per group buffer
+    constexpr int RS = N1 + 1;                  // row stride of the transposed layout
+    constexpr int BUF = P * RS;                 // complex entries per group buffer
     constexpr int half = Lg / 2;
     constexpr int F = Lg / 2 + 1;
     constexpr int Fp = (F + 1) & ~1;
@@ -354,7 +299,7 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    const int grp = (threadIdx.x >> 5) * G + lane / N1;   // slot handled by this lane group
+    const int grp = (threadIdx.x >> 5) * G + lane / N1;   // slot transformed by this lane group
     const int gl = lane % N1;                             // lane within the group
     float2* gbuf = bufs + (size_t)grp * BUF;
     const int m0 = rank * Mc;
@@ -364,45 +309,88 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
     int it = 0;
 
     for (int n = cid; n < A.N; n += nclusters, ++it) {
-        // ---------------- forward transforms (one slot per lane group)
-        {
-            const bool is_pair = grp < B;
-            const bool is_u = grp == B;
-            const int ma = m0 + 2 * grp;
-            const bool hasb = is_pair && (2 * grp + 1 < Mc);
-            const size_t ba = ((size_t)n * M + ma) * Lg;
-            const size_t bn = (size_t)n * Lg;
-            GetXT<N1, Lg> get{A.Xin, A.y2, A.y3, A.Y1, A.y1, A.DX, ba, bn, gl, lam, is_pair, is_u, hasb, y1s};
-            if (grp <= B) {
-#pragma unroll 4
-                for (int n2 = 0; n2 < P; ++n2) gbuf[n2 * (N1 + 1) + gl] = get(n2);
-                fwd_step1<N1, P>(gbuf, gl, tw2);
+        const size_t bn = (size_t)n * Lg;
+        // ---------------- 1. stream X, y2, y3 in (float4): elementwise pass, duals back to
+        // HBM, V packed two columns per complex entry in the transposed group layout
+        for (int idx = threadIdx.x; idx < (B + 1) * Lg4; idx += blockDim.x) {
+            const int sl = idx / Lg4;
+            const int l4 = idx - sl * Lg4;
+            const int l = 4 * l4;
+            float2* dst = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
+            if (sl < B) {
+                const int ma = m0 + 2 * sl;
+                const bool hasb = 2 * sl + 1 < Mc;
+                const size_t ba = ((size_t)n * M + ma) * Lg + l;
+                float4 x = *reinterpret_cast<const float4*>(A.Xin + ba);
+                float4 a = *reinterpret_cast<const float4*>(A.y2 + ba);
+                float4 c = *reinterpret_cast<const float4*>(A.y3 + ba);
+                float4 xb = make_float4(0, 0, 0, 0), ab = xb, cb = xb;
+                if (hasb) {
+                    xb = *reinterpret_cast<const float4*>(A.Xin + ba + Lg);
+                    ab = *reinterpret_cast<const float4*>(A.y2 + ba + Lg);
+                    cb = *reinterpret_cast<const float4*>(A.y3 + ba + Lg);
+                }
+                float4 na, nb, va, vb = make_float4(0, 0, 0, 0);
+                xprep1(x.x, a.x, c.x, lam, true, na.x, nb.x, va.x);   // .x is on the 4-stride
+                xprep1(x.y, a.y, c.y, lam, false, na.y, nb.y, va.y);
+                xprep1(x.z, a.z, c.z, lam, false, na.z, nb.z, va.z);
+                xprep1(x.w, a.w, c.w, lam, false, na.w, nb.w, va.w);
+                *reinterpret_cast<float4*>(A.y2 + ba) = na;
+                *reinterpret_cast<float4*>(A.y3 + ba) = nb;
+                if (hasb) {
+                    xprep1(xb.x, ab.x, cb.x, lam, true, na.x, nb.x, vb.x);
+                    xprep1(xb.y, ab.y, cb.y, lam, false, na.y, nb.y, vb.y);
+                    xprep1(xb.z, ab.z, cb.z, lam, false, na.z, nb.z, vb.z);
+                    xprep1(xb.w, ab.w, cb.w, lam, false, na.w, nb.w, vb.w);
+                    *reinterpret_cast<float4*>(A.y2 + ba + Lg) = na;
+                    *reinterpret_cast<float4*>(A.y3 + ba + Lg) = nb;
+                }
+                dst[0] = f2(va.x, vb.x);
+                dst[1] = f2(va.y, vb.y);
+                dst[2] = f2(va.z, vb.z);
+                dst[3] = f2(va.w, vb.w);
+            } else {
+                // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
+                float4 Yv = *reinterpret_cast<const float4*>(A.Y1 + bn + l);
+                float4 yv = *reinterpret_cast<const float4*>(A.y1 + bn + l);
+                float4 dv = *reinterpret_cast<const float4*>(A.DX + bn + l);
+                float4 yn = make_float4((yv.x + dv.x) - Yv.x, (yv.y + dv.y) - Yv.y,
+                                        (yv.z + dv.z) - Yv.z, (yv.w + dv.w) - Yv.w);
+                *reinterpret_cast<float4*>(y1s + l) = yn;
+                dst[0] = f2(Yv.x - yn.x, 0.f);
+                dst[1] = f2(Yv.y - yn.y, 0.f);
+                dst[2] = f2(Yv.z - yn.z, 0.f);
+                dst[3] = f2(Yv.w - yn.w, 0.f);
             }
-            __syncwarp();
-            fwd_step2<N1, P>(gbuf, gl, grp <= B);
         }
         __syncthreads();
 
-        // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
+        // ---------------- 2. forward transforms, one slot per lane group
+        if (grp <= B) fwd_step1<N1, P>(gbuf, gl, tw2);
+        __syncwarp();
+        fwd_step2<N1, P>(gbuf, gl, grp <= B);
+        __syncthreads();
+
+        // ---------------- 3. split + this CTA's part of P = sum_m G1h[m] Vh[m]
         float2* Pp = Ppart + (it & 1) * Fp;
         for (int f = threadIdx.x; f < F; f += blockDim.x) {
             float2 P_ = f2(0.f, 0.f);
             const bool edge = (f == 0) || (f == half);
             const int fr = edge ? f : Lg - f;
-            for (int s = 0; s < B; ++s) {
-                const float2* Z = bufs + (size_t)s * BUF;
+            for (int sl = 0; sl < B; ++sl) {
+                const float2* Z = bufs + (size_t)sl * BUF;
                 float2 z1 = Z[f], z2 = Z[fr];
                 float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
                 float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-                const int ma = m0 + 2 * s;
+                const int ma = m0 + 2 * sl;
                 P_ = cfma(A.G1h[(size_t)ma * F + f], va, P_);
-                if (2 * s + 1 < Mc) P_ = cfma(A.G1h[(size_t)(ma + 1) * F + f], vb, P_);
+                if (2 * sl + 1 < Mc) P_ = cfma(A.G1h[(size_t)(ma + 1) * F + f], vb, P_);
             }
             Pp[f] = P_;
         }
         cluster.sync();
 
-        // ---------------- P over the cluster, alpha, W; rank 0 packs DXh
+        // ---------------- 4. P over the cluster, alpha, W; rank 0 packs DXh
         {
             float2* ZU = bufs + (size_t)B * BUF;
             for (int f = threadIdx.x; f < F; f += blockDim.x) {
@@ -427,14 +415,14 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
         }
         __syncthreads();
 
-        // ---------------- Xh = (Vh + conj(G1h) W)/(k Lg), repacked in place
+        // ---------------- 5. Xh = (Vh + conj(G1h) W)/(k Lg), repacked in place
         for (int idx = threadIdx.x; idx < B * F; idx += blockDim.x) {
-            const int s = idx / F;
-            const int f = idx - s * F;
-            float2* Z = bufs + (size_t)s * BUF;
+            const int sl = idx / F;
+            const int f = idx - sl * F;
+            float2* Z = bufs + (size_t)sl * BUF;
             const bool edge = (f == 0) || (f == half);
-            const int ma = m0 + 2 * s;
-            const bool hasb = 2 * s + 1 < Mc;
+            const int ma = m0 + 2 * sl;
+            const bool hasb = 2 * sl + 1 < Mc;
             const float2 W = Wv[f];
             float2 z1 = Z[f], z2 = Z[edge ? f : Lg - f];
             float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
@@ -452,18 +440,51 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
         }
         __syncthreads();
 
-        // ---------------- inverse transforms and stores
+        // ---------------- 6. inverse transforms (rank 0 also transforms DX)
         {
-            const bool is_pair = grp < B;
-            const bool is_dx = (grp == B) && (rank == 0);
-            const int ma = m0 + 2 * grp;
-            const bool hasb = is_pair && (2 * grp + 1 < Mc);
-            const size_t ba = ((size_t)n * M + ma) * Lg;
-            const size_t bn = (size_t)n * Lg;
-            inv_step2<N1, P>(gbuf, gl, is_pair || is_dx, tw2);
-            PutXT<N1, Lg> put{A.Xout, A.DX, A.y1, A.Y1, A.S, ba, bn, (size_t)n * A.L4, gl, A.gamma, A.L4, A.rho, is_pair, is_dx, hasb, y1s, 0.f};
-            if (is_pair || is_dx) inv_step1<N1, P>(gbuf, gl, put);
-            absacc += (double)put.acc;
+            const bool act = grp < B || (grp == B && rank == 0);
+            inv_step2<N1, P>(gbuf, gl, act, tw2);
+            if (act) inv_step1<N1, P>(gbuf, gl);
+        }
+        __syncthreads();
+
+        // ---------------- 7. stream X out (float4); rank 0: DX, y1', Y1
+        for (int idx = threadIdx.x; idx < (B + 1) * Lg4; idx += blockDim.x) {
+            const int sl = idx / Lg4;
+            const int l4 = idx - sl * Lg4;
+            const int l = 4 * l4;
+            const float2* src = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
+            const float2 z0 = src[0], z1 = src[1], z2 = src[2], z3 = src[3];
+            if (sl < B) {
+                const int ma = m0 + 2 * sl;
+                const size_t ba = ((size_t)n * M + ma) * Lg + l;
+                float4 xa = make_float4(z0.x, z1.x, z2.x, z3.x);
+                *reinterpret_cast<float4*>(A.Xout + ba) = xa;
+                float s4 = (fabsf(xa.x) + fabsf(xa.y)) + (fabsf(xa.z) + fabsf(xa.w));
+                if (2 * sl + 1 < Mc) {
+                    float4 xb = make_float4(z0.y, z1.y, z2.y, z3.y);
+                    *reinterpret_cast<float4*>(A.Xout + ba + Lg) = xb;
+                    s4 += (fabsf(xb.x) + fabsf(xb.y)) + (fabsf(xb.z) + fabsf(xb.w));
+                }
+                absacc += (double)s4;
+            } else if (rank == 0) {
+                // Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!, csc_kernels.jl:86-95)
+                const float dx[4] = {z0.x, z1.x, z2.x, z3.x};
+                const float4 yn4 = *reinterpret_cast<const float4*>(y1s + l);
+                const float yn[4] = {yn4.x, yn4.y, yn4.z, yn4.w};
+                float Yo[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int le = l + e;
+                    const bool in = le >= A.gamma && le < A.gamma + A.L4;
+                    const float wts = in ? A.S[(size_t)n * A.L4 + (le - A.gamma)] : 0.f;
+                    const float dg = in ? 1.f : 0.f;
+                    Yo[e] = (wts + A.rho * (dx[e] + yn[e])) / (dg + A.rho);
+                }
+                *reinterpret_cast<float4*>(A.DX + bn + l) = make_float4(dx[0], dx[1], dx[2], dx[3]);
+                *reinterpret_cast<float4*>(A.y1 + bn + l) = yn4;
+                *reinterpret_cast<float4*>(A.Y1 + bn + l) = make_float4(Yo[0], Yo[1], Yo[2], Yo[3]);
+            }
         }
         __syncthreads();
     }

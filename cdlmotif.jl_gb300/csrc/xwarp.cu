@@ -275,7 +275,8 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
     constexpr int Lg4 = Lg / 4;
     constexpr int G = 32 / N1;                  // lane groups per warp
     constexpr int RS = N1 + 1;                  // row stride of the transposed layout
-    constexpr int BUF = P * RS;                 // complex entries per group buffer
+    constexpr int BUF = (P * RS + 1) & ~1;      // complex entries per group buffer, kept even
+                                                // so every region after it stays 16-byte aligned
     constexpr int half = Lg / 2;
     constexpr int F = Lg / 2 + 1;
     constexpr int Fp = (F + 1) & ~1;
@@ -516,7 +517,8 @@ const Variant* find_variant(int Lg) {
 
 size_t warp_smem(int N1, int P, int NG) {
     int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
-    return ((size_t)P * N1 + (size_t)NG * P * (N1 + 1) + 3 * (size_t)Fp) * sizeof(float2) +
+    size_t buf = ((size_t)P * (N1 + 1) + 1) & ~(size_t)1;
+    return ((size_t)P * N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2) +
            (size_t)Lg * sizeof(float);
 }
 
@@ -567,6 +569,18 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
         break;
     }
     if (!P) return nullptr;
+    {
+        // the float4 view of y1s needs a 16-byte aligned offset
+        int G = 32 / v->N1, NG = (P->threads / 32) * G;
+        int F = c->Lg / 2 + 1, Fp = (F + 1) & ~1;
+        size_t buf = ((size_t)v->P * (v->N1 + 1) + 1) & ~(size_t)1;
+        size_t off = ((size_t)v->P * v->N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2);
+        if (off % 16) {
+            delete P;
+            *status = cdlgb_seterr(c, CDLGB_ENOTSUP, "register-FFT layout misaligned (internal)");
+            return nullptr;
+        }
+    }
     // tables
     std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31);
     for (int p : kPrimesW)

@@ -146,6 +146,29 @@ def test_fp32_error_envelope(pkg, built_lib, mode):
             assert rel(getattr(c, f), getattr(ref, f)) < env, f
 
 
+@pytest.mark.parametrize("generic", [False, True])
+def test_headline_shape_parity(pkg, built_lib, generic, monkeypatch):
+    """The N=20000/L=200/K=64/W=16 workload's shapes (Lg = 928 = 2^5 * 29, clusters of
+    8 CTAs) on 6 sequences, 2 outer iterations, through the fused X-step (register-FFT
+    variant, and the generic in-kernel FFT when `generic`)."""
+    if generic:
+        monkeypatch.setenv("CDLGB_GENERIC_FFT", "1")
+    synth = pkg.synth
+    N, L, M, fs = 6, 200, 64, 16
+    bases, _, _ = synth.plant_dataset(5, N, L, [8, 14, 20], [0.3, 0.3, 0.3])
+    S = synth.onehot(bases)
+    Lg = 4 * L + 8 * fs
+    X0 = synth.init_X0(2, N, M, Lg)
+    D0 = synth.init_D0_unit_norm(2, M, Lg, 4 * fs)
+    ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    objs_ref = O.run_outer(ref, 2)
+    with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+        objs = pkg.run_outer(c, 2)
+        np.testing.assert_allclose(objs, objs_ref, rtol=TOL_OBJ)
+        assert rel(c.X, ref.X) < TOL_X and rel(c.d, ref.d) < TOL_X
+        assert rel(c.DX, ref.DX) < TOL_X and rel(c.Y1, ref.Y1) < TOL_X
+
+
 @pytest.mark.parametrize("mode", MODES)
 def test_deterministic(pkg, built_lib, mode):
     rng = np.random.default_rng(9)

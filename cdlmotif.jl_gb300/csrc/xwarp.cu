@@ -76,11 +76,13 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
     return f2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
+// a*b + c = b*a.x + (-b.y, b.x)*a.y + c, two packed FMAs
 __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
-    return f2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+    return rfma(f2(-b.y, b.x), a.y, rfma(b, a.x, c));
 }
-__device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {  // conj(a)*b + c
-    return f2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, c.y)));
+// conj(a)*b + c = b*a.x + (b.y, -b.x)*a.y + c
+__device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {
+    return rfma(f2(b.y, -b.x), a.y, rfma(b, a.x, c));
 }
 template <int SIGN>
 __device__ __forceinline__ float2 mul_i(float2 a) {  // SIGN * i * a
@@ -269,8 +271,8 @@ __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, boo
     v = (Y2 - na) + (Y3 - nb);
 }
 
-template <int N1, int P>
-__global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
+template <int N1, int P, int MINB, bool G1S>
+__global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     constexpr int Lg = N1 * P;
     constexpr int Lg4 = Lg / 4;
     constexpr int G = 32 / N1;                  // lane groups per warp
@@ -294,16 +296,22 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
     float2* Ppart = bufs + (size_t)NG * BUF;
     float2* Wv = Ppart + 2 * Fp;
     float* y1s = reinterpret_cast<float*>(Wv + Fp);
+    float2* g1s = reinterpret_cast<float2*>(y1s + Lg);   // [Mc][F] slice of G1h (G1S only)
     __shared__ double red[kMaxThreads / 32];
 
     for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
+    const int m0 = (int)cluster.block_rank() * A.Mc;
+    if (G1S) {
+        for (int t = threadIdx.x; t < A.Mc * F; t += blockDim.x) g1s[t] = A.G1h[(size_t)m0 * F + t];
+    }
+    // filter m's spectrum at bin f
+    const float2* g1 = G1S ? g1s : A.G1h + (size_t)m0 * F;
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
     const int grp = (threadIdx.x >> 5) * G + lane / N1;   // slot transformed by this lane group
     const int gl = lane % N1;                             // lane within the group
     float2* gbuf = bufs + (size_t)grp * BUF;
-    const int m0 = rank * Mc;
     const float sc = 1.f / (A.kc * (float)Lg);
     const float lam = A.lam;
     double absacc = 0.0;
@@ -383,9 +391,8 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
                 float2 z1 = Z[f], z2 = Z[fr];
                 float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
                 float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-                const int ma = m0 + 2 * sl;
-                P_ = cfma(A.G1h[(size_t)ma * F + f], va, P_);
-                if (2 * sl + 1 < Mc) P_ = cfma(A.G1h[(size_t)(ma + 1) * F + f], vb, P_);
+                P_ = cfma(g1[(2 * sl) * F + f], va, P_);
+                if (2 * sl + 1 < Mc) P_ = cfma(g1[(2 * sl + 1) * F + f], vb, P_);
             }
             Pp[f] = P_;
         }
@@ -422,14 +429,13 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
             const int f = idx - sl * F;
             float2* Z = bufs + (size_t)sl * BUF;
             const bool edge = (f == 0) || (f == half);
-            const int ma = m0 + 2 * sl;
             const bool hasb = 2 * sl + 1 < Mc;
             const float2 W = Wv[f];
             float2 z1 = Z[f], z2 = Z[edge ? f : Lg - f];
             float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
             float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-            float2 xa = cjfma(A.G1h[(size_t)ma * F + f], W, va);
-            float2 xb = hasb ? cjfma(A.G1h[(size_t)(ma + 1) * F + f], W, vb) : f2(0.f, 0.f);
+            float2 xa = cjfma(g1[(2 * sl) * F + f], W, va);
+            float2 xb = hasb ? cjfma(g1[(2 * sl + 1) * F + f], W, vb) : f2(0.f, 0.f);
             xa = f2(xa.x * sc, xa.y * sc);
             xb = f2(xb.x * sc, xb.y * sc);
             if (edge) {
@@ -503,10 +509,12 @@ __global__ void __launch_bounds__(kMaxThreads, 3) k_xstep_warp(WArgs A) {
 
 // ------------------------------------------------------------------ dispatch
 typedef void (*kern_t)(WArgs);
-struct Variant { int N1, P; kern_t k; };
+// k3: three CTAs per SM, G1h read through L2; k2: two CTAs per SM (more registers),
+// the CTA's slice of G1h cached in shared memory
+struct Variant { int N1, P; kern_t k3, k2; };
 const Variant kVariants[] = {
-    {32, 29, k_xstep_warp<32, 29>},
-    {16, 31, k_xstep_warp<16, 31>},
+    {32, 29, k_xstep_warp<32, 29, 3, false>, k_xstep_warp<32, 29, 2, true>},
+    {16, 31, k_xstep_warp<16, 31, 3, false>, k_xstep_warp<16, 31, 2, true>},
 };
 
 const Variant* find_variant(int Lg) {
@@ -515,11 +523,11 @@ const Variant* find_variant(int Lg) {
     return nullptr;
 }
 
-size_t warp_smem(int N1, int P, int NG) {
+size_t warp_smem(int N1, int P, int NG, int g1s_filters) {
     int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
     size_t buf = ((size_t)P * (N1 + 1) + 1) & ~(size_t)1;
     return ((size_t)P * N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2) +
-           (size_t)Lg * sizeof(float);
+           (size_t)Lg * sizeof(float) + (size_t)g1s_filters * F * sizeof(float2);
 }
 
 }  // namespace
@@ -530,13 +538,14 @@ int warp_variant_exists(int Lg, int M) {
     for (int cs : {1, 2, 4, 8}) {
         if (M % cs) continue;
         int B = (M / cs + 1) / 2, G = 32 / v->N1, warps = (B + 1 + G - 1) / G;
-        if (warps * 32 <= kMaxThreads && warp_smem(v->N1, v->P, warps * G) <= kWarpSmemCap) return 1;
+        if (warps * 32 <= kMaxThreads && warp_smem(v->N1, v->P, warps * G, 0) <= kWarpSmemCap) return 1;
     }
     return 0;
 }
 
 struct WarpPlan {
     const Variant* v;
+    kern_t k;
     int CS, Mc, B, threads;
     size_t smem;
     int grid;
@@ -562,10 +571,16 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
         int warps = (B + 1 + G - 1) / G;
         int threads = warps * 32;
         if (threads > kMaxThreads) continue;
-        size_t sm = warp_smem(v->N1, v->P, warps * G);
+        size_t sm = warp_smem(v->N1, v->P, warps * G, 0);
         if (sm > kWarpSmemCap) continue;
         P = new WarpPlan();
         P->v = v; P->CS = cs; P->Mc = mc; P->B = B; P->threads = threads; P->smem = sm;
+        P->k = v->k3;
+        // two-per-SM variant with G1h in shared memory when it fits (default); env
+        // CDLGB_WARP_VARIANT=3 selects the three-per-SM variant
+        const char* ev = getenv("CDLGB_WARP_VARIANT");
+        size_t sm2 = warp_smem(v->N1, v->P, warps * G, mc);
+        if ((!ev || atoi(ev) != 3) && sm2 <= 110 * 1024) { P->k = v->k2; P->smem = sm2; }
         break;
     }
     if (!P) return nullptr;
@@ -599,7 +614,7 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_w32, w32.data(), 32 * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(v->k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem);
     int nclusters = 0;
     if (e == cudaSuccess) {
         cudaLaunchConfig_t cfg = {};
@@ -613,7 +628,7 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
         cfg.dynamicSmemBytes = P->smem;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)v->k, &cfg);
+        e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)P->k, &cfg);
     }
     if (e != cudaSuccess || nclusters < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "register-FFT X-step setup failed: %s",
@@ -666,7 +681,7 @@ int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cdlgb_phase_begin(c, PH_XFUSED);
-    CU_TRY(c, cudaLaunchKernelEx(&cfg, P->v->k, a));
+    CU_TRY(c, cudaLaunchKernelEx(&cfg, P->k, a));
     LAUNCH_CHECK(c, "k_xstep_warp");
     cdlgb_phase_end(c, PH_XFUSED);
     return CDLGB_OK;

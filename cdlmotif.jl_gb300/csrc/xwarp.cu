@@ -320,56 +320,77 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     for (int n = cid; n < A.N; n += nclusters, ++it) {
         const size_t bn = (size_t)n * Lg;
         // ---------------- 1. stream X, y2, y3 in (float4): elementwise pass, duals back to
-        // HBM, V packed two columns per complex entry in the transposed group layout
-        for (int idx = threadIdx.x; idx < (B + 1) * Lg4; idx += blockDim.x) {
-            const int sl = idx / Lg4;
-            const int l4 = idx - sl * Lg4;
-            const int l = 4 * l4;
-            float2* dst = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
-            if (sl < B) {
-                const int ma = m0 + 2 * sl;
-                const bool hasb = 2 * sl + 1 < Mc;
-                const size_t ba = ((size_t)n * M + ma) * Lg + l;
-                float4 x = *reinterpret_cast<const float4*>(A.Xin + ba);
-                float4 a = *reinterpret_cast<const float4*>(A.y2 + ba);
-                float4 c = *reinterpret_cast<const float4*>(A.y3 + ba);
-                float4 xb = make_float4(0, 0, 0, 0), ab = xb, cb = xb;
-                if (hasb) {
-                    xb = *reinterpret_cast<const float4*>(A.Xin + ba + Lg);
-                    ab = *reinterpret_cast<const float4*>(A.y2 + ba + Lg);
-                    cb = *reinterpret_cast<const float4*>(A.y3 + ba + Lg);
+        // HBM, V packed two columns per complex entry in the transposed group layout.
+        // Two items per thread are loaded before any is processed (memory parallelism).
+        {
+            constexpr int kB = 2;
+            const int nitems = (B + 1) * Lg4;
+            for (int base = threadIdx.x; base < nitems; base += kB * blockDim.x) {
+                float4 x[kB][2], a[kB][2], c[kB][2];
+#pragma unroll
+                for (int u = 0; u < kB; ++u) {
+                    const int idx = base + u * blockDim.x;
+                    const int sl = idx / Lg4;
+                    const int l = 4 * (idx - sl * Lg4);
+                    x[u][0] = x[u][1] = a[u][0] = a[u][1] = c[u][0] = c[u][1] = make_float4(0, 0, 0, 0);
+                    if (idx < nitems) {
+                        if (sl < B) {
+                            const size_t ba = ((size_t)n * M + m0 + 2 * sl) * Lg + l;
+                            x[u][0] = *reinterpret_cast<const float4*>(A.Xin + ba);
+                            a[u][0] = *reinterpret_cast<const float4*>(A.y2 + ba);
+                            c[u][0] = *reinterpret_cast<const float4*>(A.y3 + ba);
+                            if (2 * sl + 1 < Mc) {
+                                x[u][1] = *reinterpret_cast<const float4*>(A.Xin + ba + Lg);
+                                a[u][1] = *reinterpret_cast<const float4*>(A.y2 + ba + Lg);
+                                c[u][1] = *reinterpret_cast<const float4*>(A.y3 + ba + Lg);
+                            }
+                        } else {
+                            x[u][0] = *reinterpret_cast<const float4*>(A.Y1 + bn + l);
+                            a[u][0] = *reinterpret_cast<const float4*>(A.y1 + bn + l);
+                            c[u][0] = *reinterpret_cast<const float4*>(A.DX + bn + l);
+                        }
+                    }
                 }
-                float4 na, nb, va, vb = make_float4(0, 0, 0, 0);
-                xprep1(x.x, a.x, c.x, lam, true, na.x, nb.x, va.x);   // .x is on the 4-stride
-                xprep1(x.y, a.y, c.y, lam, false, na.y, nb.y, va.y);
-                xprep1(x.z, a.z, c.z, lam, false, na.z, nb.z, va.z);
-                xprep1(x.w, a.w, c.w, lam, false, na.w, nb.w, va.w);
-                *reinterpret_cast<float4*>(A.y2 + ba) = na;
-                *reinterpret_cast<float4*>(A.y3 + ba) = nb;
-                if (hasb) {
-                    xprep1(xb.x, ab.x, cb.x, lam, true, na.x, nb.x, vb.x);
-                    xprep1(xb.y, ab.y, cb.y, lam, false, na.y, nb.y, vb.y);
-                    xprep1(xb.z, ab.z, cb.z, lam, false, na.z, nb.z, vb.z);
-                    xprep1(xb.w, ab.w, cb.w, lam, false, na.w, nb.w, vb.w);
-                    *reinterpret_cast<float4*>(A.y2 + ba + Lg) = na;
-                    *reinterpret_cast<float4*>(A.y3 + ba + Lg) = nb;
+#pragma unroll
+                for (int u = 0; u < kB; ++u) {
+                    const int idx = base + u * blockDim.x;
+                    if (idx >= nitems) break;
+                    const int sl = idx / Lg4;
+                    const int l = 4 * (idx - sl * Lg4);
+                    float2* dst = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
+                    if (sl < B) {
+                        const size_t ba = ((size_t)n * M + m0 + 2 * sl) * Lg + l;
+                        float4 na, nb, va, vb = make_float4(0, 0, 0, 0);
+                        xprep1(x[u][0].x, a[u][0].x, c[u][0].x, lam, true, na.x, nb.x, va.x);   // .x: 4-stride
+                        xprep1(x[u][0].y, a[u][0].y, c[u][0].y, lam, false, na.y, nb.y, va.y);
+                        xprep1(x[u][0].z, a[u][0].z, c[u][0].z, lam, false, na.z, nb.z, va.z);
+                        xprep1(x[u][0].w, a[u][0].w, c[u][0].w, lam, false, na.w, nb.w, va.w);
+                        *reinterpret_cast<float4*>(A.y2 + ba) = na;
+                        *reinterpret_cast<float4*>(A.y3 + ba) = nb;
+                        if (2 * sl + 1 < Mc) {
+                            xprep1(x[u][1].x, a[u][1].x, c[u][1].x, lam, true, na.x, nb.x, vb.x);
+                            xprep1(x[u][1].y, a[u][1].y, c[u][1].y, lam, false, na.y, nb.y, vb.y);
+                            xprep1(x[u][1].z, a[u][1].z, c[u][1].z, lam, false, na.z, nb.z, vb.z);
+                            xprep1(x[u][1].w, a[u][1].w, c[u][1].w, lam, false, na.w, nb.w, vb.w);
+                            *reinterpret_cast<float4*>(A.y2 + ba + Lg) = na;
+                            *reinterpret_cast<float4*>(A.y3 + ba + Lg) = nb;
+                        }
+                        dst[0] = f2(va.x, vb.x);
+                        dst[1] = f2(va.y, vb.y);
+                        dst[2] = f2(va.z, vb.z);
+                        dst[3] = f2(va.w, vb.w);
+                    } else {
+                        // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
+                        const float4 Yv = x[u][0], yv = a[u][0], dv = c[u][0];
+                        float4 yn = make_float4((yv.x + dv.x) - Yv.x, (yv.y + dv.y) - Yv.y,
+                                                (yv.z + dv.z) - Yv.z, (yv.w + dv.w) - Yv.w);
+                        *reinterpret_cast<float4*>(y1s + l) = yn;
+                        dst[0] = f2(Yv.x - yn.x, 0.f);
+                        dst[1] = f2(Yv.y - yn.y, 0.f);
+                        dst[2] = f2(Yv.z - yn.z, 0.f);
+                        dst[3] = f2(Yv.w - yn.w, 0.f);
+                    }
                 }
-                dst[0] = f2(va.x, vb.x);
-                dst[1] = f2(va.y, vb.y);
-                dst[2] = f2(va.z, vb.z);
-                dst[3] = f2(va.w, vb.w);
-            } else {
-                // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
-                float4 Yv = *reinterpret_cast<const float4*>(A.Y1 + bn + l);
-                float4 yv = *reinterpret_cast<const float4*>(A.y1 + bn + l);
-                float4 dv = *reinterpret_cast<const float4*>(A.DX + bn + l);
-                float4 yn = make_float4((yv.x + dv.x) - Yv.x, (yv.y + dv.y) - Yv.y,
-                                        (yv.z + dv.z) - Yv.z, (yv.w + dv.w) - Yv.w);
-                *reinterpret_cast<float4*>(y1s + l) = yn;
-                dst[0] = f2(Yv.x - yn.x, 0.f);
-                dst[1] = f2(Yv.y - yn.y, 0.f);
-                dst[2] = f2(Yv.z - yn.z, 0.f);
-                dst[3] = f2(Yv.w - yn.w, 0.f);
             }
         }
         __syncthreads();

@@ -59,6 +59,8 @@ SIGNATURES = {
     "cdlgb_set_stream": (C.c_int, [_vp, _vp]),
     "cdlgb_profile": (C.c_int, [_vp, C.c_int32]),
     "cdlgb_profile_read": (C.c_int, [_vp, _f64p, _i64p, _i64p, _i64p, C.c_int32]),
+    "cdlgb_objective_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32,
+                                          C.c_int32, C.c_float, _f64p, _vp]),
 }
 
 _lib = None

@@ -200,6 +200,21 @@ int cdlgb_profile(cdlgb_ctx* ctx, int32_t enable);
 int cdlgb_profile_read(cdlgb_ctx* ctx, double* ms, int64_t* counts, int64_t* launches,
                        int64_t* fft_calls, int32_t reset);
 
+/* ---- Allocation-free objective.  No counterpart in the reference. ----
+ * objective (src/SETUP/CDL_setup.jl:286's formula, 0.5*||W*DX - S||^2 + lambda*sum|X|)
+ * of caller-owned DEVICE buffers X (Lg, M, N) col-major, DX (Lg, N), S (4L, N), with
+ * Lg = L4 + 2*gamma, accumulated in float64; the value is written to *obj (host).
+ * It calls no cudaMalloc / cudaFree: for callers whose device memory belongs to their
+ * own allocator (e.g. a CUDA.jl memory pool holding the free memory, or a serving loop
+ * with a fixed budget).  Its scratch is a static 1 MiB device array: at most 65536
+ * sequences (larger N returns CDLGB_EINVAL before any GPU work); every call shares it,
+ * so calls that overlap on the GPU race; the first call on a device looks up the
+ * array's address and should come before any stream capture.  stream: cudaStream_t or
+ * NULL (legacy default stream). */
+int cdlgb_objective_noalloc(const float* X, const float* DX, const float* S, int32_t L4,
+                            int32_t N, int32_t M, int32_t gamma, float lambda, double* obj,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -315,51 +315,87 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     const float sc = 1.f / (A.kc * (float)Lg);
     const float lam = A.lam;
     double absacc = 0.0;
-    int it = 0;
 
-    for (int n = cid; n < A.N; n += nclusters, ++it) {
-        const size_t bn = (size_t)n * Lg;
-        // ---------------- 1. stream X, y2, y3 in (float4): elementwise pass, duals back to
-        // HBM, V packed two columns per complex entry in the transposed group layout.
-        // Two items per thread are loaded before any is processed (memory parallelism).
-        {
-            constexpr int kB = 2;
-            const int nitems = (B + 1) * Lg4;
-            for (int base = threadIdx.x; base < nitems; base += kB * blockDim.x) {
-                float4 x[kB][2], a[kB][2], c[kB][2];
+    // Streamed pass over the items (slot, 4 consecutive rows): stores the results of
+    // sequence ns (X of the filter pairs; on rank 0 also DX, y1', Y1) from the group
+    // buffers and loads sequence nl (shrink!, projectionX!, the dual updates written
+    // back, V and U packed into the same buffer positions).  Either may be -1.  Loads of
+    // kB items are issued before any item is processed.
+    auto streamed = [&](int ns, int nl) {
+        constexpr int kB = 2;
+        const int nitems = (B + 1) * Lg4;
+        for (int base = threadIdx.x; base < nitems; base += kB * blockDim.x) {
+            float4 x[kB][2], a[kB][2], c[kB][2];
 #pragma unroll
-                for (int u = 0; u < kB; ++u) {
-                    const int idx = base + u * blockDim.x;
-                    const int sl = idx / Lg4;
-                    const int l = 4 * (idx - sl * Lg4);
-                    x[u][0] = x[u][1] = a[u][0] = a[u][1] = c[u][0] = c[u][1] = make_float4(0, 0, 0, 0);
-                    if (idx < nitems) {
-                        if (sl < B) {
-                            const size_t ba = ((size_t)n * M + m0 + 2 * sl) * Lg + l;
-                            x[u][0] = *reinterpret_cast<const float4*>(A.Xin + ba);
-                            a[u][0] = *reinterpret_cast<const float4*>(A.y2 + ba);
-                            c[u][0] = *reinterpret_cast<const float4*>(A.y3 + ba);
-                            if (2 * sl + 1 < Mc) {
-                                x[u][1] = *reinterpret_cast<const float4*>(A.Xin + ba + Lg);
-                                a[u][1] = *reinterpret_cast<const float4*>(A.y2 + ba + Lg);
-                                c[u][1] = *reinterpret_cast<const float4*>(A.y3 + ba + Lg);
-                            }
-                        } else {
-                            x[u][0] = *reinterpret_cast<const float4*>(A.Y1 + bn + l);
-                            a[u][0] = *reinterpret_cast<const float4*>(A.y1 + bn + l);
-                            c[u][0] = *reinterpret_cast<const float4*>(A.DX + bn + l);
+            for (int u = 0; u < kB; ++u) {
+                const int idx = base + u * blockDim.x;
+                const int sl = idx / Lg4;
+                const int l = 4 * (idx - sl * Lg4);
+                x[u][0] = x[u][1] = a[u][0] = a[u][1] = c[u][0] = c[u][1] = make_float4(0, 0, 0, 0);
+                if (idx < nitems && nl >= 0) {
+                    if (sl < B) {
+                        const size_t ba = ((size_t)nl * M + m0 + 2 * sl) * Lg + l;
+                        x[u][0] = *reinterpret_cast<const float4*>(A.Xin + ba);
+                        a[u][0] = *reinterpret_cast<const float4*>(A.y2 + ba);
+                        c[u][0] = *reinterpret_cast<const float4*>(A.y3 + ba);
+                        if (2 * sl + 1 < Mc) {
+                            x[u][1] = *reinterpret_cast<const float4*>(A.Xin + ba + Lg);
+                            a[u][1] = *reinterpret_cast<const float4*>(A.y2 + ba + Lg);
+                            c[u][1] = *reinterpret_cast<const float4*>(A.y3 + ba + Lg);
                         }
+                    } else {
+                        const size_t bl = (size_t)nl * Lg + l;
+                        x[u][0] = *reinterpret_cast<const float4*>(A.Y1 + bl);
+                        a[u][0] = *reinterpret_cast<const float4*>(A.y1 + bl);
+                        c[u][0] = *reinterpret_cast<const float4*>(A.DX + bl);
                     }
                 }
+            }
 #pragma unroll
-                for (int u = 0; u < kB; ++u) {
-                    const int idx = base + u * blockDim.x;
-                    if (idx >= nitems) break;
-                    const int sl = idx / Lg4;
-                    const int l = 4 * (idx - sl * Lg4);
-                    float2* dst = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
+            for (int u = 0; u < kB; ++u) {
+                const int idx = base + u * blockDim.x;
+                if (idx >= nitems) break;
+                const int sl = idx / Lg4;
+                const int l = 4 * (idx - sl * Lg4);
+                float2* z = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
+                // ---- results of sequence ns
+                if (ns >= 0) {
+                    const float2 z0 = z[0], z1 = z[1], z2 = z[2], z3 = z[3];
                     if (sl < B) {
-                        const size_t ba = ((size_t)n * M + m0 + 2 * sl) * Lg + l;
+                        const size_t ba = ((size_t)ns * M + m0 + 2 * sl) * Lg + l;
+                        const float4 xa = make_float4(z0.x, z1.x, z2.x, z3.x);
+                        *reinterpret_cast<float4*>(A.Xout + ba) = xa;
+                        float s4 = (fabsf(xa.x) + fabsf(xa.y)) + (fabsf(xa.z) + fabsf(xa.w));
+                        if (2 * sl + 1 < Mc) {
+                            const float4 xb = make_float4(z0.y, z1.y, z2.y, z3.y);
+                            *reinterpret_cast<float4*>(A.Xout + ba + Lg) = xb;
+                            s4 += (fabsf(xb.x) + fabsf(xb.y)) + (fabsf(xb.z) + fabsf(xb.w));
+                        }
+                        absacc += (double)s4;
+                    } else if (rank == 0) {
+                        // Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!, csc_kernels.jl:86-95)
+                        const float dx[4] = {z0.x, z1.x, z2.x, z3.x};
+                        const float4 yn4 = *reinterpret_cast<const float4*>(y1s + l);
+                        const float yn[4] = {yn4.x, yn4.y, yn4.z, yn4.w};
+                        float Yo[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int le = l + e;
+                            const bool in = le >= A.gamma && le < A.gamma + A.L4;
+                            const float wts = in ? A.S[(size_t)ns * A.L4 + (le - A.gamma)] : 0.f;
+                            const float dg = in ? 1.f : 0.f;
+                            Yo[e] = (wts + A.rho * (dx[e] + yn[e])) / (dg + A.rho);
+                        }
+                        const size_t bs = (size_t)ns * Lg + l;
+                        *reinterpret_cast<float4*>(A.DX + bs) = make_float4(dx[0], dx[1], dx[2], dx[3]);
+                        *reinterpret_cast<float4*>(A.y1 + bs) = yn4;
+                        *reinterpret_cast<float4*>(A.Y1 + bs) = make_float4(Yo[0], Yo[1], Yo[2], Yo[3]);
+                    }
+                }
+                // ---- inputs of sequence nl
+                if (nl >= 0) {
+                    if (sl < B) {
+                        const size_t ba = ((size_t)nl * M + m0 + 2 * sl) * Lg + l;
                         float4 na, nb, va, vb = make_float4(0, 0, 0, 0);
                         xprep1(x[u][0].x, a[u][0].x, c[u][0].x, lam, true, na.x, nb.x, va.x);   // .x: 4-stride
                         xprep1(x[u][0].y, a[u][0].y, c[u][0].y, lam, false, na.y, nb.y, va.y);
@@ -375,33 +411,37 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
                             *reinterpret_cast<float4*>(A.y2 + ba + Lg) = na;
                             *reinterpret_cast<float4*>(A.y3 + ba + Lg) = nb;
                         }
-                        dst[0] = f2(va.x, vb.x);
-                        dst[1] = f2(va.y, vb.y);
-                        dst[2] = f2(va.z, vb.z);
-                        dst[3] = f2(va.w, vb.w);
+                        z[0] = f2(va.x, vb.x);
+                        z[1] = f2(va.y, vb.y);
+                        z[2] = f2(va.z, vb.z);
+                        z[3] = f2(va.w, vb.w);
                     } else {
                         // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
                         const float4 Yv = x[u][0], yv = a[u][0], dv = c[u][0];
-                        float4 yn = make_float4((yv.x + dv.x) - Yv.x, (yv.y + dv.y) - Yv.y,
-                                                (yv.z + dv.z) - Yv.z, (yv.w + dv.w) - Yv.w);
+                        const float4 yn = make_float4((yv.x + dv.x) - Yv.x, (yv.y + dv.y) - Yv.y,
+                                                      (yv.z + dv.z) - Yv.z, (yv.w + dv.w) - Yv.w);
                         *reinterpret_cast<float4*>(y1s + l) = yn;
-                        dst[0] = f2(Yv.x - yn.x, 0.f);
-                        dst[1] = f2(Yv.y - yn.y, 0.f);
-                        dst[2] = f2(Yv.z - yn.z, 0.f);
-                        dst[3] = f2(Yv.w - yn.w, 0.f);
+                        z[0] = f2(Yv.x - yn.x, 0.f);
+                        z[1] = f2(Yv.y - yn.y, 0.f);
+                        z[2] = f2(Yv.z - yn.z, 0.f);
+                        z[3] = f2(Yv.w - yn.w, 0.f);
                     }
                 }
             }
         }
-        __syncthreads();
+    };
 
-        // ---------------- 2. forward transforms, one slot per lane group
+    int it = 0;
+    if (cid < A.N) streamed(-1, cid);
+    __syncthreads();
+    for (int n = cid; n < A.N; n += nclusters, ++it) {
+        // ---------------- forward transforms, one slot per lane group
         if (grp <= B) fwd_step1<N1, P>(gbuf, gl, tw2);
         __syncwarp();
         fwd_step2<N1, P>(gbuf, gl, grp <= B);
         __syncthreads();
 
-        // ---------------- 3. split + this CTA's part of P = sum_m G1h[m] Vh[m]
+        // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
         float2* Pp = Ppart + (it & 1) * Fp;
         for (int f = threadIdx.x; f < F; f += blockDim.x) {
             float2 P_ = f2(0.f, 0.f);
@@ -409,9 +449,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
             const int fr = edge ? f : Lg - f;
             for (int sl = 0; sl < B; ++sl) {
                 const float2* Z = bufs + (size_t)sl * BUF;
-                float2 z1 = Z[f], z2 = Z[fr];
-                float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-                float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+                const float2 z1 = Z[f], z2 = Z[fr];
+                const float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+                const float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
                 P_ = cfma(g1[(2 * sl) * F + f], va, P_);
                 if (2 * sl + 1 < Mc) P_ = cfma(g1[(2 * sl + 1) * F + f], vb, P_);
             }
@@ -419,7 +459,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
         }
         cluster.sync();
 
-        // ---------------- 4. P over the cluster, alpha, W; rank 0 packs DXh
+        // ---------------- P over the cluster (fixed rank order), alpha, W; rank 0 packs
+        // DXh = (P + A W)/(k Lg); every CTA repacks Xh = (Vh + conj(G1h) W)/(k Lg)
         {
             float2* ZU = bufs + (size_t)B * BUF;
             for (int f = threadIdx.x; f < F; f += blockDim.x) {
@@ -428,47 +469,40 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
                 const float Av = A.Ah[f];
                 const float2 U = ZU[f];
                 const float inv_s = 1.f / (Av + A.kc);
-                float2 alpha = f2(fmaf(Av, U.x, P_.x) * inv_s, fmaf(Av, U.y, P_.y) * inv_s);
-                float2 W = csub(U, alpha);
-                Wv[f] = W;
+                const float2 alpha = f2(fmaf(Av, U.x, P_.x) * inv_s, fmaf(Av, U.y, P_.y) * inv_s);
+                const float2 W = csub(U, alpha);
+                const bool edge = (f == 0) || (f == half);
                 if (rank == 0) {
-                    float2 D = f2(fmaf(Av, W.x, P_.x) * sc, fmaf(Av, W.y, P_.y) * sc);
-                    if (f == 0 || f == half) {
+                    const float2 D = f2(fmaf(Av, W.x, P_.x) * sc, fmaf(Av, W.y, P_.y) * sc);
+                    if (edge) {
                         ZU[f] = f2(D.x, 0.f);
                     } else {
                         ZU[f] = D;
                         ZU[Lg - f] = f2(D.x, -D.y);
                     }
                 }
+                for (int sl = 0; sl < B; ++sl) {
+                    float2* Z = bufs + (size_t)sl * BUF;
+                    const bool hasb = 2 * sl + 1 < Mc;
+                    const float2 z1 = Z[f], z2 = Z[edge ? f : Lg - f];
+                    const float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+                    const float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+                    float2 xa = cjfma(g1[(2 * sl) * F + f], W, va);
+                    float2 xb = hasb ? cjfma(g1[(2 * sl + 1) * F + f], W, vb) : f2(0.f, 0.f);
+                    xa = f2(xa.x * sc, xa.y * sc);
+                    xb = f2(xb.x * sc, xb.y * sc);
+                    if (edge) {
+                        Z[f] = f2(xa.x, xb.x);
+                    } else {
+                        Z[f] = f2(xa.x - xb.y, xa.y + xb.x);
+                        Z[Lg - f] = f2(xa.x + xb.y, xb.x - xa.y);
+                    }
+                }
             }
         }
         __syncthreads();
 
-        // ---------------- 5. Xh = (Vh + conj(G1h) W)/(k Lg), repacked in place
-        for (int idx = threadIdx.x; idx < B * F; idx += blockDim.x) {
-            const int sl = idx / F;
-            const int f = idx - sl * F;
-            float2* Z = bufs + (size_t)sl * BUF;
-            const bool edge = (f == 0) || (f == half);
-            const bool hasb = 2 * sl + 1 < Mc;
-            const float2 W = Wv[f];
-            float2 z1 = Z[f], z2 = Z[edge ? f : Lg - f];
-            float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-            float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-            float2 xa = cjfma(g1[(2 * sl) * F + f], W, va);
-            float2 xb = hasb ? cjfma(g1[(2 * sl + 1) * F + f], W, vb) : f2(0.f, 0.f);
-            xa = f2(xa.x * sc, xa.y * sc);
-            xb = f2(xb.x * sc, xb.y * sc);
-            if (edge) {
-                Z[f] = f2(xa.x, xb.x);
-            } else {
-                Z[f] = f2(xa.x - xb.y, xa.y + xb.x);
-                Z[Lg - f] = f2(xa.x + xb.y, xb.x - xa.y);
-            }
-        }
-        __syncthreads();
-
-        // ---------------- 6. inverse transforms (rank 0 also transforms DX)
+        // ---------------- inverse transforms (rank 0 also transforms DX)
         {
             const bool act = grp < B || (grp == B && rank == 0);
             inv_step2<N1, P>(gbuf, gl, act, tw2);
@@ -476,44 +510,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
         }
         __syncthreads();
 
-        // ---------------- 7. stream X out (float4); rank 0: DX, y1', Y1
-        for (int idx = threadIdx.x; idx < (B + 1) * Lg4; idx += blockDim.x) {
-            const int sl = idx / Lg4;
-            const int l4 = idx - sl * Lg4;
-            const int l = 4 * l4;
-            const float2* src = bufs + (size_t)sl * BUF + (l / N1) * RS + (l % N1);
-            const float2 z0 = src[0], z1 = src[1], z2 = src[2], z3 = src[3];
-            if (sl < B) {
-                const int ma = m0 + 2 * sl;
-                const size_t ba = ((size_t)n * M + ma) * Lg + l;
-                float4 xa = make_float4(z0.x, z1.x, z2.x, z3.x);
-                *reinterpret_cast<float4*>(A.Xout + ba) = xa;
-                float s4 = (fabsf(xa.x) + fabsf(xa.y)) + (fabsf(xa.z) + fabsf(xa.w));
-                if (2 * sl + 1 < Mc) {
-                    float4 xb = make_float4(z0.y, z1.y, z2.y, z3.y);
-                    *reinterpret_cast<float4*>(A.Xout + ba + Lg) = xb;
-                    s4 += (fabsf(xb.x) + fabsf(xb.y)) + (fabsf(xb.z) + fabsf(xb.w));
-                }
-                absacc += (double)s4;
-            } else if (rank == 0) {
-                // Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!, csc_kernels.jl:86-95)
-                const float dx[4] = {z0.x, z1.x, z2.x, z3.x};
-                const float4 yn4 = *reinterpret_cast<const float4*>(y1s + l);
-                const float yn[4] = {yn4.x, yn4.y, yn4.z, yn4.w};
-                float Yo[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int le = l + e;
-                    const bool in = le >= A.gamma && le < A.gamma + A.L4;
-                    const float wts = in ? A.S[(size_t)n * A.L4 + (le - A.gamma)] : 0.f;
-                    const float dg = in ? 1.f : 0.f;
-                    Yo[e] = (wts + A.rho * (dx[e] + yn[e])) / (dg + A.rho);
-                }
-                *reinterpret_cast<float4*>(A.DX + bn + l) = make_float4(dx[0], dx[1], dx[2], dx[3]);
-                *reinterpret_cast<float4*>(A.y1 + bn + l) = yn4;
-                *reinterpret_cast<float4*>(A.Y1 + bn + l) = make_float4(Yo[0], Yo[1], Yo[2], Yo[3]);
-            }
-        }
+        // ---------------- store this sequence, load the cluster's next one
+        const int nn = n + nclusters;
+        streamed(n, nn < A.N ? nn : -1);
         __syncthreads();
     }
     cluster.sync();

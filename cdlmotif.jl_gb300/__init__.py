@@ -44,7 +44,8 @@ from ._lib import CdlgbParams, ptr
 __all__ = ["CDLSetup", "CDL", "CDLGBError", "init_cdl", "code_update", "dict_update",
            "update_best", "objective", "cdl_train", "scan_w_gpu", "overlapping_scan",
            "posdicts2pfms", "count_matrices", "pfm2pwm", "pwm_complement",
-           "save_pfms_as_transfac", "transfac_text", "FIELDS", "build"]
+           "save_pfms_as_transfac", "transfac_text", "FIELDS", "build", "ActivationRecord",
+           "record_training_result", "get_spatial_info", "get_pair_pfms", "select_pairs"]
 
 FIELDS = {"X": 0, "X_best": 1, "d": 2, "D_best": 3, "G1": 4, "G3": 5, "DX": 6, "Y1": 7,
           "y2": 8, "y3": 9, "g1": 10, "g3": 11, "Td": 12, "G2": 13, "g2": 14, "y1": 15}
@@ -351,6 +352,101 @@ def posdicts2pfms(c: CDL, positions: np.ndarray, lens, use_comp=None, pseudocoun
     if st != 0:
         raise CDLGBError(st, "counts_to_pfms")
     return [out[k, : lens[k], :].T.copy() for k in range(K)]
+
+
+# ---------------------------------------------------------------------------- code -> counts
+class ActivationRecord:
+    """activation_record (src/SETUP/SEARCH_setup.jl:6-57), device resident: the codes of
+    `T` trainings over N sequences of L bases with M filters each."""
+
+    def __init__(self, N: int, L: int, M: int, T: int = 2, device: int = 0):
+        h = C.c_void_p()
+        st = _lib.lib().cdlgb_ar_create(int(N), int(L), int(M), int(T), int(device), C.byref(h))
+        if st != 0:
+            raise CDLGBError(st, "cdlgb_ar_create failed")
+        self._h = h
+        self.N, self.L, self.M, self.T = N, L, M, T
+
+    def _check(self, st):
+        if st != 0:
+            msg = _lib.lib().cdlgb_ar_last_error(self._h)
+            raise CDLGBError(st, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().cdlgb_ar_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self):
+        """(uinds, training_num, filter_lengths) of the recorded filters, 1-based."""
+        K = C.c_int32()
+        self._check(_lib.lib().cdlgb_ar_info(self._h, C.byref(K), None, None, None, 0))
+        k = K.value
+        u, t, f = (np.zeros(max(k, 1), np.int32) for _ in range(3))
+        self._check(_lib.lib().cdlgb_ar_info(self._h, C.byref(K), ptr(u, C.c_int32), ptr(t, C.c_int32),
+                                             ptr(f, C.c_int32), max(k, 1)))
+        return u[:k], t[:k], f[:k]
+
+
+def record_training_result(c: CDL, thresh: float, ar: ActivationRecord, train_num: int,
+                           filter_size: int) -> int:
+    """record_training_result! (src/SEARCH/store.jl:1-40): returns the number of
+    filters added."""
+    added = C.c_int32()
+    ar._check(_lib.lib().cdlgb_ar_record(ar._h, c._h, float(thresh), int(train_num),
+                                         int(filter_size), C.byref(added)))
+    return added.value
+
+
+def get_spatial_info(ar: ActivationRecord):
+    """get_spatial_info! (src/SEARCH/store.jl:121-144).  Returns numpy int32 arrays
+    over (maxlen, K, K), non_over (L - minlen - 1, K, K), next_to (K, K), indexed
+    [distance, fc, fr] (Julia [fr, fc, distance])."""
+    u, t, f = ar.info()
+    K = len(u)
+    maxlen, minlen = int(f.max()), int(f.min())
+    over = np.zeros((maxlen, K, K), np.int32)
+    non_over = np.zeros((max(ar.L - minlen - 1, 0), K, K), np.int32)
+    next_to = np.zeros((K, K), np.int32)
+    ar._check(_lib.lib().cdlgb_ar_topology(ar._h, ptr(over, C.c_int32), ptr(non_over, C.c_int32),
+                                           ptr(next_to, C.c_int32)))
+    return over, non_over, next_to
+
+
+def select_pairs(over: np.ndarray, count_threshold: int) -> np.ndarray:
+    """findall(over .> count_threshold) in Julia order (extractions.jl:24-26): rows of
+    1-based (fr, fc, overlap)."""
+    o, fc, fr = np.nonzero(np.asarray(over) > count_threshold)
+    order = np.lexsort((fr, fc, o))
+    return np.stack([fr[order] + 1, fc[order] + 1, o[order] + 1], axis=1).astype(np.int32)
+
+
+def get_pair_pfms(ar: ActivationRecord, c: CDL, over: np.ndarray, count_threshold: int,
+                  filter_size: int):
+    """get_pair_pfms! (src/SEARCH/extractions.jl:18-114) without the p-value thresholds:
+    returns (pairs (P, 3), span_lens (P,), pfms list of (4, span) float32)."""
+    pairs = np.ascontiguousarray(select_pairs(over, count_threshold))
+    P = len(pairs)
+    if P == 0:
+        return pairs, np.zeros(0, np.int32), []
+    max_span = 2 * filter_size - 1
+    out = np.zeros((max_span, 4, P), np.float32)
+    spans = np.zeros(P, np.int32)
+    ar._check(_lib.lib().cdlgb_ar_pair_pfms(ar._h, c._h, ptr(pairs, C.c_int32), P, int(filter_size),
+                                            ptr(out, C.c_float), ptr(spans, C.c_int32)))
+    return pairs, spans, [out[: spans[p], :, p].T.copy() for p in range(P)]
 
 
 def pfm2pwm(pfm, bg=(0.25, 0.25, 0.25, 0.25)):

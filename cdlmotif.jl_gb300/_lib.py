@@ -59,6 +59,13 @@ SIGNATURES = {
     "cdlgb_set_stream": (C.c_int, [_vp, _vp]),
     "cdlgb_profile": (C.c_int, [_vp, C.c_int32]),
     "cdlgb_profile_read": (C.c_int, [_vp, _f64p, _i64p, _i64p, _i64p, C.c_int32]),
+    "cdlgb_ar_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(_vp)]),
+    "cdlgb_ar_destroy": (C.c_int, [_vp]),
+    "cdlgb_ar_last_error": (C.c_char_p, [_vp]),
+    "cdlgb_ar_record": (C.c_int, [_vp, _vp, C.c_double, C.c_int32, C.c_int32, _i32p]),
+    "cdlgb_ar_info": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, C.c_int32]),
+    "cdlgb_ar_topology": (C.c_int, [_vp, _i32p, _i32p, _i32p]),
+    "cdlgb_ar_pair_pfms": (C.c_int, [_vp, _vp, _i32p, C.c_int32, C.c_int32, _f32p, _i32p]),
     "cdlgb_objective_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32,
                                           C.c_int32, C.c_float, _f64p, _vp]),
 }

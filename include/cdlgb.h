@@ -40,6 +40,7 @@ extern "C" {
 #endif
 
 typedef struct cdlgb_ctx cdlgb_ctx;
+typedef struct cdlgb_ar cdlgb_ar;      /* activation record (code -> counts stage) */
 
 typedef enum {
     CDLGB_OK = 0,
@@ -183,6 +184,40 @@ int cdlgb_counts_to_pfms(const int32_t* counts, const int32_t* nseq, const int32
  * writes at most cap bytes including a NUL.  Host only. */
 int64_t cdlgb_transfac_format(const float* pfm, int32_t w, int32_t reverse_complement,
                               char* out, size_t cap);
+
+/* ---- Code -> activations -> filter-pair topology -> pair count matrices. ----
+ * The activation record (activation_record, src/SETUP/SEARCH_setup.jl:6-57) holds, on
+ * the device, the codes of T trainings (X_best rows gamma+1:4:gamma+4L) and their
+ * thresholds; filter k = (training, m) for every filter with an activation. */
+int cdlgb_ar_create(int32_t N, int32_t L, int32_t M, int32_t T, int32_t device, cdlgb_ar** out);
+int cdlgb_ar_destroy(cdlgb_ar* ar);
+const char* cdlgb_ar_last_error(const cdlgb_ar* ar);
+
+/* record_training_result! (src/SEARCH/store.jl:1-40): codes of ctx's X_best, activations
+ * codes > thresh (thresh > 0, e.g. from cdlgb_code_threshold); appends the filters with
+ * any activation (uinds) as filters of training train_num (1-based) with length
+ * filter_size bases.  *added (may be NULL) = the number appended. */
+int cdlgb_ar_record(cdlgb_ar* ar, cdlgb_ctx* ctx, double thresh, int32_t train_num,
+                    int32_t filter_size, int32_t* added);
+
+/* The record's filters: K, and per filter (arrays of >= cap entries, may be NULL) the
+ * 1-based filter index within its training, the training number and the length. */
+int cdlgb_ar_info(const cdlgb_ar* ar, int32_t* K, int32_t* uinds, int32_t* training_num,
+                  int32_t* filter_lengths, int32_t cap);
+
+/* get_spatial_info! / topology_at_nth_pt! (src/SEARCH/store.jl:64-144), cover_starts = 1:
+ * integer counts over all sequences of ordered pairs of activations of filters from
+ * different trainings.  over (K, K, maxlen), non_over (K, K, L - minlen - 1),
+ * next_to (K, K), col-major int32, indexed [fr, fc, distance]. */
+int cdlgb_ar_topology(cdlgb_ar* ar, int32_t* over, int32_t* non_over, int32_t* next_to);
+
+/* get_pair_pfms! (src/SEARCH/extractions.jl:18-114) for the given pairs (P, 3) row-major
+ * (fr, fc, overlap) 1-based (the reference selects overlap counts > count_threshold in
+ * findall order): code-weighted one-hot MSAs summed over sequences, + 0.1 in the span,
+ * normalised by the first column.  ctx holds the data.  pfms (P, 4, 2*filter_size-1)
+ * col-major float32, span_lens (P). */
+int cdlgb_ar_pair_pfms(cdlgb_ar* ar, cdlgb_ctx* ctx, const int32_t* pairs, int32_t P,
+                       int32_t filter_size, float* pfms, int32_t* span_lens);
 
 /* ---- Instrumentation and stream control.  No counterpart in the reference, which
  * times phases with `@time` only (src/WRAPPER/wrap.jl:30,52,54,67,80,100,137). ---- */

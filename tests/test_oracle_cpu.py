@@ -198,3 +198,13 @@ def test_scan_oracle_reproduces_golden():
     np.testing.assert_array_equal(pos, g["pos"])
     np.testing.assert_array_equal(score, g["score"])
     np.testing.assert_array_equal(comp, g["comp"])
+
+
+def test_select_pairs_is_julia_findall_order(pkg, built_lib):
+    """findall on Julia (K, K, maxlen) walks fr fastest, then fc, then the overlap."""
+    rng = np.random.default_rng(9)
+    over = rng.integers(0, 10, (3, 4, 4)).astype(np.int32)
+    got = [tuple(int(v) for v in p) for p in pkg.select_pairs(over, 6)]
+    exp = [(fr + 1, fc + 1, o + 1) for o in range(3) for fc in range(4) for fr in range(4)
+           if over[o, fc, fr] > 6]
+    assert got == exp

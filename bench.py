@@ -300,6 +300,51 @@ def roofline(prof, steps, fused):
             "avg_launch_ms": round(ms_avg, 4)}
 
 
+def serve_requests(n_req: int, seed: int = 77, rate: float = 20.0):
+    """The serving workload's request stream: Poisson arrivals (mean `rate`/s),
+    N log-uniform in [200, 50000], L uniform in [50, 1000] padded to the next FFT-friendly
+    length, 1-6 planted Dirichlet(0.1) motifs of width 8-20 at 10-40 % occupancy."""
+    pkg = _pkg()
+    from cdlmotif_gb300 import serve
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for i in range(n_req):
+        t += rng.exponential(1.0 / rate)
+        N = int(round(np.exp(rng.uniform(np.log(200), np.log(50000)))))
+        L = int(rng.integers(50, 1001))
+        k = int(rng.integers(1, 7))
+        widths = [int(w) for w in rng.integers(8, 21, k)]
+        occ = [float(o) for o in rng.uniform(0.1, 0.4, k)]
+        bases, _, _ = pkg.synth.plant_dataset(seed * 1000 + i, N, L, widths, occ)
+        Lp = serve.friendly_length(L, 16)
+        out.append((t, serve.pad_onehot(pkg.synth.onehot(bases), L, Lp), N, L, Lp))
+    return out
+
+
+def run_serve(args):
+    pkg = _pkg()
+    from cdlmotif_gb300 import serve
+    reqs = serve_requests(args.serve_requests)
+    setup = pkg.CDLSetup(M=32, filter_size=16, lambda_=0.1, rho=1.0, sigma=100.0)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    res = serve.serve_stream(setup, [(t, d) for t, d, *_ in reqs], slots=args.serve_slots,
+                             iter_num=args.serve_iters, seed=1)
+    clocks = sampler.stop()
+    res.pop("results", None)
+    return {"metric": "served datasets/hr (Poisson 20/s, N log-uniform 200-50000, L 50-1000, K=32, W=16)",
+            "value": res["datasets_per_hr"], "unit": "datasets/hr", "higher_is_better": True,
+            "p50_latency_s": res["p50_s"], "p99_latency_s": res["p99_s"],
+            "mean_queue_s": res["mean_queue_s"], "makespan_s": res["makespan_s"],
+            "requests": res["requests"], "completed": res["completed"],
+            "rejected": res["rejected"], "slots": args.serve_slots,
+            "outer_iterations_per_dataset": args.serve_iters, "dtype": "f32",
+            "data": "synthetic (seeded planted motifs)", "clocks": clocks,
+            "config": {"workload": "serving", "requests": args.serve_requests,
+                       "L_padded": [int(r[4]) for r in reqs], "N": [int(r[2]) for r in reqs]}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -312,6 +357,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=0, help="override N (small cases for profiling)")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--serve", action="store_true",
+                    help="serving workload: Poisson request stream, datasets/hr and p50/p99")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-iters", type=int, default=3)
+    ap.add_argument("--serve-slots", type=int, default=8)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.n:
@@ -325,6 +375,11 @@ def main():
               "rho": wl["rho"], "sigma": wl["sigma"], "csc_iter_num": wl["csc_iter"],
               "cdl_iter_num": wl["cdl_iter"], "parallelism": f"replicas{world}",
               "l2": "inputs larger than L2 (ADMM state ~28 GB per replica)"}
+
+    if args.serve:
+        if rank == 0:
+            print(json.dumps(run_serve(args)))
+        return
 
     if args.impl == "reference":
         if world > 1 and rank != 0:

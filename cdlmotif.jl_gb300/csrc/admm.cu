@@ -424,49 +424,71 @@ double host_uniform(uint64_t seed, uint64_t i) {
     return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
 
-int make_plans(cdlgb_ctx* c) {
-    long long n[1] = {c->Lg};
-    long long in_r[1] = {c->Lg}, in_c[1] = {c->F};
+struct PlanEntry { int dir; long long batch; cufftHandle h; };
+typedef std::vector<PlanEntry> PlanCache;
+
+// R2C (dir 0) or C2R (dir 1) plan of length Lg over `batch` contiguous columns
+int get_plan(cdlgb_ctx* c, int dir, long long batch, cufftHandle* out) {
+    if (!c->plans) c->plans = new PlanCache();
+    PlanCache& pc = *(PlanCache*)c->plans;
+    for (auto& e : pc)
+        if (e.dir == dir && e.batch == batch) { *out = e.h; return CDLGB_OK; }
+    long long n[1] = {c->Lg}, in_r[1] = {c->Lg}, in_c[1] = {c->F};
     size_t ws = 0;
-    long long bLMN = (long long)c->M * c->N, bLN = c->N, bLM = c->M;
-    FFT_TRY(c, cufftCreate(&c->pR2C_LMN));
-    FFT_TRY(c, cufftMakePlanMany64(c->pR2C_LMN, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, bLMN, &ws));
-    FFT_TRY(c, cufftCreate(&c->pC2R_LMN));
-    FFT_TRY(c, cufftMakePlanMany64(c->pC2R_LMN, 1, n, in_c, 1, c->F, in_r, 1, c->Lg, CUFFT_C2R, bLMN, &ws));
-    FFT_TRY(c, cufftCreate(&c->pR2C_LN));
-    FFT_TRY(c, cufftMakePlanMany64(c->pR2C_LN, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, bLN, &ws));
-    FFT_TRY(c, cufftCreate(&c->pC2R_LN));
-    FFT_TRY(c, cufftMakePlanMany64(c->pC2R_LN, 1, n, in_c, 1, c->F, in_r, 1, c->Lg, CUFFT_C2R, bLN, &ws));
-    FFT_TRY(c, cufftCreate(&c->pR2C_LM));
-    FFT_TRY(c, cufftMakePlanMany64(c->pR2C_LM, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, bLM, &ws));
-    c->plans = true;
+    cufftHandle h;
+    FFT_TRY(c, cufftCreate(&h));
+    if (dir == 0)
+        FFT_TRY(c, cufftMakePlanMany64(h, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, batch, &ws));
+    else
+        FFT_TRY(c, cufftMakePlanMany64(h, 1, n, in_c, 1, c->F, in_r, 1, c->Lg, CUFFT_C2R, batch, &ws));
+    FFT_TRY(c, cufftSetStream(h, c->stream));
+    pc.push_back({dir, batch, h});
+    *out = h;
     return CDLGB_OK;
 }
 
 int set_plan_streams(cdlgb_ctx* c) {
     if (!c->plans) return CDLGB_OK;
-    FFT_TRY(c, cufftSetStream(c->pR2C_LMN, c->stream));
-    FFT_TRY(c, cufftSetStream(c->pC2R_LMN, c->stream));
-    FFT_TRY(c, cufftSetStream(c->pR2C_LN, c->stream));
-    FFT_TRY(c, cufftSetStream(c->pC2R_LN, c->stream));
-    FFT_TRY(c, cufftSetStream(c->pR2C_LM, c->stream));
+    for (auto& e : *(PlanCache*)c->plans) FFT_TRY(c, cufftSetStream(e.h, c->stream));
     return CDLGB_OK;
 }
 
-int r2c(cdlgb_ctx* c, cufftHandle p, float* in, float2* out) {
+void free_plans(cdlgb_ctx* c) {
+    if (!c->plans) return;
+    for (auto& e : *(PlanCache*)c->plans) cufftDestroy(e.h);
+    delete (PlanCache*)c->plans;
+    c->plans = nullptr;
+}
+
+int r2c(cdlgb_ctx* c, long long batch, float* in, float2* out) {
+    cufftHandle p;
+    ST_TRY(get_plan(c, 0, batch, &p));
     FFT_TRY(c, cufftExecR2C(p, (cufftReal*)in, (cufftComplex*)out));
     c->fft_calls++;
     return CDLGB_OK;
 }
-int c2r(cdlgb_ctx* c, cufftHandle p, float2* in, float* out) {
+int c2r(cdlgb_ctx* c, long long batch, float2* in, float* out) {
+    cufftHandle p;
+    ST_TRY(get_plan(c, 1, batch, &p));
     FFT_TRY(c, cufftExecC2R(p, (cufftComplex*)in, (cufftReal*)out));
     c->fft_calls++;
     return CDLGB_OK;
 }
 
+// sequences per chunk of the cuFFT passes: the per-sequence scratch (two real and
+// three half-spectrum (Lg, M) slices) times the chunk stays near 2 GiB
+int chunk_for(int N, int M, int Lg) {
+    size_t F = Lg / 2 + 1;
+    size_t per = (size_t)M * (2 * (size_t)Lg * 4 + 3 * F * 8);
+    size_t ch = ((size_t)2 << 30) / per;
+    if (ch < 1) ch = 1;
+    if (ch > (size_t)N) ch = N;
+    return (int)ch;
+}
+
 // G1h = rfft(G1) and A = sum_m |G1h|^2
 int refresh_G1h(cdlgb_ctx* c) {
-    ST_TRY(r2c(c, c->pR2C_LM, c->G1, c->G1h));
+    ST_TRY(r2c(c, c->M, c->G1, c->G1h));
     k_colnorm<<<(c->F + 127) / 128, 128, 0, c->stream>>>(c->G1h, c->Ah, c->F, c->M);
     LAUNCH_CHECK(c, "k_colnorm");
     return CDLGB_OK;
@@ -487,8 +509,9 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
     b += 2 * N * F * 8;                         // LN spectra
     if (fused) b += fused_scratch_bytes((int)Lg, (int)M, N);
-    b += 2 * LMN * 4 + 3 * (size_t)N * M * F * 8;       // cuFFT-path scratch (D-step)
-    b += LMN * 4 / 2;                                   // cuFFT work area (estimate)
+    size_t ch = chunk_for(N, (int)M, (int)Lg);
+    b += ch * M * (2 * Lg * 4 + 3 * F * 8);             // cuFFT-path scratch, one chunk
+    b += ch * M * Lg * 4;                               // cuFFT work area (estimate)
     b += 64ull * 3 * LM * 4;                    // D-step partials
     b += (64u << 20);                           // reductions, scan scratch, slack
     return b;
@@ -523,20 +546,21 @@ int admm_alloc(cdlgb_ctx* c) {
     ST_TRY(A((void**)&c->Ah, (size_t)c->F * 4));
     ST_TRY(A((void**)&c->sUh, (size_t)c->N * c->F * 8));
     ST_TRY(A((void**)&c->sVh, (size_t)c->N * c->F * 8));
-    // spectra of the whole dataset are needed at init (DX) and by the cuFFT path
-    ST_TRY(A((void**)&c->sA, LMN * 4));
-    ST_TRY(A((void**)&c->sAh, (size_t)c->N * c->M * c->F * 8));
-    ST_TRY(A((void**)&c->sB, LMN * 4));
-    ST_TRY(A((void**)&c->sBh, (size_t)c->N * c->M * c->F * 8));
-    ST_TRY(A((void**)&c->sCh, (size_t)c->N * c->M * c->F * 8));
+    // cuFFT-path scratch for one chunk of sequences (init's DX, the D-step, and the
+    // X-step when no fused kernel covers Lg)
+    c->chunk = chunk_for(c->N, c->M, c->Lg);
+    const size_t cLMN = (size_t)c->chunk * c->M * c->Lg, cSp = (size_t)c->chunk * c->M * c->F;
+    ST_TRY(A((void**)&c->sA, cLMN * 4));
+    ST_TRY(A((void**)&c->sAh, cSp * 8));
+    ST_TRY(A((void**)&c->sB, cLMN * 4));
+    ST_TRY(A((void**)&c->sBh, cSp * 8));
+    ST_TRY(A((void**)&c->sCh, cSp * 8));
     c->nchunk = std::max(1, std::min(64, c->N));
     ST_TRY(A((void**)&c->part, (size_t)c->nchunk * 3 * LM * 4));
     c->nred = 152 * 4;
     ST_TRY(A((void**)&c->dred, (size_t)c->nred * 4 * sizeof(double)));
     ST_TRY(A((void**)&c->dscalar, 8 * sizeof(double)));
     CU_TRY(c, cudaMallocHost((void**)&c->hscalar, 8 * sizeof(double)));
-    ST_TRY(make_plans(c));
-    ST_TRY(set_plan_streams(c));
     return CDLGB_OK;
 }
 
@@ -551,11 +575,7 @@ void admm_free(cdlgb_ctx* c) {
     if (c->dscalar) cudaFree(c->dscalar);
     if (c->hscalar) cudaFreeHost(c->hscalar);
     c->dred = nullptr; c->dscalar = nullptr; c->hscalar = nullptr;
-    if (c->plans) {
-        cufftDestroy(c->pR2C_LMN); cufftDestroy(c->pC2R_LMN); cufftDestroy(c->pR2C_LN);
-        cufftDestroy(c->pC2R_LN); cufftDestroy(c->pR2C_LM);
-        c->plans = false;
-    }
+    free_plans(c);
 }
 
 int cdlgb_set_plan_streams(cdlgb_ctx* c) { return set_plan_streams(c); }
@@ -622,12 +642,15 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     CU_TRY(c, cudaMemsetAsync(c->Td, 0, LN * 4, s));
     ST_TRY(refresh_G1h(c));
     // DX = real(ifft(sum_m D-hat .* X-hat)) (CDL_setup.jl:197-203); G2 = DX
-    ST_TRY(r2c(c, c->pR2C_LMN, X, c->sAh));
-    size_t FN = (size_t)c->F * N;
-    k_spec_dot<<<(unsigned)((FN + 255) / 256), 256, 0, s>>>(c->sAh, c->G1h, c->sVh, c->F, M, N,
-                                                          1.f / (float)Lg);
-    LAUNCH_CHECK(c, "k_spec_dot");
-    ST_TRY(c2r(c, c->pC2R_LN, c->sVh, c->DX));
+    for (int n0 = 0; n0 < N; n0 += c->chunk) {
+        const int cn = std::min(c->chunk, N - n0);
+        ST_TRY(r2c(c, (long long)M * cn, X + (size_t)n0 * M * Lg, c->sAh));
+        size_t FN = (size_t)c->F * cn;
+        k_spec_dot<<<(unsigned)((FN + 255) / 256), 256, 0, s>>>(c->sAh, c->G1h, c->sVh + (size_t)n0 * c->F,
+                                                              c->F, M, cn, 1.f / (float)Lg);
+        LAUNCH_CHECK(c, "k_spec_dot");
+    }
+    ST_TRY(c2r(c, N, c->sVh, c->DX));
     CU_TRY(c, cudaMemcpyAsync(c->G2, c->DX, LN * 4, cudaMemcpyDeviceToDevice, s));
     c->initialized = true;
     double obj = 0;
@@ -650,22 +673,26 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
             c->absx_fused = 1;
         } else {
             c->absx_fused = 0;
-            k_xprep<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>(
-                (const float4*)Xin, (float4*)c->y2, (float4*)c->y3, (float4*)c->sA, LMN / 4,
-                c->p.lambda);
-            LAUNCH_CHECK(c, "k_xprep");
+            const int Lg = c->Lg;
             k_xprep_ln<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->y1, c->DX, c->Y1, c->sU, LN);
             LAUNCH_CHECK(c, "k_xprep_ln");
-            ST_TRY(r2c(c, c->pR2C_LMN, c->sA, c->sAh));
-            ST_TRY(r2c(c, c->pR2C_LN, c->sU, c->sUh));
-            int nfb = (F + 127) / 128;
-            k_xsolve<<<(unsigned)((size_t)nfb * N), 128, 0, s>>>(c->sAh, c->sUh, c->G1h, c->Ah,
-                                                                 c->sVh, F, M, nfb,
-                                                                 c->p.sherman_const_csc,
-                                                                 1.f / (float)c->Lg);
-            LAUNCH_CHECK(c, "k_xsolve");
-            ST_TRY(c2r(c, c->pC2R_LMN, c->sAh, Xout));
-            ST_TRY(c2r(c, c->pC2R_LN, c->sVh, c->DX));
+            ST_TRY(r2c(c, N, c->sU, c->sUh));
+            const int nfb = (F + 127) / 128;
+            for (int n0 = 0; n0 < N; n0 += c->chunk) {
+                const int cn = std::min(c->chunk, N - n0);
+                const size_t off = (size_t)n0 * M * Lg, cl = (size_t)cn * M * Lg;
+                k_xprep<<<grid_for(cl / 4, kBlock), kBlock, 0, s>>>(
+                    (const float4*)(Xin + off), (float4*)(c->y2 + off), (float4*)(c->y3 + off),
+                    (float4*)c->sA, cl / 4, c->p.lambda);
+                LAUNCH_CHECK(c, "k_xprep");
+                ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
+                k_xsolve<<<(unsigned)((size_t)nfb * cn), 128, 0, s>>>(
+                    c->sAh, c->sUh + (size_t)n0 * F, c->G1h, c->Ah, c->sVh + (size_t)n0 * F, F, M, nfb,
+                    c->p.sherman_const_csc, 1.f / (float)Lg);
+                LAUNCH_CHECK(c, "k_xsolve");
+                ST_TRY(c2r(c, (long long)M * cn, c->sAh, Xout + off));
+            }
+            ST_TRY(c2r(c, N, c->sVh, c->DX));
             k_mask_update<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Y1, c->DX, c->y1, c->S, c->Lg,
                                                                  c->L4, c->gamma, LN, c->p.rho);
             LAUNCH_CHECK(c, "k_mask_update");
@@ -686,25 +713,29 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
     for (int it = 0; it < iters; ++it) {
         cdlgb_phase_begin(c, PH_DSTEP);
         {
-            k_dprep<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>(
-                (const float4*)cur_X(c), (const float4*)c->y3, (const float4*)c->g1,
-                (const float4*)c->g3, (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA,
-                (float4*)c->sB, LMN / 4, LM / 4);
-            LAUNCH_CHECK(c, "k_dprep");
             k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
             LAUNCH_CHECK(c, "k_sub");
-            ST_TRY(r2c(c, c->pR2C_LMN, c->sA, c->sAh));
-            ST_TRY(r2c(c, c->pR2C_LMN, c->sB, c->sBh));
-            ST_TRY(r2c(c, c->pR2C_LMN, c->d, c->sCh));
-            ST_TRY(r2c(c, c->pR2C_LN, c->sU, c->sUh));
-            int nfb = (F + 127) / 128;
-            k_dsolve<<<(unsigned)((size_t)nfb * N), 128, 0, s>>>(c->sAh, c->sBh, c->sCh, c->sUh,
-                                                                 c->sVh, F, M, nfb,
-                                                                 c->p.sherman_const_cdl,
-                                                                 1.f / (float)Lg);
-            LAUNCH_CHECK(c, "k_dsolve");
-            ST_TRY(c2r(c, c->pC2R_LMN, c->sBh, c->d));
-            ST_TRY(c2r(c, c->pC2R_LN, c->sVh, c->Td));
+            ST_TRY(r2c(c, N, c->sU, c->sUh));
+            const int nfb = (F + 127) / 128;
+            for (int n0 = 0; n0 < N; n0 += c->chunk) {
+                const int cn = std::min(c->chunk, N - n0);
+                const size_t off = (size_t)n0 * M * Lg, cl = (size_t)cn * M * Lg;
+                k_dprep<<<grid_for(cl / 4, kBlock), kBlock, 0, s>>>(
+                    (const float4*)(cur_X(c) + off), (const float4*)(c->y3 + off),
+                    (const float4*)(c->g1 + off), (const float4*)(c->g3 + off),
+                    (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA, (float4*)c->sB,
+                    cl / 4, LM / 4);
+                LAUNCH_CHECK(c, "k_dprep");
+                ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
+                ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh));
+                ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh));
+                k_dsolve<<<(unsigned)((size_t)nfb * cn), 128, 0, s>>>(
+                    c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F, c->sVh + (size_t)n0 * F, F, M, nfb,
+                    c->p.sherman_const_cdl, 1.f / (float)Lg);
+                LAUNCH_CHECK(c, "k_dsolve");
+                ST_TRY(c2r(c, (long long)M * cn, c->sBh, c->d + off));
+            }
+            ST_TRY(c2r(c, N, c->sVh, c->Td));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
                                                          c->gamma, LN, c->p.sigma);
             LAUNCH_CHECK(c, "k_dg2");

@@ -68,8 +68,8 @@ struct cdlgb_ctx {
     // fused path twiddles / plan
     void* fplan = nullptr;
 
-    cufftHandle pR2C_LMN = 0, pC2R_LMN = 0, pR2C_LN = 0, pC2R_LN = 0, pR2C_LM = 0;
-    bool plans = false;
+    void* plans = nullptr;          // cuFFT plan cache keyed by (direction, batch)
+    int chunk = 0;                  // sequences per chunk of the cuFFT-transform passes
 
     // scan scratch
     int32_t* scan_i = nullptr; size_t scan_i_cap = 0;

@@ -573,8 +573,10 @@ int fused_setup(cdlgb_ctx* c) {
         tw[t] = make_float2((float)cos(2.0 * M_PI * t / P->Lg), (float)-sin(2.0 * M_PI * t / P->Lg));
     CU_TRY(c, cudaMalloc((void**)&P->tw, P->Lg * sizeof(float2)));
     CU_TRY(c, cudaMemcpy(P->tw, tw.data(), P->Lg * sizeof(float2), cudaMemcpyHostToDevice));
+    // the attribute is process-wide per kernel: always the same cap, never a
+    // context's own size (contexts with different Lg run concurrently)
     CU_TRY(c, cudaFuncSetAttribute(k_xstep_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)P->smem));
+                                   (int)kSmemCap));
     // persistent grid: as many clusters as can be resident at once (at most one per sequence)
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];

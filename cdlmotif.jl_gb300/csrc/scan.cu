@@ -203,7 +203,7 @@ int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* 
     size_t shm = (size_t)4 * L * sizeof(float);
     if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
     if (shm > 48 * 1024)
-        CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     k_scan_fwd<<<N, kScanThreads, shm, c->stream>>>(c->S, c->scan_f, c->scan_i,
                                                      c->scan_f + (size_t)K * 4 * maxlen, K, maxlen,
                                                      L, dpos);
@@ -226,7 +226,7 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
     size_t shm = (size_t)4 * L * sizeof(float);
     if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
     if (shm > 48 * 1024)
-        CU_TRY(c, cudaFuncSetAttribute(k_scan_both, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        CU_TRY(c, cudaFuncSetAttribute(k_scan_both, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     k_scan_both<<<N, kScanThreads, shm, c->stream>>>(c->S, c->scan_f, c->scan_i,
                                                       c->scan_f + (size_t)K * 4 * maxlen, K,
                                                       maxlen, L, dpos, dscore, c->scan_u);

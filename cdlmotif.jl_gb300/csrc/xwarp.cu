@@ -634,7 +634,8 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_w32, w32.data(), 32 * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem);
+    // process-wide per kernel: the same cap for every context
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024);
     int nclusters = 0;
     if (e == cudaSuccess) {
         cudaLaunchConfig_t cfg = {};

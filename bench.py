@@ -345,6 +345,50 @@ def run_serve(args):
                        "L_padded": [int(r[4]) for r in reqs], "N": [int(r[2]) for r in reqs]}}
 
 
+def run_precision(args):
+    """The float32 path (fused X-step, float64 objective) against the all-FP64 GPU
+    reference from the same initial state, outer iteration by outer iteration: relative
+    L2 error of X, X_best, d, D_best, G1 and the objective gap."""
+    import torch
+    pkg = _pkg()
+    from cdlmotif_gb300.fp64ref import FP64Reference
+    wl = WORKLOAD
+    bases = dataset(wl)
+    S = pkg.synth.onehot(bases)
+    setup = pkg.CDLSetup(M=wl["M"], filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
+                         sigma=wl["sigma"], csc_iter_num=wl["csc_iter"], cdl_iter_num=wl["cdl_iter"])
+    c = pkg.init_cdl(setup, S, seed=wl["seed"])
+    dev = "cuda:0"
+
+    def rel(a32, b64):
+        a = torch.from_numpy(a32).to(dev, torch.float64)
+        return float((a - b64).norm() / b64.norm())
+
+    ref = FP64Reference(S, c.X, c.G1, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"],
+                        device=dev)
+    rows = []
+    t32 = t64 = 0.0
+    for it in range(1, args.precision_iters + 1):
+        t0 = time.perf_counter()
+        o32 = float(pkg.run_outer(c, 1)[0])
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        o64 = ref.run_outer(1)[0]
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        t32 += t1 - t0
+        t64 += t2 - t1
+        rows.append({"outer_iteration": it, "objective_f32": o32, "objective_f64": o64,
+                     "objective_rel_gap": abs(o32 - o64) / abs(o64),
+                     "X_rel_l2": rel(c.X, ref.X), "d_rel_l2": rel(c.d, ref.d),
+                     "X_best_rel_l2": rel(c.X_best, ref.X_best),
+                     "D_best_rel_l2": rel(c.D_best, ref.D_best), "G1_rel_l2": rel(c.G1, ref.G1)})
+    c.close()
+    return {"metric": "precision: float32 path vs all-FP64 GPU reference", "workload": wl["name"],
+            "N": wl["N"], "rows": rows, "seconds_f32": t32, "seconds_f64": t64,
+            "note": "float64 objective / reductions in both; FP64 reference = torch float64 cuFFT"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -362,6 +406,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-iters", type=int, default=3)
     ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--precision", action="store_true",
+                    help="precision study: float32 GPU path vs an all-FP64 GPU reference")
+    ap.add_argument("--precision-iters", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.n:
@@ -379,6 +426,10 @@ def main():
     if args.serve:
         if rank == 0:
             print(json.dumps(run_serve(args)))
+        return
+    if args.precision:
+        if rank == 0:
+            print(json.dumps(run_precision(args)))
         return
 
     if args.impl == "reference":

@@ -294,8 +294,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     float2* tw2 = reinterpret_cast<float2*>(smem4);
     float2* bufs = tw2 + P * N1;
     float2* Ppart = bufs + (size_t)NG * BUF;
-    float2* Ush = Ppart + 2 * Fp;                        // [2][Fp] U-hat of rank 0, by parity
-    float* y1s = reinterpret_cast<float*>(Ush + 2 * Fp);
+    float2* Wv = Ppart + 2 * Fp;
+    float* y1s = reinterpret_cast<float*>(Wv + Fp);
     float2* g1s = reinterpret_cast<float2*>(y1s + Lg);   // [Mc][F] slice of G1h (G1S only)
     __shared__ double red[kMaxThreads / 32];
 
@@ -322,9 +322,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     // back, V and U packed into the same buffer positions).  Either may be -1.  Loads of
     // kB items are issued before any item is processed.
     auto streamed = [&](int ns, int nl) {
-        constexpr int kB = 3;
-        // rank 0 alone transforms U (and later DX): the other ranks skip that slot
-        const int nitems = (rank == 0 ? B + 1 : B) * Lg4;
+        constexpr int kB = 2;
+        const int nitems = (B + 1) * Lg4;
         for (int base = threadIdx.x; base < nitems; base += kB * blockDim.x) {
             float4 x[kB][2], a[kB][2], c[kB][2];
 #pragma unroll
@@ -437,17 +436,14 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     __syncthreads();
     for (int n = cid; n < A.N; n += nclusters, ++it) {
         // ---------------- forward transforms, one slot per lane group
-        const bool fwd_act = grp < B || (grp == B && rank == 0);
-        if (fwd_act) fwd_step1<N1, P>(gbuf, gl, tw2);
+        if (grp <= B) fwd_step1<N1, P>(gbuf, gl, tw2);
         __syncwarp();
-        fwd_step2<N1, P>(gbuf, gl, fwd_act);
+        fwd_step2<N1, P>(gbuf, gl, grp <= B);
         __syncthreads();
 
         // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
         float2* Pp = Ppart + (it & 1) * Fp;
-        float2* Up = Ush + (it & 1) * Fp;
         for (int f = threadIdx.x; f < F; f += blockDim.x) {
-            if (rank == 0) Up[f] = bufs[(size_t)B * BUF + f];
             float2 P_ = f2(0.f, 0.f);
             const bool edge = (f == 0) || (f == half);
             const int fr = edge ? f : Lg - f;
@@ -471,7 +467,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
                 float2 P_ = f2(0.f, 0.f);
                 for (int r = 0; r < CS; ++r) P_ = cadd(P_, cluster.map_shared_rank(Pp, r)[f]);
                 const float Av = A.Ah[f];
-                const float2 U = cluster.map_shared_rank(Up, 0)[f];
+                const float2 U = ZU[f];
                 const float inv_s = 1.f / (Av + A.kc);
                 const float2 alpha = f2(fmaf(Av, U.x, P_.x) * inv_s, fmaf(Av, U.y, P_.y) * inv_s);
                 const float2 W = csub(U, alpha);
@@ -550,7 +546,7 @@ const Variant* find_variant(int Lg) {
 size_t warp_smem(int N1, int P, int NG, int g1s_filters) {
     int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
     size_t buf = ((size_t)P * (N1 + 1) + 1) & ~(size_t)1;
-    return ((size_t)P * N1 + (size_t)NG * buf + 4 * (size_t)Fp) * sizeof(float2) +
+    return ((size_t)P * N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2) +
            (size_t)Lg * sizeof(float) + (size_t)g1s_filters * F * sizeof(float2);
 }
 
@@ -613,7 +609,7 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
         int G = 32 / v->N1, NG = (P->threads / 32) * G;
         int F = c->Lg / 2 + 1, Fp = (F + 1) & ~1;
         size_t buf = ((size_t)v->P * (v->N1 + 1) + 1) & ~(size_t)1;
-        size_t off = ((size_t)v->P * v->N1 + (size_t)NG * buf + 4 * (size_t)Fp) * sizeof(float2);
+        size_t off = ((size_t)v->P * v->N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2);
         if (off % 16) {
             delete P;
             *status = cdlgb_seterr(c, CDLGB_ENOTSUP, "register-FFT layout misaligned (internal)");

@@ -289,11 +289,12 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     const int cid = blockIdx.x / CS;
     const int nclusters = gridDim.x / CS;
     const int B = A.B, Mc = A.Mc, M = A.M;
-    const int NG = (blockDim.x >> 5) * G;
+    const int NG = (blockDim.x >> 5) * G;      // lane groups in the CTA
+    const int Q = (B + 1 + NG - 1) / NG;       // slots (B pairs + the U/DX slot) per group
 
     float2* tw2 = reinterpret_cast<float2*>(smem4);
     float2* bufs = tw2 + P * N1;
-    float2* Ppart = bufs + (size_t)NG * BUF;
+    float2* Ppart = bufs + (size_t)(B + 1) * BUF;
     float2* Wv = Ppart + 2 * Fp;
     float* y1s = reinterpret_cast<float*>(Wv + Fp);
     float2* g1s = reinterpret_cast<float2*>(y1s + Lg);   // [Mc][F] slice of G1h (G1S only)
@@ -309,9 +310,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     __syncthreads();
 
     const int lane = threadIdx.x & 31;
-    const int grp = (threadIdx.x >> 5) * G + lane / N1;   // slot transformed by this lane group
+    const int grp = (threadIdx.x >> 5) * G + lane / N1;   // lane group; transforms slots grp + q*NG
     const int gl = lane % N1;                             // lane within the group
-    float2* gbuf = bufs + (size_t)grp * BUF;
     const float sc = 1.f / (A.kc * (float)Lg);
     const float lam = A.lam;
     double absacc = 0.0;
@@ -435,10 +435,14 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
     if (cid < A.N) streamed(-1, cid);
     __syncthreads();
     for (int n = cid; n < A.N; n += nclusters, ++it) {
-        // ---------------- forward transforms, one slot per lane group
-        if (grp <= B) fwd_step1<N1, P>(gbuf, gl, tw2);
-        __syncwarp();
-        fwd_step2<N1, P>(gbuf, gl, grp <= B);
+        // ---------------- forward transforms, Q slots per lane group
+        for (int q = 0; q < Q; ++q) {
+            const int sl = grp + q * NG;
+            float2* sb = bufs + (size_t)sl * BUF;
+            if (sl <= B) fwd_step1<N1, P>(sb, gl, tw2);
+            __syncwarp();
+            fwd_step2<N1, P>(sb, gl, sl <= B);
+        }
         __syncthreads();
 
         // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
@@ -503,10 +507,12 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
         __syncthreads();
 
         // ---------------- inverse transforms (rank 0 also transforms DX)
-        {
-            const bool act = grp < B || (grp == B && rank == 0);
-            inv_step2<N1, P>(gbuf, gl, act, tw2);
-            if (act) inv_step1<N1, P>(gbuf, gl);
+        for (int q = 0; q < Q; ++q) {
+            const int sl = grp + q * NG;
+            float2* sb = bufs + (size_t)sl * BUF;
+            const bool act = sl < B || (sl == B && rank == 0);
+            inv_step2<N1, P>(sb, gl, act, tw2);
+            if (act) inv_step1<N1, P>(sb, gl);
         }
         __syncthreads();
 
@@ -531,10 +537,13 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
 typedef void (*kern_t)(WArgs);
 // k3: three CTAs per SM, G1h read through L2; k2: two CTAs per SM (more registers),
 // the CTA's slice of G1h cached in shared memory
-struct Variant { int N1, P; kern_t k3, k2; };
+// k2n: two CTAs per SM, G1h read through L2 (for CTAs too large for three per SM)
+struct Variant { int N1, P; kern_t k3, k2, k2n; };
 const Variant kVariants[] = {
-    {32, 29, k_xstep_warp<32, 29, 3, false>, k_xstep_warp<32, 29, 2, true>},
-    {16, 31, k_xstep_warp<16, 31, 3, false>, k_xstep_warp<16, 31, 2, true>},
+    {32, 29, k_xstep_warp<32, 29, 3, false>, k_xstep_warp<32, 29, 2, true>,
+     k_xstep_warp<32, 29, 2, false>},
+    {16, 31, k_xstep_warp<16, 31, 3, false>, k_xstep_warp<16, 31, 2, true>,
+     k_xstep_warp<16, 31, 2, false>},
 };
 
 const Variant* find_variant(int Lg) {
@@ -543,10 +552,10 @@ const Variant* find_variant(int Lg) {
     return nullptr;
 }
 
-size_t warp_smem(int N1, int P, int NG, int g1s_filters) {
+size_t warp_smem(int N1, int P, int slots, int g1s_filters) {
     int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
     size_t buf = ((size_t)P * (N1 + 1) + 1) & ~(size_t)1;
-    return ((size_t)P * N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2) +
+    return ((size_t)P * N1 + (size_t)slots * buf + 3 * (size_t)Fp) * sizeof(float2) +
            (size_t)Lg * sizeof(float) + (size_t)g1s_filters * F * sizeof(float2);
 }
 
@@ -555,11 +564,8 @@ size_t warp_smem(int N1, int P, int NG, int g1s_filters) {
 int warp_variant_exists(int Lg, int M) {
     const Variant* v = find_variant(Lg);
     if (!v) return 0;
-    for (int cs : {1, 2, 4, 8}) {
-        if (M % cs) continue;
-        int B = (M / cs + 1) / 2, G = 32 / v->N1, warps = (B + 1 + G - 1) / G;
-        if (warps * 32 <= kMaxThreads && warp_smem(v->N1, v->P, warps * G, 0) <= kWarpSmemCap) return 1;
-    }
+    for (int cs : {1, 2, 4, 8})
+        if (M % cs == 0 && warp_smem(v->N1, v->P, (M / cs + 1) / 2 + 1, 0) <= kWarpSmemCap) return 1;
     return 0;
 }
 
@@ -582,34 +588,40 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
     int want_cs = 0;
     if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
     WarpPlan* P = nullptr;
+    // smallest cluster whose slots (B pairs + 1) fit the shared-memory cap with at most
+    // 5 warps, each lane group transforming ceil(slots / groups) slots; CDLGB_CLUSTER
+    // forces a cluster size
     for (int cs : {1, 2, 4, 8}) {
         if (c->M % cs) continue;
         if (want_cs && cs != want_cs) continue;
         int mc = c->M / cs;
         int B = (mc + 1) / 2;
         int G = 32 / v->N1;
-        int warps = (B + 1 + G - 1) / G;
+        int slots = B + 1;
+        int warps = (slots + G - 1) / G;
+        if (warps > kMaxThreads / 32) warps = kMaxThreads / 32;
         int threads = warps * 32;
-        if (threads > kMaxThreads) continue;
-        size_t sm = warp_smem(v->N1, v->P, warps * G, 0);
-        if (sm > kWarpSmemCap) continue;
-        P = new WarpPlan();
-        P->v = v; P->CS = cs; P->Mc = mc; P->B = B; P->threads = threads; P->smem = sm;
-        P->k = v->k3;
-        // two-per-SM variant with G1h in shared memory when it fits (default); env
-        // CDLGB_WARP_VARIANT=3 selects the three-per-SM variant
+        const size_t sm = warp_smem(v->N1, v->P, slots, 0);        // G1h through L2
+        const size_t sm2 = warp_smem(v->N1, v->P, slots, mc);      // G1h slice in shared memory
         const char* ev = getenv("CDLGB_WARP_VARIANT");
-        size_t sm2 = warp_smem(v->N1, v->P, warps * G, mc);
-        if ((!ev || atoi(ev) != 3) && sm2 <= 110 * 1024) { P->k = v->k2; P->smem = sm2; }
+        const bool force3 = ev && atoi(ev) == 3;
+        kern_t k = nullptr;
+        size_t bytes = 0;
+        if (!force3 && sm2 <= 110 * 1024) { k = v->k2; bytes = sm2; }       // default
+        else if (sm <= kWarpSmemCap) { k = v->k3; bytes = sm; }             // three per SM
+        else if (want_cs && sm <= 110 * 1024) { k = v->k2n; bytes = sm; }   // forced cluster size
+        if (!k) continue;
+        P = new WarpPlan();
+        P->v = v; P->CS = cs; P->Mc = mc; P->B = B; P->threads = threads; P->smem = bytes;
+        P->k = k;
         break;
     }
     if (!P) return nullptr;
     {
         // the float4 view of y1s needs a 16-byte aligned offset
-        int G = 32 / v->N1, NG = (P->threads / 32) * G;
         int F = c->Lg / 2 + 1, Fp = (F + 1) & ~1;
         size_t buf = ((size_t)v->P * (v->N1 + 1) + 1) & ~(size_t)1;
-        size_t off = ((size_t)v->P * v->N1 + (size_t)NG * buf + 3 * (size_t)Fp) * sizeof(float2);
+        size_t off = ((size_t)v->P * v->N1 + (size_t)(P->B + 1) * buf + 3 * (size_t)Fp) * sizeof(float2);
         if (off % 16) {
             delete P;
             *status = cdlgb_seterr(c, CDLGB_ENOTSUP, "register-FFT layout misaligned (internal)");

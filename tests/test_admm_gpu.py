@@ -146,13 +146,16 @@ def test_fp32_error_envelope(pkg, built_lib, mode):
             assert rel(getattr(c, f), getattr(ref, f)) < env, f
 
 
-@pytest.mark.parametrize("generic", [False, True])
-def test_headline_shape_parity(pkg, built_lib, generic, monkeypatch):
-    """The N=20000/L=200/K=64/W=16 workload's shapes (Lg = 928 = 2^5 * 29, clusters of
-    8 CTAs) on 6 sequences, 2 outer iterations, through the fused X-step (register-FFT
-    variant, and the generic in-kernel FFT when `generic`)."""
-    if generic:
+@pytest.mark.parametrize("variant", ["register_fft", "register_fft_cluster4", "generic"])
+def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
+    """The N=20000/L=200/K=64/W=16 workload's shapes (Lg = 928 = 2^5 * 29) on 6
+    sequences, 2 outer iterations, through the fused X-step: the register-FFT kernel
+    with its default 8-CTA clusters, forced into 4-CTA clusters (two slots per lane
+    group), and the generic in-kernel FFT."""
+    if variant == "generic":
         monkeypatch.setenv("CDLGB_GENERIC_FFT", "1")
+    if variant == "register_fft_cluster4":
+        monkeypatch.setenv("CDLGB_CLUSTER", "4")
     synth = pkg.synth
     N, L, M, fs = 6, 200, 64, 16
     bases, _, _ = synth.plant_dataset(5, N, L, [8, 14, 20], [0.3, 0.3, 0.3])

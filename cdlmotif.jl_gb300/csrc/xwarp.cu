@@ -565,7 +565,7 @@ int warp_variant_exists(int Lg, int M) {
     const Variant* v = find_variant(Lg);
     if (!v) return 0;
     for (int cs : {1, 2, 4, 8})
-        if (M % cs == 0 && warp_smem(v->N1, v->P, (M / cs + 1) / 2 + 1, 0) <= kWarpSmemCap) return 1;
+        if (M % cs == 0 && warp_smem(v->N1, v->P, (M / cs + 1) / 2 + 1, 0) <= 110 * 1024) return 1;
     return 0;
 }
 
@@ -579,7 +579,7 @@ struct WarpPlan {
     double* absx_part;
 };
 
-// Picks the smallest cluster whose CTA fits 3 per SM; returns nullptr when the size
+// Picks the smallest cluster whose CTA fits 2 per SM; returns nullptr when the size
 // has no register-FFT variant.
 void* warp_plan_create(cdlgb_ctx* c, int* status) {
     *status = CDLGB_OK;
@@ -588,8 +588,8 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
     int want_cs = 0;
     if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
     WarpPlan* P = nullptr;
-    // smallest cluster whose slots (B pairs + 1) fit the shared-memory cap with at most
-    // 5 warps, each lane group transforming ceil(slots / groups) slots; CDLGB_CLUSTER
+    // smallest cluster whose slots (B pairs + 1) fit two CTAs per SM with at most 5
+    // warps, each lane group transforming ceil(slots / groups) slots; CDLGB_CLUSTER
     // forces a cluster size
     for (int cs : {1, 2, 4, 8}) {
         if (c->M % cs) continue;
@@ -605,11 +605,15 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
         const size_t sm2 = warp_smem(v->N1, v->P, slots, mc);      // G1h slice in shared memory
         const char* ev = getenv("CDLGB_WARP_VARIANT");
         const bool force3 = ev && atoi(ev) == 3;
+        // Fewest CTAs per cluster that still fit two per SM: each lane group then
+        // transforms more slots per cluster barrier and the U slot is shared by more
+        // filters (measured at L=200, K=64: 4-CTA clusters with two slots per group,
+        // 10.5 ms per X-step, vs 8-CTA clusters with one, 11.7 ms).
         kern_t k = nullptr;
         size_t bytes = 0;
-        if (!force3 && sm2 <= 110 * 1024) { k = v->k2; bytes = sm2; }       // default
-        else if (sm <= kWarpSmemCap) { k = v->k3; bytes = sm; }             // three per SM
-        else if (want_cs && sm <= 110 * 1024) { k = v->k2n; bytes = sm; }   // forced cluster size
+        if (force3 && sm <= kWarpSmemCap) { k = v->k3; bytes = sm; }       // three per SM
+        else if (sm2 <= 110 * 1024) { k = v->k2; bytes = sm2; }            // G1h slice in smem
+        else if (sm <= 110 * 1024) { k = v->k2n; bytes = sm; }             // G1h through L2
         if (!k) continue;
         P = new WarpPlan();
         P->v = v; P->CS = cs; P->Mc = mc; P->B = B; P->threads = threads; P->smem = bytes;

@@ -663,6 +663,20 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
     cudaStream_t s = c->stream;
     const size_t LMN = c->LMN, LN = c->LN;
     const int F = c->F, M = c->M, N = c->N;
+    if (iters > 0 && c->fused && fused_has_multi(c)) {
+        // all iterations in one launch, the state on chip in between
+        cdlgb_phase_begin(c, PH_XSTEP);
+        float* Xin = cur_X(c);
+        float* Xout = c->best_is_cur ? c->Xb[1 - c->xcur] : Xin;
+        ST_TRY(fused_xsteps(c, Xin, Xout, iters));
+        c->absx_fused = 1;
+        if (Xout != Xin) {
+            c->xcur = 1 - c->xcur;
+            c->best_is_cur = 0;
+        }
+        cdlgb_phase_end_n(c, PH_XSTEP, iters);
+        return CDLGB_OK;
+    }
     for (int it = 0; it < iters; ++it) {
         cdlgb_phase_begin(c, PH_XSTEP);
         // X_best aliases the current buffer: write the new X into the other one

@@ -32,6 +32,7 @@ constexpr int kRing = 4096;
 struct Ring {
     cudaEvent_t ev[2 * kRing];
     int ph[kRing];
+    int w[kRing];           // units the interval covers (X-step iterations for PH_XSTEP)
     int used = 0;
     int open[PH_COUNT];
 };
@@ -45,7 +46,7 @@ static void ring_collect(cdlgb_ctx* c) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, r->ev[2 * k], r->ev[2 * k + 1]) == cudaSuccess) {
             c->ph_ms[r->ph[k]] += ms;
-            c->ph_n[r->ph[k]] += 1;
+            c->ph_n[r->ph[k]] += r->w[k];
         }
     }
     r->used = 0;
@@ -57,18 +58,22 @@ void cdlgb_phase_begin(cdlgb_ctx* c, int ph) {
     if (r->used >= kRing) ring_collect(c);
     int k = r->used++;
     r->ph[k] = ph;
+    r->w[k] = 1;
     r->open[ph] = k;
     cudaEventRecord(r->ev[2 * k], c->stream);
 }
 
-void cdlgb_phase_end(cdlgb_ctx* c, int ph) {
+void cdlgb_phase_end_n(cdlgb_ctx* c, int ph, int units) {
     Ring* r = (Ring*)c->ring;
     if (!c->profile || !r) return;
     int k = r->open[ph];
     if (k < 0 || k >= r->used) return;
+    r->w[k] = units;
     cudaEventRecord(r->ev[2 * k + 1], c->stream);
     r->open[ph] = -1;
 }
+
+void cdlgb_phase_end(cdlgb_ctx* c, int ph) { cdlgb_phase_end_n(c, ph, 1); }
 
 // one-hot validation on the device: every entry must be 0 or 1 (the integer count
 // kernels rely on it).  Sets c->onehot_exact; synchronises the stream.

@@ -116,6 +116,7 @@ int cdlgb_after_launch(cdlgb_ctx* c, const char* what);
 // phase timers
 void cdlgb_phase_begin(cdlgb_ctx* c, int ph);
 void cdlgb_phase_end(cdlgb_ctx* c, int ph);
+void cdlgb_phase_end_n(cdlgb_ctx* c, int ph, int units);   // interval covering `units` steps
 
 // ---- admm.cu ----
 int admm_alloc(cdlgb_ctx* c);
@@ -144,6 +145,14 @@ void warp_plan_free(void* p);
 int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout);
 int warp_absx(void* p, const double** part, int* n);
 int warp_variant_exists(int Lg, int M);
+// multi-iteration fused X-step (xiter.cu): all iterations of one code update per launch
+void* iter_plan_create(cdlgb_ctx* c, int* status);
+void iter_plan_free(void* p);
+int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters);
+int iter_absx(void* p, const double** part, int* n);
+int iter_plan_cluster(void* p);
+int fused_has_multi(cdlgb_ctx* c);
+int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 
 // ---- scan.cu ----
 int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,

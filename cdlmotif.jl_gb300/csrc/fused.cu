@@ -52,6 +52,7 @@ struct FusedPlan {
     float2* tw;             // Lg twiddles exp(-2 pi i t / Lg), device
     double* absx_part;      // one partial sum of |X| per CTA
     void* warp;             // register-FFT variant (xwarp.cu) when Lg has one
+    void* iter;             // multi-iteration register-FFT variant (xiter.cu)
 };
 
 struct XArgs {
@@ -553,6 +554,9 @@ int fused_setup(cdlgb_ctx* c) {
     P->F = c->F;
     if (!getenv("CDLGB_GENERIC_FFT")) {
         int st = CDLGB_OK;
+        P->iter = iter_plan_create(c, &st);
+        if (st != CDLGB_OK) return st;
+        if (P->iter) return CDLGB_OK;
         P->warp = warp_plan_create(c, &st);
         if (st != CDLGB_OK) return st;
         if (P->warp) return CDLGB_OK;
@@ -606,13 +610,25 @@ void fused_free(cdlgb_ctx* c) {
     if (P->tw) cudaFree(P->tw);
     if (P->absx_part) cudaFree(P->absx_part);
     warp_plan_free(P->warp);
+    iter_plan_free(P->iter);
     delete P;
     c->fplan = nullptr;
+}
+
+int fused_has_multi(cdlgb_ctx* c) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    return P && P->iter;
+}
+
+int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    return iter_xsteps(c, P->iter, Xin, Xout, iters);
 }
 
 int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs) {
     (void)accum_abs;
     FusedPlan* P = (FusedPlan*)c->fplan;
+    if (P->iter) return iter_xsteps(c, P->iter, Xin, Xout, 1);
     if (P->warp) return warp_xstep(c, P->warp, Xin, Xout);
     XArgs a;
     a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
@@ -647,6 +663,7 @@ int fused_dstep(cdlgb_ctx* c) { return cdlgb_seterr(c, CDLGB_ENOTSUP, "fused D-s
 int fused_absx(cdlgb_ctx* c, const double** part, int* n) {
     FusedPlan* P = (FusedPlan*)c->fplan;
     if (!P) return 0;
+    if (P->iter) return iter_absx(P->iter, part, n);
     if (P->warp) return warp_absx(P->warp, part, n);
     *part = P->absx_part;
     *n = P->grid;

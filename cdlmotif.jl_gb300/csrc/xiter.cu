@@ -1,0 +1,418 @@
+// Fused X-steps: every iteration of one code update (code_update!, src/CDL/train.jl:1-44,
+// csc_iter_num iterations) in one launch, with the per-sequence state resident on chip.
+//
+// The X-step couples the M filters of one sequence and nothing across sequences, and
+// G1 (hence G1-hat and A = sum_m |G1-hat|^2) is fixed for the whole code update.  A
+// cluster of CS CTAs therefore takes one sequence at a time and runs all the
+// iterations on it before moving on:
+//   * each CTA owns Mc = M / CS filters; their duals y2, y3 (2 x Mc x Lg floats) stay in
+//     its shared memory for all iterations;
+//   * X never leaves the chip between iterations: the inverse DFT-P of the X spectrum
+//     leaves X[n1 + N1 n2] in lane n1's column of its slot buffer, where the next
+//     iteration's shrink!/projectionX!/dual updates (csc_kernels.jl:53-82,
+//     train.jl:12-14) turn it into V in place for the forward DFT-P;
+//   * every CTA transforms DX itself (the cross-filter sum P is identical on every
+//     rank, summed in fixed rank order) and keeps y1 in shared memory; Y1 is formed
+//     from DX (update_Y1!, csc_kernels.jl:86-95) and consumed at once.
+// HBM is touched once per sequence per code update: X, y2, y3, Y1, y1, DX are read at
+// the first iteration and X, y2, y3, Y1, y1, DX written after the last.  The
+// arithmetic of every iteration is the one-X-step kernel's (xwarp.cu), operation for
+// operation, so both give the same bits.
+#include "cdlgb_internal.h"
+#include "regfft.cuh"
+
+#include <cooperative_groups.h>
+#include <stdlib.h>
+#include <vector>
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+struct IArgs {
+    const float* Xin;
+    float* Xout;
+    float* y2;
+    float* y3;
+    float* Y1;
+    float* y1;
+    float* DX;
+    const float* S;
+    const float2* G1h;
+    const float* Ah;
+    const float2* tw2;      // [P][N1] exp(-2 pi i n1 k2 / Lg)
+    double* absx_part;
+    int N, M, L4, gamma, iters;
+    float lam, rho, kc;
+    int Mc, B, ld, ld3;     // row strides (floats) of the y2 and compacted y3 rows in shared memory
+};
+
+template <int N1, int P, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
+    constexpr int Lg = N1 * P;
+    constexpr int G = 32 / N1;                  // lane groups per warp
+    constexpr int RS = N1 + 1;
+    constexpr int BUF = (P * RS + 1) & ~1;
+    constexpr int half = Lg / 2;
+    constexpr int F = Lg / 2 + 1;
+    constexpr int Fp = (F + 1) & ~1;
+    extern __shared__ float4 smem4[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CS = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int cid = blockIdx.x / CS;
+    const int nclusters = gridDim.x / CS;
+    constexpr int W3 = 3 * N1 / 4;              // y3 entries per n2 row (l % 4 != 0 only)
+    const int B = A.B, Mc = A.Mc, M = A.M, ld = A.ld, ld3 = A.ld3;
+
+    float2* bufs = reinterpret_cast<float2*>(smem4);       // [B + 1][BUF] slot buffers
+    float2* Ppart = bufs + (size_t)(B + 1) * BUF;          // [2][Fp] this CTA's part of P
+    float2* tw2 = Ppart + 2 * Fp;                          // [P][N1] twiddles
+    float* y2s = reinterpret_cast<float*>(tw2 + P * N1);   // [Mc][ld]
+    // y3 is identically zero on the rows l % 4 == 0: there projectionX! keeps X + y3,
+    // so the update y3 + X - Y3 is (y3 + X) - (X + y3) = +0 exactly.  Only the other
+    // rows are kept, [Mc][ld3], row n2 of lane n1 at n2 W3 + n1 - n1/4 - 1.
+    float* y3s = y2s + (size_t)Mc * ld;
+    float* y1s = y3s + (size_t)Mc * ld3;                   // [Lg]
+    float* Ahs = y1s + Lg;                                 // [Fp] sum_m |G1h|^2
+    float* Ss = Ahs + Fp;                                  // [L4] this sequence's W'S window
+    __shared__ double red[NT / 32];
+
+    for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
+    for (int t = threadIdx.x; t < F; t += blockDim.x) Ahs[t] = A.Ah[t];
+    __syncthreads();
+
+    const int m0 = rank * Mc;
+    const float2* __restrict__ g1 = A.G1h + (size_t)m0 * F;
+    const int lane = threadIdx.x & 31;
+    const int grp = (threadIdx.x >> 5) * G + lane / N1;   // this lane group's slot
+    const int gl = lane % N1;                             // lane within the group
+    const bool act = grp <= B;
+    const bool pair = grp < B;
+    const bool hasb = pair && 2 * grp + 1 < Mc;
+    float2* sb = bufs + (size_t)(act ? grp : 0) * BUF;
+    float* y2a = y2s + (size_t)(pair ? 2 * grp : 0) * ld + gl;
+    const bool keep = (gl & 3) == 0;                      // l = gl + N1 n2, N1 % 4 == 0
+    float* y3a = y3s + (size_t)(pair ? 2 * grp : 0) * ld3 + (keep ? 0 : gl - (gl >> 2) - 1);
+    const float sc = 1.f / (A.kc * (float)Lg);
+    const float lam = A.lam, rho = A.rho;
+    const unsigned gmask = N1 == 32 ? 0xffffffffu : (0xffffu << (lane & 16));   // this lane group
+    double absacc = 0.0;
+    int it = 0;                                           // parity of the P buffers
+
+    for (int n = cid; n < A.N; n += nclusters) {
+        // ---------------- first iteration's inputs, from HBM
+        // (V and U are written to the slot buffer and transformed from there, so that
+        // the HBM loads need no register array)
+        if (pair) {
+            const size_t ra = ((size_t)n * M + m0 + 2 * grp) * Lg + gl;
+#pragma unroll 4
+            for (int n2 = 0; n2 < P; ++n2) {
+                const int o = N1 * n2;
+                float na, nb, va, vb = 0.f;
+                const int o3 = W3 * n2;
+                xprep1(A.Xin[ra + o], A.y2[ra + o], A.y3[ra + o], lam, keep, na, nb, va);
+                y2a[o] = na;
+                if (!keep) y3a[o3] = nb;
+                if (hasb) {
+                    xprep1(A.Xin[ra + Lg + o], A.y2[ra + Lg + o], A.y3[ra + Lg + o], lam, keep, na, nb, vb);
+                    y2a[ld + o] = na;
+                    if (!keep) y3a[ld3 + o3] = nb;
+                }
+                sb[n2 * RS + gl] = f2(va, vb);
+            }
+            fwd_step1<N1, P>(sb, gl, tw2);
+        } else if (act) {
+            // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
+            __syncwarp(gmask);                  // the previous sequence's reads of Ss are done
+            for (int t = gl; t < A.L4; t += N1) Ss[t] = A.S[(size_t)n * A.L4 + t];
+            __syncwarp(gmask);
+            const size_t r = (size_t)n * Lg + gl;
+#pragma unroll 4
+            for (int n2 = 0; n2 < P; ++n2) {
+                const int o = N1 * n2;
+                const float Yv = A.Y1[r + o], yv = A.y1[r + o], dv = A.DX[r + o];
+                const float yn = (yv + dv) - Yv;
+                y1s[gl + o] = yn;
+                sb[n2 * RS + gl] = f2(Yv - yn, 0.f);
+            }
+            fwd_step1<N1, P>(sb, gl, tw2);
+        }
+
+        for (int t = 0; t < A.iters; ++t, ++it) {
+            __syncwarp();
+            fwd_step2<N1, P>(sb, gl, act);
+            __syncthreads();
+
+            // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
+            float2* Pp = Ppart + (it & 1) * Fp;
+            for (int f = threadIdx.x; f < F; f += blockDim.x)
+                Pp[f] = partial_P<Lg>(bufs, BUF, B, Mc, F, f, g1);
+            cluster.sync();
+
+            // ---------------- P over the cluster (fixed rank order), alpha, W; every CTA
+            // packs DXh = (P + A W)/(k Lg) and repacks Xh = (Vh + conj(G1h) W)/(k Lg)
+            {
+                float2* ZU = bufs + (size_t)B * BUF;
+                for (int f = threadIdx.x; f < F; f += blockDim.x) {
+                    const float2 P_ = cluster_sum<8>(cluster, Pp, CS, f);
+                    const float Av = Ahs[f];
+                    const float2 U = ZU[f];
+                    const float inv_s = 1.f / (Av + A.kc);
+                    const float2 alpha = f2(fmaf(Av, U.x, P_.x) * inv_s, fmaf(Av, U.y, P_.y) * inv_s);
+                    const float2 W = csub(U, alpha);
+                    const bool edge = (f == 0) || (f == half);
+                    const float2 D = f2(fmaf(Av, W.x, P_.x) * sc, fmaf(Av, W.y, P_.y) * sc);
+                    if (edge) {
+                        ZU[f] = f2(D.x, 0.f);
+                    } else {
+                        ZU[f] = D;
+                        ZU[Lg - f] = f2(D.x, -D.y);
+                    }
+                    repack_X<Lg>(bufs, BUF, B, Mc, F, f, g1, W, sc);
+                }
+            }
+            __syncthreads();
+
+            // ---------------- inverse transforms; then either the next iteration's
+            // inputs (in registers, straight into the forward DFT-P) or the results
+            inv_step2<N1, P, false>(sb, gl, act, tw2);
+            const bool last = t == A.iters - 1;
+            if (act) inv_step1<N1, P, true>(sb, gl, tw2);   // X (or DX) at T[n2][gl], l = gl + N1 n2
+            if (pair) {
+                if (!last) {
+#pragma unroll 4
+                    for (int n2 = 0; n2 < P; ++n2) {
+                        const int o = N1 * n2;
+                        const int o3 = W3 * n2;
+                        const float2 xv = sb[n2 * RS + gl];
+                        float na, nb, va, vb = 0.f;
+                        xprep1(xv.x, y2a[o], keep ? 0.f : y3a[o3], lam, keep, na, nb, va);
+                        y2a[o] = na;
+                        if (!keep) y3a[o3] = nb;
+                        if (hasb) {
+                            xprep1(xv.y, y2a[ld + o], keep ? 0.f : y3a[ld3 + o3], lam, keep, na, nb, vb);
+                            y2a[ld + o] = na;
+                            if (!keep) y3a[ld3 + o3] = nb;
+                        }
+                        sb[n2 * RS + gl] = f2(va, vb);
+                    }
+                    fwd_step1<N1, P>(sb, gl, tw2);
+                } else {
+                    const size_t ra = ((size_t)n * M + m0 + 2 * grp) * Lg + gl;
+                    float s = 0.f;
+#pragma unroll
+                    for (int n2 = 0; n2 < P; ++n2) {
+                        const int o = N1 * n2;
+                        const float2 xv = sb[n2 * RS + gl];
+                        const int o3 = W3 * n2;
+                        A.Xout[ra + o] = xv.x;
+                        A.y2[ra + o] = y2a[o];
+                        A.y3[ra + o] = keep ? 0.f : y3a[o3];
+                        s += fabsf(xv.x);
+                        if (hasb) {
+                            A.Xout[ra + Lg + o] = xv.y;
+                            A.y2[ra + Lg + o] = y2a[ld + o];
+                            A.y3[ra + Lg + o] = keep ? 0.f : y3a[ld3 + o3];
+                            s += fabsf(xv.y);
+                        }
+                    }
+                    absacc += (double)s;
+                }
+            } else if (act) {
+                // DX, then Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!,
+                // csc_kernels.jl:86-95), then the next iteration's y1' and U
+                const size_t r = (size_t)n * Lg + gl;
+#pragma unroll 4
+                for (int n2 = 0; n2 < P; ++n2) {
+                    const int o = N1 * n2;
+                    const int l = gl + o;
+                    const bool in = l >= A.gamma && l < A.gamma + A.L4;
+                    const float wts = in ? Ss[l - A.gamma] : 0.f;
+                    const float dg = in ? 1.f : 0.f;
+                    const float dx = sb[n2 * RS + gl].x, yp = y1s[l];
+                    const float Y1n = (wts + rho * (dx + yp)) / (dg + rho);
+                    if (!last) {
+                        const float yn = (yp + dx) - Y1n;
+                        y1s[l] = yn;
+                        sb[n2 * RS + gl] = f2(Y1n - yn, 0.f);
+                    } else if (rank == 0) {
+                        A.DX[r + o] = dx;
+                        A.Y1[r + o] = Y1n;
+                        A.y1[r + o] = yp;
+                    }
+                }
+                if (!last) fwd_step1<N1, P>(sb, gl, tw2);
+            }
+        }
+    }
+    cluster.sync();
+
+    for (int o = 16; o > 0; o >>= 1) absacc += __shfl_xor_sync(0xffffffffu, absacc, o);
+    if (lane == 0) red[threadIdx.x >> 5] = absacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        A.absx_part[blockIdx.x] = t;
+    }
+}
+
+// ------------------------------------------------------------------ dispatch
+typedef void (*kern_t)(IArgs);
+constexpr size_t kCap2 = 115200;       // two CTAs per SM (2 x (this + 1 KB reserved) <= 228 KB)
+constexpr size_t kCap1 = 220 * 1024;   // one CTA per SM
+// k2: up to 5 warps, two CTAs per SM; k1: up to 9 warps, one CTA per SM
+struct Variant { int N1, P; kern_t k2, k1; };
+const Variant kVariants[] = {
+    {32, 29, k_xiter<32, 29, 160, 2>, k_xiter<32, 29, 288, 1>},
+    {16, 31, k_xiter<16, 31, 160, 2>, k_xiter<16, 31, 288, 1>},
+};
+
+const Variant* find_variant(int Lg) {
+    for (const Variant& v : kVariants)
+        if (v.N1 * v.P == Lg) return &v;
+    return nullptr;
+}
+
+// row stride of the y2 / y3 rows: with two lane groups per warp (N1 = 16) the groups
+// touch rows 2 apart, which land on opposite bank halves when ld = 8 (mod 16)
+int pad_ld(int N1, int n) {
+    if (N1 == 32) return n;
+    return n + ((8 - n % 16) + 16) % 16;
+}
+
+size_t iter_smem(int N1, int P, int slots, int Mc, int ld, int ld3, int L4) {
+    const int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
+    const size_t buf = ((size_t)P * (N1 + 1) + 1) & ~(size_t)1;
+    return ((size_t)slots * buf + 2 * (size_t)Fp + (size_t)P * N1) * sizeof(float2) +
+           ((size_t)Mc * ld + (size_t)Mc * ld3 + Lg + Fp + L4) * sizeof(float);
+}
+
+struct IterPlan {
+    kern_t k;
+    int CS, Mc, B, ld, ld3, threads, grid;
+    size_t smem;
+    float2* tw2;
+    double* absx_part;
+};
+
+}  // namespace
+
+// Smallest cluster whose CTA fits two per SM (at most 5 warps), else the smallest
+// that fits one per SM (at most 9 warps); CDLGB_CLUSTER forces a cluster size and
+// CDLGB_XITER=0 turns the multi-iteration kernel off.  Returns nullptr when the size
+// has no variant.
+void* iter_plan_create(cdlgb_ctx* c, int* status) {
+    *status = CDLGB_OK;
+    if (const char* e = getenv("CDLGB_XITER"))
+        if (atoi(e) == 0) return nullptr;
+    const Variant* v = find_variant(c->Lg);
+    if (!v) return nullptr;
+    int want_cs = 0;
+    if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
+    const int G = 32 / v->N1;
+    const int ld = pad_ld(v->N1, c->Lg);
+    const int ld3 = pad_ld(v->N1, 3 * v->N1 / 4 * v->P);
+    IterPlan* P = nullptr;
+    for (int pass = 0; pass < 2 && !P; ++pass) {
+        for (int cs : {1, 2, 4, 8}) {
+            if (c->M % cs) continue;
+            if (want_cs && cs != want_cs) continue;
+            const int mc = c->M / cs, B = (mc + 1) / 2, slots = B + 1;
+            const int warps = (slots + G - 1) / G;
+            const size_t sm = iter_smem(v->N1, v->P, slots, mc, ld, ld3, c->L4);
+            kern_t k = nullptr;
+            if (pass == 0 && warps <= 5 && sm <= kCap2) k = v->k2;
+            if (pass == 1 && warps <= 9 && sm <= kCap1) k = v->k1;
+            if (!k) continue;
+            P = new IterPlan();
+            P->k = k; P->CS = cs; P->Mc = mc; P->B = B; P->ld = ld; P->ld3 = ld3;
+            P->threads = warps * 32; P->smem = sm;
+            break;
+        }
+    }
+    if (!P) return nullptr;
+    std::vector<float2> tw2 = regfft_twiddles(v->N1, v->P);
+    cudaError_t e = regfft_upload_tables();
+    if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    // process-wide per kernel: the same cap for every context
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(P->k == v->k2 ? kCap2 : kCap1));
+    int nclusters = 0;
+    if (e == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = P->CS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(P->CS * 152 * 4, 1, 1);
+        cfg.blockDim = dim3(P->threads, 1, 1);
+        cfg.dynamicSmemBytes = P->smem;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaOccupancyMaxActiveClusters(&nclusters, (void*)P->k, &cfg);
+    }
+    if (e == cudaSuccess && nclusters >= 1) {
+        if (nclusters > c->N) nclusters = c->N;
+        P->grid = nclusters * P->CS;
+        e = cudaMalloc((void**)&P->absx_part, (size_t)P->grid * sizeof(double));
+    }
+    if (e != cudaSuccess || nclusters < 1) {
+        *status = cdlgb_seterr(c, CDLGB_ECUDA, "multi-iteration X-step setup failed: %s",
+                               e != cudaSuccess ? cudaGetErrorString(e) : "no cluster fits");
+        if (P->tw2) cudaFree(P->tw2);
+        delete P;
+        return nullptr;
+    }
+    return P;
+}
+
+void iter_plan_free(void* p) {
+    IterPlan* P = (IterPlan*)p;
+    if (!P) return;
+    if (P->tw2) cudaFree(P->tw2);
+    if (P->absx_part) cudaFree(P->absx_part);
+    delete P;
+}
+
+int iter_plan_cluster(void* p) { return p ? ((IterPlan*)p)->CS : 0; }
+
+int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters) {
+    IterPlan* P = (IterPlan*)p;
+    IArgs a;
+    a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
+    a.Y1 = c->Y1; a.y1 = c->y1; a.DX = c->DX; a.S = c->S;
+    a.G1h = c->G1h; a.Ah = c->Ah; a.tw2 = P->tw2; a.absx_part = P->absx_part;
+    a.N = c->N; a.M = c->M; a.L4 = c->L4; a.gamma = c->gamma; a.iters = iters;
+    a.lam = c->p.lambda; a.rho = c->p.rho; a.kc = c->p.sherman_const_csc;
+    a.Mc = P->Mc; a.B = P->B; a.ld = P->ld; a.ld3 = P->ld3;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = P->CS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(P->grid, 1, 1);
+    cfg.blockDim = dim3(P->threads, 1, 1);
+    cfg.dynamicSmemBytes = P->smem;
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cdlgb_phase_begin(c, PH_XFUSED);
+    CU_TRY(c, cudaLaunchKernelEx(&cfg, P->k, a));
+    LAUNCH_CHECK(c, "k_xiter");
+    cdlgb_phase_end(c, PH_XFUSED);
+    return CDLGB_OK;
+}
+
+int iter_absx(void* p, const double** part, int* n) {
+    IterPlan* P = (IterPlan*)p;
+    if (!P) return 0;
+    *part = P->absx_part;
+    *n = P->grid;
+    return 1;
+}

@@ -1,19 +1,13 @@
-// Fused X-step with register-resident four-step FFTs (Lg = N1 * P, N1 in {16, 32}
-// lanes, P an odd prime).  Same algebra and cluster structure as the generic fused
-// kernel (fused.cu), but each packed column pair (and the U / DX slot) is owned by a
-// group of N1 lanes that transforms it without block-wide barriers:
-//   forward  x[n1 + N1 n2] (lane n1 holds n2 = 0..P-1)
-//     1. DFT-P over n2 in registers (pairwise-symmetric form), twiddle w_Lg^(n1 k2),
-//        write T[k2][n1] (row stride N1+1: conflict-free both ways);
-//     2. lane j takes rows r = j + N1 q: DFT-N1 in registers (radix-2 DIF) gives
-//        X[r + P k1], written in natural order into the same buffer.
-//   inverse  the same steps backwards (inverse DFT-N1 per row, conjugate twiddles,
-//     transpose, inverse DFT-P per lane, results streamed to HBM).
-// The block-wide phases between the transforms (split of the packed spectra,
-// cross-filter sums, Sherman-Morrison combine) read and write the spectra in shared
-// memory; the cross-filter sum over the cluster goes through distributed shared
-// memory in fixed rank order.
+// Fused X-step, one ADMM X-step per launch, with register-resident four-step FFTs
+// (regfft.cuh).  Same algebra and cluster structure as the generic fused kernel
+// (fused.cu), but each packed column pair (and the U / DX slot) is owned by a group
+// of N1 lanes that transforms it without block-wide barriers.  The block-wide phases
+// between the transforms (split of the packed spectra, cross-filter sums,
+// Sherman-Morrison combine) read and write the spectra in shared memory; the
+// cross-filter sum over the cluster goes through distributed shared memory in fixed
+// rank order.  The state streams through HBM once per X-step.
 #include "cdlgb_internal.h"
+#include "regfft.cuh"
 
 #include <cooperative_groups.h>
 #include <math.h>
@@ -26,222 +20,6 @@ namespace {
 
 constexpr int kMaxThreads = 160;
 constexpr size_t kWarpSmemCap = 72 * 1024;   // three CTAs per SM
-
-// cos/sin(2 pi m / p) for the odd primes 3..31, concatenated; exp(-2 pi i j / 32)
-__constant__ float2 c_trigw[3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31];
-__constant__ float2 c_w32[32];
-
-__host__ __device__ constexpr int toff(int p) {
-    return p == 3 ? 0 : p == 5 ? 3 : p == 7 ? 8 : p == 11 ? 15 : p == 13 ? 26 : p == 17 ? 39
-         : p == 19 ? 56 : p == 23 ? 75 : p == 29 ? 98 : p == 31 ? 127 : -1;
-}
-const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31};
-
-__host__ __device__ constexpr int brev(int k, int bits) {
-    int r = 0;
-    for (int b = 0; b < bits; ++b) r |= ((k >> b) & 1) << (bits - 1 - b);
-    return r;
-}
-__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
-
-__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
-// Blackwell packed FP32x2 arithmetic (one instruction for both halves, IEEE-identical
-// to the two scalar operations); the pairs are formed inside the asm so that the
-// register allocator can keep them as adjacent registers
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
-        "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 csub(float2 a, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
-        "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return r;
-}
-// a * (c, c) + b  for a complex a and a real c
-__device__ __forceinline__ float2 rfma(float2 a, float c, float2 b) {
-    float2 r;
-    asm("{\n\t.reg .b64 pa, pc, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pc, {%4, %4};\n\t"
-        "mov.b64 pb, {%5, %6};\n\tfma.rn.f32x2 pd, pa, pc, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
-        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(c), "f"(b.x), "f"(b.y));
-    return r;
-}
-__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-    return f2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
-}
-__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
-    return f2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
-}
-// a*b + c = b*a.x + (-b.y, b.x)*a.y + c, two packed FMAs
-__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
-    return rfma(f2(-b.y, b.x), a.y, rfma(b, a.x, c));
-}
-// conj(a)*b + c = b*a.x + (b.y, -b.x)*a.y + c
-__device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {
-    return rfma(f2(b.y, -b.x), a.y, rfma(b, a.x, c));
-}
-template <int SIGN>
-__device__ __forceinline__ float2 mul_i(float2 a) {  // SIGN * i * a
-    return SIGN > 0 ? f2(-a.y, a.x) : f2(a.y, -a.x);
-}
-
-// in-register radix-2 DIF DFT of length N (16 or 32); X[k] ends in x[brev(k)]
-template <int N, int SIGN>
-__device__ __forceinline__ void dft_reg(float2 (&x)[N]) {
-    constexpr int LOG = ilog2c(N);
-#pragma unroll
-    for (int st = 0; st < LOG; ++st) {
-        const int span = N >> (st + 1);
-#pragma unroll
-        for (int blk = 0; blk < N; blk += 2 * span) {
-#pragma unroll
-            for (int j = 0; j < span; ++j) {
-                float2 a = x[blk + j], b = x[blk + j + span];
-                x[blk + j] = cadd(a, b);
-                float2 t = csub(a, b);
-                if (j == 0) {
-                    x[blk + j + span] = t;
-                } else if (4 * j == 2 * span) {          // w = SIGN * i
-                    x[blk + j + span] = mul_i<SIGN>(t);
-                } else {
-                    float2 w = c_w32[j * (32 / (2 * span))];
-                    x[blk + j + span] = SIGN < 0 ? cmul(t, w) : cmulc(t, w);
-                }
-            }
-        }
-    }
-}
-
-// Forward step 1, in place on this lane's column of the group buffer: inputs
-// z[n2] at T[n2][n1], DFT-P over n2, twiddle by w_Lg^(n1 k2), outputs at T[k2][n1].
-template <int N1, int P>
-__device__ __forceinline__ void fwd_step1(float2* __restrict__ T, int n1,
-                                          const float2* __restrict__ tw2) {
-    constexpr int H = (P - 1) / 2;
-    constexpr int OFF = toff(P);
-    constexpr int RS = N1 + 1;
-    float2 x0 = T[n1];
-    float2 s[H], d[H];
-    float2 y0 = x0;
-#pragma unroll
-    for (int j = 1; j <= H; ++j) {
-        float2 a = T[j * RS + n1], b = T[(P - j) * RS + n1];
-        s[j - 1] = cadd(a, b);
-        d[j - 1] = csub(a, b);
-        y0 = cadd(y0, s[j - 1]);
-    }
-    T[n1] = y0;
-#pragma unroll
-    for (int k = 1; k <= H; ++k) {
-        float2 A = x0, B = f2(0.f, 0.f);
-#pragma unroll
-        for (int j = 1; j <= H; ++j) {
-            const float2 cs = c_trigw[OFF + (j * k) % P];
-            A = rfma(s[j - 1], cs.x, A);
-            B = rfma(d[j - 1], cs.y, B);
-        }
-        float2 ib = mul_i<-1>(B);
-        T[k * RS + n1] = cmul(cadd(A, ib), tw2[k * N1 + n1]);
-        T[(P - k) * RS + n1] = cmul(csub(A, ib), tw2[(P - k) * N1 + n1]);
-    }
-}
-
-// Inverse step 1, in place on this lane's column: inputs T[k2][n1] (already
-// twiddled), inverse DFT-P over k2, outputs x[n1 + N1 n2] at T[n2][n1].
-template <int N1, int P>
-__device__ __forceinline__ void inv_step1(float2* __restrict__ T, int n1) {
-    constexpr int H = (P - 1) / 2;
-    constexpr int OFF = toff(P);
-    constexpr int RS = N1 + 1;
-    float2 x0 = T[n1];
-    float2 s[H], d[H];
-    float2 y0 = x0;
-#pragma unroll
-    for (int j = 1; j <= H; ++j) {
-        float2 a = T[j * RS + n1], b = T[(P - j) * RS + n1];
-        s[j - 1] = cadd(a, b);
-        d[j - 1] = csub(a, b);
-        y0 = cadd(y0, s[j - 1]);
-    }
-    T[n1] = y0;
-#pragma unroll
-    for (int k = 1; k <= H; ++k) {
-        float2 A = x0, B = f2(0.f, 0.f);
-#pragma unroll
-        for (int j = 1; j <= H; ++j) {
-            const float2 cs = c_trigw[OFF + (j * k) % P];
-            A = rfma(s[j - 1], cs.x, A);
-            B = rfma(d[j - 1], cs.y, B);
-        }
-        float2 ib = mul_i<1>(B);
-        T[k * RS + n1] = cadd(A, ib);
-        T[(P - k) * RS + n1] = csub(A, ib);
-    }
-}
-
-// Forward step 2: rows of T -> DFT-N1 -> natural-order spectrum Z (same buffer).
-template <int N1, int P>
-__device__ __forceinline__ void fwd_step2(float2* __restrict__ buf, int j, bool active) {
-    constexpr int RQ = (P + N1 - 1) / N1;
-    constexpr int RS = N1 + 1;
-    constexpr int LB = ilog2c(N1);
-    float2 v[RQ][N1];
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-        int r = j + N1 * q;
-        if (active && r < P) {
-#pragma unroll
-            for (int t = 0; t < N1; ++t) v[q][t] = buf[r * RS + t];
-        }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-        int r = j + N1 * q;
-        if (active && r < P) {
-            dft_reg<N1, -1>(v[q]);
-#pragma unroll
-            for (int i = 0; i < N1; ++i) buf[r + P * brev(i, LB)] = v[q][i];   // X[k1] is v[brev(k1)]
-        }
-    }
-    __syncwarp();
-}
-
-// Inverse step 2: natural-order spectrum -> inverse DFT-N1 per row -> conj twiddle -> T.
-template <int N1, int P>
-__device__ __forceinline__ void inv_step2(float2* __restrict__ buf, int j, bool active,
-                                          const float2* __restrict__ tw2) {
-    constexpr int RQ = (P + N1 - 1) / N1;
-    constexpr int RS = N1 + 1;
-    constexpr int LB = ilog2c(N1);
-    float2 v[RQ][N1];
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-        int r = j + N1 * q;
-        if (active && r < P) {
-#pragma unroll
-            for (int k1 = 0; k1 < N1; ++k1) v[q][k1] = buf[r + P * k1];
-        }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int q = 0; q < RQ; ++q) {
-        int r = j + N1 * q;
-        if (active && r < P) {
-            dft_reg<N1, 1>(v[q]);
-#pragma unroll
-            for (int i = 0; i < N1; ++i) {
-                const int n1 = brev(i, LB);
-                buf[r * RS + n1] = cmulc(v[q][i], tw2[r * N1 + n1]);
-            }
-        }
-    }
-    __syncwarp();
-}
 
 struct WArgs {
     const float* Xin;
@@ -260,16 +38,6 @@ struct WArgs {
     float lam, rho, kc;
     int Mc, B;
 };
-
-__device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
-                                       float& na, float& nb, float& v) {
-    float t = x + a;                                        // X + y2
-    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);    // shrink!  (csc_kernels.jl:53-64)
-    float Y3 = keep ? x + b : 0.f;                          // projectionX! (:68-82)
-    na = (a + x) - Y2;                                      // train.jl:13
-    nb = (b + x) - Y3;                                      // train.jl:14
-    v = (Y2 - na) + (Y3 - nb);
-}
 
 template <int N1, int P, int MINB, bool G1S>
 __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
@@ -447,20 +215,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
 
         // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
         float2* Pp = Ppart + (it & 1) * Fp;
-        for (int f = threadIdx.x; f < F; f += blockDim.x) {
-            float2 P_ = f2(0.f, 0.f);
-            const bool edge = (f == 0) || (f == half);
-            const int fr = edge ? f : Lg - f;
-            for (int sl = 0; sl < B; ++sl) {
-                const float2* Z = bufs + (size_t)sl * BUF;
-                const float2 z1 = Z[f], z2 = Z[fr];
-                const float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-                const float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-                P_ = cfma(g1[(2 * sl) * F + f], va, P_);
-                if (2 * sl + 1 < Mc) P_ = cfma(g1[(2 * sl + 1) * F + f], vb, P_);
-            }
-            Pp[f] = P_;
-        }
+        for (int f = threadIdx.x; f < F; f += blockDim.x)
+            Pp[f] = partial_P<Lg>(bufs, BUF, B, Mc, F, f, g1);
         cluster.sync();
 
         // ---------------- P over the cluster (fixed rank order), alpha, W; rank 0 packs
@@ -468,8 +224,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
         {
             float2* ZU = bufs + (size_t)B * BUF;
             for (int f = threadIdx.x; f < F; f += blockDim.x) {
-                float2 P_ = f2(0.f, 0.f);
-                for (int r = 0; r < CS; ++r) P_ = cadd(P_, cluster.map_shared_rank(Pp, r)[f]);
+                const float2 P_ = cluster_sum<8>(cluster, Pp, CS, f);
                 const float Av = A.Ah[f];
                 const float2 U = ZU[f];
                 const float inv_s = 1.f / (Av + A.kc);
@@ -485,23 +240,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
                         ZU[Lg - f] = f2(D.x, -D.y);
                     }
                 }
-                for (int sl = 0; sl < B; ++sl) {
-                    float2* Z = bufs + (size_t)sl * BUF;
-                    const bool hasb = 2 * sl + 1 < Mc;
-                    const float2 z1 = Z[f], z2 = Z[edge ? f : Lg - f];
-                    const float2 va = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-                    const float2 vb = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
-                    float2 xa = cjfma(g1[(2 * sl) * F + f], W, va);
-                    float2 xb = hasb ? cjfma(g1[(2 * sl + 1) * F + f], W, vb) : f2(0.f, 0.f);
-                    xa = f2(xa.x * sc, xa.y * sc);
-                    xb = f2(xb.x * sc, xb.y * sc);
-                    if (edge) {
-                        Z[f] = f2(xa.x, xb.x);
-                    } else {
-                        Z[f] = f2(xa.x - xb.y, xa.y + xb.x);
-                        Z[Lg - f] = f2(xa.x + xb.y, xb.x - xa.y);
-                    }
-                }
+                repack_X<Lg>(bufs, BUF, B, Mc, F, f, g1, W, sc);
             }
         }
         __syncthreads();
@@ -633,21 +372,9 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
         }
     }
     // tables
-    std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31);
-    for (int p : kPrimesW)
-        for (int m = 0; m < p; ++m)
-            trig[toff(p) + m] = make_float2((float)cos(2.0 * M_PI * m / p), (float)sin(2.0 * M_PI * m / p));
-    std::vector<float2> w32(32);
-    for (int j = 0; j < 32; ++j) w32[j] = make_float2((float)cos(2.0 * M_PI * j / 32), (float)-sin(2.0 * M_PI * j / 32));
-    int N1 = v->N1, Pp = v->P, Lg = N1 * Pp;
-    std::vector<float2> tw2((size_t)Pp * N1);
-    for (int k2 = 0; k2 < Pp; ++k2)
-        for (int n1 = 0; n1 < N1; ++n1) {
-            double a = 2.0 * M_PI * (double)((n1 * k2) % Lg) / Lg;
-            tw2[(size_t)k2 * N1 + n1] = make_float2((float)cos(a), (float)-sin(a));
-        }
-    cudaError_t e = cudaMemcpyToSymbol(c_trigw, trig.data(), trig.size() * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_w32, w32.data(), 32 * sizeof(float2));
+    const int N1 = v->N1, Pp = v->P;
+    std::vector<float2> tw2 = regfft_twiddles(N1, Pp);
+    cudaError_t e = regfft_upload_tables();
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
     // process-wide per kernel: the same cap for every context

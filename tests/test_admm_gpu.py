@@ -146,16 +146,20 @@ def test_fp32_error_envelope(pkg, built_lib, mode):
             assert rel(getattr(c, f), getattr(ref, f)) < env, f
 
 
-@pytest.mark.parametrize("variant", ["register_fft", "register_fft_cluster4", "generic"])
+@pytest.mark.parametrize("variant", ["multi_iter", "multi_iter_cluster8", "register_fft",
+                                     "register_fft_cluster8", "generic"])
 def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
     """The N=20000/L=200/K=64/W=16 workload's shapes (Lg = 928 = 2^5 * 29) on 6
-    sequences, 2 outer iterations, through the fused X-step: the register-FFT kernel
-    with its default 8-CTA clusters, forced into 4-CTA clusters (two slots per lane
-    group), and the generic in-kernel FFT."""
+    sequences, 2 outer iterations, through the fused X-step: all iterations of a code
+    update in one launch (default clusters, and 8-CTA clusters), the one-X-step
+    register-FFT kernel (default 4-CTA clusters with two slots per lane group, and
+    8-CTA clusters), and the generic in-kernel FFT."""
     if variant == "generic":
         monkeypatch.setenv("CDLGB_GENERIC_FFT", "1")
-    if variant == "register_fft_cluster4":
-        monkeypatch.setenv("CDLGB_CLUSTER", "4")
+    if variant.startswith("register_fft"):
+        monkeypatch.setenv("CDLGB_XITER", "0")
+    if variant.endswith("cluster8"):
+        monkeypatch.setenv("CDLGB_CLUSTER", "8")
     synth = pkg.synth
     N, L, M, fs = 6, 200, 64, 16
     bases, _, _ = synth.plant_dataset(5, N, L, [8, 14, 20], [0.3, 0.3, 0.3])
@@ -174,6 +178,39 @@ def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
         # path; inside the data window it is what the objective sees
         g, L4 = 4 * fs, 4 * L
         assert rel(c.DX[:, g:g + L4], ref.DX[:, g:g + L4]) < 10 * TOL_X
+
+
+@pytest.mark.parametrize("shape", [(5, 200, 64, 16, "4"), (5, 200, 64, 16, "8"),
+                                   (7, 100, 16, 12, "")])
+def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, monkeypatch):
+    """All X-steps of a code update in one launch (state on chip) against one launch
+    per X-step (state through HBM): the same operations in the same order, so every
+    field the X-step writes agrees bit for bit (Lg = 928 = 32 * 29 and 496 = 16 * 31)."""
+    N, L, M, fs, cs = shape
+    if cs:
+        monkeypatch.setenv("CDLGB_CLUSTER", cs)
+    synth = pkg.synth
+    bases, _, _ = synth.plant_dataset(11, N, L, [8, 12], [0.4, 0.4])
+    S = synth.onehot(bases)
+    Lg = 4 * L + 8 * fs
+    X0 = synth.init_X0(3, N, M, Lg)
+    D0 = synth.init_D0_unit_norm(3, M, Lg, 4 * fs)
+    out = {}
+    for multi in ("1", "0"):
+        monkeypatch.setenv("CDLGB_XITER", multi)
+        with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+            objs = []
+            for _ in range(2):
+                pkg.code_update(c, 15)
+                objs.append(pkg.update_best(c)[0])
+                pkg.dict_update(c, 1)
+            pkg.code_update(c, 4)
+            out[multi] = {f: c.get(f) for f in ("X", "X_best", "y2", "y3", "DX", "Y1", "y1")}
+            out[multi]["objs"] = np.array(objs)
+    for f in ("X", "X_best", "y2", "y3", "DX", "Y1", "y1"):
+        np.testing.assert_array_equal(out["1"][f], out["0"][f], err_msg=f)
+    # the objective's sum of |X| is associated differently (FP32 partial sums per lane)
+    np.testing.assert_allclose(out["1"]["objs"], out["0"]["objs"], rtol=1e-6)
 
 
 @pytest.mark.parametrize("mode", MODES)

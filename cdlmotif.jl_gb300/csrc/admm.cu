@@ -171,7 +171,8 @@ __global__ void k_mask_update(float* __restrict__ out, const float* __restrict__
         bool in = l >= gamma && l < gamma + L4;
         float wts = in ? S[nn * L4 + (l - gamma)] : 0.f;
         float dg = in ? 1.f : 0.f;
-        out[i] = (wts + pen * (a[i] + b[i])) / (dg + pen);
+        // separately rounded product and sum (no contraction), as the reference's broadcast
+        out[i] = __fadd_rn(wts, __fmul_rn(pen, a[i] + b[i])) / (dg + pen);
     }
 }
 

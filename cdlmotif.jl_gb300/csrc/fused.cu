@@ -423,8 +423,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_xstep_fused(XArgs A) {
                 }
                 float2 xa = cjfma(ga, W, va);
                 float2 xb = hasb ? cjfma(gb, W, vb) : f2(0.f, 0.f);
-                xa = f2(xa.x * sc, xa.y * sc);
-                xb = f2(xb.x * sc, xb.y * sc);
+                xa = f2(__fmul_rn(xa.x, sc), __fmul_rn(xa.y, sc));
+                xb = f2(__fmul_rn(xb.x, sc), __fmul_rn(xb.y, sc));
                 if (edge) {
                     Z[f] = f2(xa.x, xb.x);
                 } else {
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_xstep_fused(XArgs A) {
                     bool in = l >= A.gamma && l < A.gamma + A.L4;
                     float wts = in ? A.S[(size_t)n * A.L4 + (l - A.gamma)] : 0.f;
                     float dg = in ? 1.f : 0.f;
-                    Yo[e] = (wts + A.rho * (dx[e] + yn[e])) / (dg + A.rho);
+                    Yo[e] = __fadd_rn(wts, __fmul_rn(A.rho, dx[e] + yn[e])) / (dg + A.rho);
                 }
                 size_t o = (size_t)n * Lg + 4 * (size_t)l4;
                 reinterpret_cast<float4*>(A.DX + o)[0] = make_float4(dx[0], dx[1], dx[2], dx[3]);

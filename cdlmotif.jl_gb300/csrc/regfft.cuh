@@ -256,7 +256,9 @@ __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, boo
 // (stride BUF) holds the packed spectrum Z = Vh[2 sl] + i Vh[2 sl + 1] of this CTA's
 // filters 2 sl, 2 sl + 1 (the second absent when 2 sl + 1 == Mc); g1 is this CTA's
 // [Mc][F] slice of G1h.  The loads of CH slots are issued together before their
-// arithmetic, which stays in slot order (the same sums, the same bits).
+// arithmetic, which stays in slot order (the same sums, the same bits).  Products that
+// the compiler could fuse into a following add are written as separately rounded
+// intrinsics, so that every kernel using these phases rounds identically.
 constexpr int kSlotChunk = 4;
 
 // this CTA's part of P = sum_m G1h[m] Vh[m] at bin f (train.jl:18-25, the RHS dot)
@@ -339,8 +341,8 @@ __device__ __forceinline__ void repack_X(float2* __restrict__ bufs, int BUF, int
                 const float2 vb = f2(0.5f * (z1[u].y + z2[u].y), 0.5f * (z2[u].x - z1[u].x));
                 float2 xa = cjfma(ga[u], W, va);
                 float2 xb = hb ? cjfma(gb[u], W, vb) : f2(0.f, 0.f);
-                xa = f2(xa.x * sc, xa.y * sc);
-                xb = f2(xb.x * sc, xb.y * sc);
+                xa = f2(__fmul_rn(xa.x, sc), __fmul_rn(xa.y, sc));
+                xb = f2(__fmul_rn(xb.x, sc), __fmul_rn(xb.y, sc));
                 if (edge) {
                     Z[f] = f2(xa.x, xb.x);
                 } else {

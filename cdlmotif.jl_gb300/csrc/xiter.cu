@@ -44,10 +44,69 @@ struct IArgs {
     double* absx_part;
     int N, M, L4, gamma, iters;
     float lam, rho, kc;
-    int Mc, B, ld, ld3;     // row strides (floats) of the y2 and compacted y3 rows in shared memory
+    int ld, ld3;            // row strides (floats) of the y2 and compacted y3 rows in shared memory
 };
 
-template <int N1, int P, int NT, int MINB>
+// this CTA's part of P = sum_m G1h[m] Vh[m] at bin f, G1h from registers (the sum in
+// slot order, as partial_P)
+template <int Lg, int MC>
+__device__ __forceinline__ float2 partial_P_r(const float2* __restrict__ bufs, int BUF, int f,
+                                             const float2 (&g)[MC]) {
+    constexpr int B = (MC + 1) / 2;
+    const bool edge = (f == 0) || (f == Lg / 2);
+    const int fr = edge ? f : Lg - f;
+    float2 z1[B], z2[B];
+#pragma unroll
+    for (int sl = 0; sl < B; ++sl) {
+        z1[sl] = bufs[sl * BUF + f];
+        z2[sl] = bufs[sl * BUF + fr];
+    }
+    float2 P_ = f2(0.f, 0.f);
+#pragma unroll
+    for (int sl = 0; sl < B; ++sl) {
+        const float2 va = f2(0.5f * (z1[sl].x + z2[sl].x), 0.5f * (z1[sl].y - z2[sl].y));
+        const float2 vb = f2(0.5f * (z1[sl].y + z2[sl].y), 0.5f * (z2[sl].x - z1[sl].x));
+        P_ = cfma(g[2 * sl], va, P_);
+        if (2 * sl + 1 < MC) P_ = cfma(g[2 * sl + 1], vb, P_);
+    }
+    return P_;
+}
+
+// Xh = (Vh + conj(G1h) W) * sc at bins f and Lg - f, packed back into the slots, G1h
+// from registers (as repack_X)
+template <int Lg, int MC>
+__device__ __forceinline__ void repack_X_r(float2* __restrict__ bufs, int BUF, int f,
+                                           const float2 (&g)[MC], float2 W, float sc) {
+    constexpr int B = (MC + 1) / 2;
+    const bool edge = (f == 0) || (f == Lg / 2);
+    const int fr = edge ? f : Lg - f;
+    float2 z1[B], z2[B];
+#pragma unroll
+    for (int sl = 0; sl < B; ++sl) {
+        z1[sl] = bufs[sl * BUF + f];
+        z2[sl] = bufs[sl * BUF + fr];
+    }
+#pragma unroll
+    for (int sl = 0; sl < B; ++sl) {
+        const float2 va = f2(0.5f * (z1[sl].x + z2[sl].x), 0.5f * (z1[sl].y - z2[sl].y));
+        const float2 vb = f2(0.5f * (z1[sl].y + z2[sl].y), 0.5f * (z2[sl].x - z1[sl].x));
+        float2 xa = cjfma(g[2 * sl], W, va);
+        float2 xb = 2 * sl + 1 < MC ? cjfma(g[2 * sl + 1], W, vb) : f2(0.f, 0.f);
+        xa = f2(__fmul_rn(xa.x, sc), __fmul_rn(xa.y, sc));
+        xb = f2(__fmul_rn(xb.x, sc), __fmul_rn(xb.y, sc));
+        if (edge) {
+            bufs[sl * BUF + f] = f2(xa.x, xb.x);
+        } else {
+            bufs[sl * BUF + f] = f2(xa.x - xb.y, xa.y + xb.x);
+            bufs[sl * BUF + Lg - f] = f2(xa.x + xb.y, xb.x - xa.y);
+        }
+    }
+}
+
+// MC filters per CTA (compile time), NT threads: every slot's lane group and every
+// thread's bins of the cross-filter phases are fixed, and each thread keeps the G1h
+// values of its bins in registers for the whole launch (G1 is fixed during a code update).
+template <int N1, int P, int NT, int MINB, int MC>
 __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     constexpr int Lg = N1 * P;
     constexpr int G = 32 / N1;                  // lane groups per warp
@@ -63,7 +122,10 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     const int cid = blockIdx.x / CS;
     const int nclusters = gridDim.x / CS;
     constexpr int W3 = 3 * N1 / 4;              // y3 entries per n2 row (l % 4 != 0 only)
-    const int B = A.B, Mc = A.Mc, M = A.M, ld = A.ld, ld3 = A.ld3;
+    constexpr int B = (MC + 1) / 2;             // packed pairs
+    constexpr int Mc = MC;
+    constexpr int NFR = (F + NT - 1) / NT;      // bins per thread in the cross-filter phases
+    const int M = A.M, ld = A.ld, ld3 = A.ld3;
 
     float2* bufs = reinterpret_cast<float2*>(smem4);       // [B + 1][BUF] slot buffers
     float2* Ppart = bufs + (size_t)(B + 1) * BUF;          // [2][Fp] this CTA's part of P
@@ -83,7 +145,13 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     __syncthreads();
 
     const int m0 = rank * Mc;
-    const float2* __restrict__ g1 = A.G1h + (size_t)m0 * F;
+    float2 g1r[NFR][MC];
+#pragma unroll
+    for (int r = 0; r < NFR; ++r) {
+        const int f = threadIdx.x + r * NT;
+#pragma unroll
+        for (int m = 0; m < MC; ++m) g1r[r][m] = f < F ? A.G1h[(size_t)(m0 + m) * F + f] : f2(0.f, 0.f);
+    }
     const int lane = threadIdx.x & 31;
     const int grp = (threadIdx.x >> 5) * G + lane / N1;   // this lane group's slot
     const int gl = lane % N1;                             // lane within the group
@@ -146,15 +214,21 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
 
             // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
             float2* Pp = Ppart + (it & 1) * Fp;
-            for (int f = threadIdx.x; f < F; f += blockDim.x)
-                Pp[f] = partial_P<Lg>(bufs, BUF, B, Mc, F, f, g1);
+#pragma unroll
+            for (int r = 0; r < NFR; ++r) {
+                const int f = threadIdx.x + r * NT;
+                if (f < F) Pp[f] = partial_P_r<Lg, MC>(bufs, BUF, f, g1r[r]);
+            }
             cluster.sync();
 
             // ---------------- P over the cluster (fixed rank order), alpha, W; every CTA
             // packs DXh = (P + A W)/(k Lg) and repacks Xh = (Vh + conj(G1h) W)/(k Lg)
             {
                 float2* ZU = bufs + (size_t)B * BUF;
-                for (int f = threadIdx.x; f < F; f += blockDim.x) {
+#pragma unroll
+                for (int r = 0; r < NFR; ++r) {
+                    const int f = threadIdx.x + r * NT;
+                    if (f >= F) break;
                     const float2 P_ = cluster_sum<8>(cluster, Pp, CS, f);
                     const float Av = Ahs[f];
                     const float2 U = ZU[f];
@@ -169,7 +243,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                         ZU[f] = D;
                         ZU[Lg - f] = f2(D.x, -D.y);
                     }
-                    repack_X<Lg>(bufs, BUF, B, Mc, F, f, g1, W, sc);
+                    repack_X_r<Lg, MC>(bufs, BUF, f, g1r[r], W, sc);
                 }
             }
             __syncthreads();
@@ -231,7 +305,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                     const float wts = in ? Ss[l - A.gamma] : 0.f;
                     const float dg = in ? 1.f : 0.f;
                     const float dx = sb[n2 * RS + gl].x, yp = y1s[l];
-                    const float Y1n = (wts + rho * (dx + yp)) / (dg + rho);
+                    const float Y1n = __fadd_rn(wts, __fmul_rn(rho, dx + yp)) / (dg + rho);
                     if (!last) {
                         const float yn = (yp + dx) - Y1n;
                         y1s[l] = yn;
@@ -262,18 +336,15 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
 typedef void (*kern_t)(IArgs);
 constexpr size_t kCap2 = 115200;       // two CTAs per SM (2 x (this + 1 KB reserved) <= 228 KB)
 constexpr size_t kCap1 = 220 * 1024;   // one CTA per SM
-// k2: up to 5 warps, two CTAs per SM; k1: up to 9 warps, one CTA per SM
-struct Variant { int N1, P; kern_t k2, k1; };
+// (N1, P, filters per CTA): threads = 32 ceil((MC/2 + 1) / (32 / N1)) rounded to a warp
+struct Variant { int N1, P, MC, threads, minb; kern_t k; };
+// in order of preference (measured at L=200, K=64: 16 filters per CTA, one CTA per SM,
+// 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms)
 const Variant kVariants[] = {
-    {32, 29, k_xiter<32, 29, 160, 2>, k_xiter<32, 29, 288, 1>},
-    {16, 31, k_xiter<16, 31, 160, 2>, k_xiter<16, 31, 288, 1>},
+    {32, 29, 16, 288, 1, k_xiter<32, 29, 288, 1, 16>},
+    {32, 29, 8, 160, 2, k_xiter<32, 29, 160, 2, 8>},
+    {16, 31, 16, 160, 2, k_xiter<16, 31, 160, 2, 16>},
 };
-
-const Variant* find_variant(int Lg) {
-    for (const Variant& v : kVariants)
-        if (v.N1 * v.P == Lg) return &v;
-    return nullptr;
-}
 
 // row stride of the y2 / y3 rows: with two lane groups per warp (N1 = 16) the groups
 // touch rows 2 apart, which land on opposite bank halves when ld = 8 (mod 16)
@@ -291,7 +362,7 @@ size_t iter_smem(int N1, int P, int slots, int Mc, int ld, int ld3, int L4) {
 
 struct IterPlan {
     kern_t k;
-    int CS, Mc, B, ld, ld3, threads, grid;
+    int CS, Mc, ld, ld3, threads, grid;
     size_t smem;
     float2* tw2;
     double* absx_part;
@@ -299,38 +370,32 @@ struct IterPlan {
 
 }  // namespace
 
-// Smallest cluster whose CTA fits two per SM (at most 5 warps), else the smallest
-// that fits one per SM (at most 9 warps); CDLGB_CLUSTER forces a cluster size and
+// The first variant of kVariants whose transform length is Lg and whose filters per
+// CTA divide M into 1, 2, 4 or 8 CTAs; CDLGB_CLUSTER forces a cluster size and
 // CDLGB_XITER=0 turns the multi-iteration kernel off.  Returns nullptr when the size
 // has no variant.
 void* iter_plan_create(cdlgb_ctx* c, int* status) {
     *status = CDLGB_OK;
     if (const char* e = getenv("CDLGB_XITER"))
         if (atoi(e) == 0) return nullptr;
-    const Variant* v = find_variant(c->Lg);
-    if (!v) return nullptr;
     int want_cs = 0;
     if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
-    const int G = 32 / v->N1;
-    const int ld = pad_ld(v->N1, c->Lg);
-    const int ld3 = pad_ld(v->N1, 3 * v->N1 / 4 * v->P);
     IterPlan* P = nullptr;
-    for (int pass = 0; pass < 2 && !P; ++pass) {
-        for (int cs : {1, 2, 4, 8}) {
-            if (c->M % cs) continue;
-            if (want_cs && cs != want_cs) continue;
-            const int mc = c->M / cs, B = (mc + 1) / 2, slots = B + 1;
-            const int warps = (slots + G - 1) / G;
-            const size_t sm = iter_smem(v->N1, v->P, slots, mc, ld, ld3, c->L4);
-            kern_t k = nullptr;
-            if (pass == 0 && warps <= 5 && sm <= kCap2) k = v->k2;
-            if (pass == 1 && warps <= 9 && sm <= kCap1) k = v->k1;
-            if (!k) continue;
-            P = new IterPlan();
-            P->k = k; P->CS = cs; P->Mc = mc; P->B = B; P->ld = ld; P->ld3 = ld3;
-            P->threads = warps * 32; P->smem = sm;
-            break;
-        }
+    const Variant* v = nullptr;
+    for (const Variant& cand : kVariants) {
+        if (cand.N1 * cand.P != c->Lg || c->M % cand.MC) continue;
+        const int cs = c->M / cand.MC;
+        if (cs != 1 && cs != 2 && cs != 4 && cs != 8) continue;
+        if (want_cs && cs != want_cs) continue;
+        const int ld = pad_ld(cand.N1, c->Lg);
+        const int ld3 = pad_ld(cand.N1, 3 * cand.N1 / 4 * cand.P);
+        const size_t sm = iter_smem(cand.N1, cand.P, (cand.MC + 1) / 2 + 1, cand.MC, ld, ld3, c->L4);
+        if (sm > (cand.minb == 2 ? kCap2 : kCap1)) continue;
+        v = &cand;
+        P = new IterPlan();
+        P->k = cand.k; P->CS = cs; P->Mc = cand.MC; P->ld = ld; P->ld3 = ld3;
+        P->threads = cand.threads; P->smem = sm;
+        break;
     }
     if (!P) return nullptr;
     std::vector<float2> tw2 = regfft_twiddles(v->N1, v->P);
@@ -340,7 +405,7 @@ void* iter_plan_create(cdlgb_ctx* c, int* status) {
     // process-wide per kernel: the same cap for every context
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(P->k == v->k2 ? kCap2 : kCap1));
+                                 (int)(v->minb == 2 ? kCap2 : kCap1));
     int nclusters = 0;
     if (e == cudaSuccess) {
         cudaLaunchConfig_t cfg = {};
@@ -389,7 +454,7 @@ int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters)
     a.G1h = c->G1h; a.Ah = c->Ah; a.tw2 = P->tw2; a.absx_part = P->absx_part;
     a.N = c->N; a.M = c->M; a.L4 = c->L4; a.gamma = c->gamma; a.iters = iters;
     a.lam = c->p.lambda; a.rho = c->p.rho; a.kc = c->p.sherman_const_csc;
-    a.Mc = P->Mc; a.B = P->B; a.ld = P->ld; a.ld3 = P->ld3;
+    a.ld = P->ld; a.ld3 = P->ld3;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
                             const bool in = le >= A.gamma && le < A.gamma + A.L4;
                             const float wts = in ? A.S[(size_t)ns * A.L4 + (le - A.gamma)] : 0.f;
                             const float dg = in ? 1.f : 0.f;
-                            Yo[e] = (wts + A.rho * (dx[e] + yn[e])) / (dg + A.rho);
+                            Yo[e] = __fadd_rn(wts, __fmul_rn(A.rho, dx[e] + yn[e])) / (dg + A.rho);
                         }
                         const size_t bs = (size_t)ns * Lg + l;
                         *reinterpret_cast<float4*>(A.DX + bs) = make_float4(dx[0], dx[1], dx[2], dx[3]);

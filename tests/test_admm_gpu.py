@@ -151,9 +151,9 @@ def test_fp32_error_envelope(pkg, built_lib, mode):
 def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
     """The N=20000/L=200/K=64/W=16 workload's shapes (Lg = 928 = 2^5 * 29) on 6
     sequences, 2 outer iterations, through the fused X-step: all iterations of a code
-    update in one launch (default clusters, and 8-CTA clusters), the one-X-step
-    register-FFT kernel (default 4-CTA clusters with two slots per lane group, and
-    8-CTA clusters), and the generic in-kernel FFT."""
+    update in one launch (default 4-CTA clusters of 16 filters each, and 8-CTA
+    clusters), the one-X-step register-FFT kernel (default 4-CTA clusters with two
+    slots per lane group, and 8-CTA clusters), and the generic in-kernel FFT."""
     if variant == "generic":
         monkeypatch.setenv("CDLGB_GENERIC_FFT", "1")
     if variant.startswith("register_fft"):

@@ -241,14 +241,35 @@ __device__ __forceinline__ void inv_step2(float2* __restrict__ buf, int j, bool 
     __syncwarp();
 }
 
+// shrink!, projectionX! and the dual updates of one entry (train.jl:12-14,
+// csc_kernels.jl:53-82), returning V = (Y2 - y2') + (Y3 - y3') in na, nb, v:
+//   Y2 = t - clamp(t, -lam, lam), t = X + y2 (= sign(t) max(|t| - lam, 0), the soft
+//        threshold at lam, up to the sign of a zero result);  y2' = (y2 + X) - Y2;
+//   on the rows projectionX! keeps (keep): Y3 = X + y3 and y3' = (y3 + X) - Y3 = +0;
+//   elsewhere Y3 = 0 and y3' = y3 + X.
 __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
                                        float& na, float& nb, float& v) {
-    float t = x + a;                                        // X + y2
-    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);    // shrink!  (csc_kernels.jl:53-64)
-    float Y3 = keep ? x + b : 0.f;                          // projectionX! (:68-82)
-    na = (a + x) - Y2;                                      // train.jl:13
-    nb = (b + x) - Y3;                                      // train.jl:14
-    v = (Y2 - na) + (Y3 - nb);
+    const float t = x + a;
+    const float Y2 = t - fminf(fmaxf(t, -lam), lam);
+    na = t - Y2;
+    const float u = x + b;
+    nb = keep ? 0.f : u;
+    const float w = Y2 - na;
+    v = keep ? w + u : w - u;
+}
+
+// xprep1 for the two filters of a slot at once (packed FP32x2: the same operations
+// on both halves, so the same bits); y2 and y3 are updated in place, V returned
+__device__ __forceinline__ float2 xprep2(float2 x, float2& y2, float2& y3, float lam, bool keep) {
+    const float2 t = cadd(x, y2);
+    const float2 c = f2(fminf(fmaxf(t.x, -lam), lam), fminf(fmaxf(t.y, -lam), lam));
+    const float2 Y2 = csub(t, c);
+    const float2 na = csub(t, Y2);
+    const float2 u = cadd(x, y3);
+    const float2 w = csub(Y2, na);
+    y2 = na;
+    y3 = keep ? f2(0.f, 0.f) : u;
+    return keep ? cadd(w, u) : csub(w, u);
 }
 
 
@@ -286,14 +307,14 @@ __device__ __forceinline__ float2 partial_P(const float2* __restrict__ bufs, int
         for (int u = 0; u < kSlotChunk; ++u) {
             const int sl = s0 + u;
             if (sl < B) {
-                const float2 va = f2(0.5f * (z1[u].x + z2[u].x), 0.5f * (z1[u].y - z2[u].y));
-                const float2 vb = f2(0.5f * (z1[u].y + z2[u].y), 0.5f * (z2[u].x - z1[u].x));
+                const float2 va = f2(z1[u].x + z2[u].x, z1[u].y - z2[u].y);     // 2 Vh[2 sl]
+                const float2 vb = f2(z1[u].y + z2[u].y, z2[u].x - z1[u].x);     // 2 Vh[2 sl + 1]
                 P_ = cfma(ga[u], va, P_);
                 if (2 * sl + 1 < Mc) P_ = cfma(gb[u], vb, P_);
             }
         }
     }
-    return P_;
+    return f2(0.5f * P_.x, 0.5f * P_.y);      // every partial sum was exactly doubled
 }
 
 // P = sum over the cluster's CTAs of their parts at bin f, in rank order; the CS
@@ -316,6 +337,9 @@ template <int Lg>
 __device__ __forceinline__ void repack_X(float2* __restrict__ bufs, int BUF, int B, int Mc,
                                          int F, int f, const float2* g1, float2 W, float sc) {
     constexpr int half = Lg / 2;
+    // with 2 Vh and 2 W every term is exactly doubled; the scale sc / 2 undoes it
+    const float2 W2 = f2(W.x + W.x, W.y + W.y);
+    const float sch = 0.5f * sc;
     const bool edge = (f == 0) || (f == half);
     const int fr = edge ? f : Lg - f;
     for (int s0 = 0; s0 < B; s0 += kSlotChunk) {
@@ -337,12 +361,12 @@ __device__ __forceinline__ void repack_X(float2* __restrict__ bufs, int BUF, int
             if (sl < B) {
                 float2* Z = bufs + (size_t)sl * BUF;
                 const bool hb = 2 * sl + 1 < Mc;
-                const float2 va = f2(0.5f * (z1[u].x + z2[u].x), 0.5f * (z1[u].y - z2[u].y));
-                const float2 vb = f2(0.5f * (z1[u].y + z2[u].y), 0.5f * (z2[u].x - z1[u].x));
-                float2 xa = cjfma(ga[u], W, va);
-                float2 xb = hb ? cjfma(gb[u], W, vb) : f2(0.f, 0.f);
-                xa = f2(__fmul_rn(xa.x, sc), __fmul_rn(xa.y, sc));
-                xb = f2(__fmul_rn(xb.x, sc), __fmul_rn(xb.y, sc));
+                const float2 va = f2(z1[u].x + z2[u].x, z1[u].y - z2[u].y);
+                const float2 vb = f2(z1[u].y + z2[u].y, z2[u].x - z1[u].x);
+                float2 xa = cjfma(ga[u], W2, va);
+                float2 xb = hb ? cjfma(gb[u], W2, vb) : f2(0.f, 0.f);
+                xa = f2(__fmul_rn(xa.x, sch), __fmul_rn(xa.y, sch));
+                xb = f2(__fmul_rn(xb.x, sch), __fmul_rn(xb.y, sch));
                 if (edge) {
                     Z[f] = f2(xa.x, xb.x);
                 } else {

@@ -44,7 +44,7 @@ struct IArgs {
     double* absx_part;
     int N, M, L4, gamma, iters;
     float lam, rho, kc;
-    int ld, ld3;            // row strides (floats) of the y2 and compacted y3 rows in shared memory
+    int ld, ld3;            // row strides (pairs) of the y2 and compacted y3 rows in shared memory
 };
 
 // this CTA's part of P = sum_m G1h[m] Vh[m] at bin f, G1h from registers (the sum in
@@ -64,12 +64,12 @@ __device__ __forceinline__ float2 partial_P_r(const float2* __restrict__ bufs, i
     float2 P_ = f2(0.f, 0.f);
 #pragma unroll
     for (int sl = 0; sl < B; ++sl) {
-        const float2 va = f2(0.5f * (z1[sl].x + z2[sl].x), 0.5f * (z1[sl].y - z2[sl].y));
-        const float2 vb = f2(0.5f * (z1[sl].y + z2[sl].y), 0.5f * (z2[sl].x - z1[sl].x));
+        const float2 va = f2(z1[sl].x + z2[sl].x, z1[sl].y - z2[sl].y);      // 2 Vh[2 sl]
+        const float2 vb = f2(z1[sl].y + z2[sl].y, z2[sl].x - z1[sl].x);      // 2 Vh[2 sl + 1]
         P_ = cfma(g[2 * sl], va, P_);
         if (2 * sl + 1 < MC) P_ = cfma(g[2 * sl + 1], vb, P_);
     }
-    return P_;
+    return f2(0.5f * P_.x, 0.5f * P_.y);      // every partial sum was exactly doubled
 }
 
 // Xh = (Vh + conj(G1h) W) * sc at bins f and Lg - f, packed back into the slots, G1h
@@ -80,6 +80,9 @@ __device__ __forceinline__ void repack_X_r(float2* __restrict__ bufs, int BUF, i
     constexpr int B = (MC + 1) / 2;
     const bool edge = (f == 0) || (f == Lg / 2);
     const int fr = edge ? f : Lg - f;
+    // with 2 Vh and 2 W every term is exactly doubled; the scale sc / 2 undoes it
+    const float2 W2 = f2(W.x + W.x, W.y + W.y);
+    const float sch = 0.5f * sc;
     float2 z1[B], z2[B];
 #pragma unroll
     for (int sl = 0; sl < B; ++sl) {
@@ -88,12 +91,12 @@ __device__ __forceinline__ void repack_X_r(float2* __restrict__ bufs, int BUF, i
     }
 #pragma unroll
     for (int sl = 0; sl < B; ++sl) {
-        const float2 va = f2(0.5f * (z1[sl].x + z2[sl].x), 0.5f * (z1[sl].y - z2[sl].y));
-        const float2 vb = f2(0.5f * (z1[sl].y + z2[sl].y), 0.5f * (z2[sl].x - z1[sl].x));
-        float2 xa = cjfma(g[2 * sl], W, va);
-        float2 xb = 2 * sl + 1 < MC ? cjfma(g[2 * sl + 1], W, vb) : f2(0.f, 0.f);
-        xa = f2(__fmul_rn(xa.x, sc), __fmul_rn(xa.y, sc));
-        xb = f2(__fmul_rn(xb.x, sc), __fmul_rn(xb.y, sc));
+        const float2 va = f2(z1[sl].x + z2[sl].x, z1[sl].y - z2[sl].y);
+        const float2 vb = f2(z1[sl].y + z2[sl].y, z2[sl].x - z1[sl].x);
+        float2 xa = cjfma(g[2 * sl], W2, va);
+        float2 xb = 2 * sl + 1 < MC ? cjfma(g[2 * sl + 1], W2, vb) : f2(0.f, 0.f);
+        xa = f2(__fmul_rn(xa.x, sch), __fmul_rn(xa.y, sch));
+        xb = f2(__fmul_rn(xb.x, sch), __fmul_rn(xb.y, sch));
         if (edge) {
             bufs[sl * BUF + f] = f2(xa.x, xb.x);
         } else {
@@ -130,12 +133,13 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     float2* bufs = reinterpret_cast<float2*>(smem4);       // [B + 1][BUF] slot buffers
     float2* Ppart = bufs + (size_t)(B + 1) * BUF;          // [2][Fp] this CTA's part of P
     float2* tw2 = Ppart + 2 * Fp;                          // [P][N1] twiddles
-    float* y2s = reinterpret_cast<float*>(tw2 + P * N1);   // [Mc][ld]
+    // the duals of the two filters of pair s, interleaved: [B][ld] (y2 of filters 2s, 2s+1)
+    float2* y2s = tw2 + P * N1;
     // y3 is identically zero on the rows l % 4 == 0: there projectionX! keeps X + y3,
     // so the update y3 + X - Y3 is (y3 + X) - (X + y3) = +0 exactly.  Only the other
-    // rows are kept, [Mc][ld3], row n2 of lane n1 at n2 W3 + n1 - n1/4 - 1.
-    float* y3s = y2s + (size_t)Mc * ld;
-    float* y1s = y3s + (size_t)Mc * ld3;                   // [Lg]
+    // rows are kept, [B][ld3], row n2 of lane n1 at n2 W3 + n1 - n1/4 - 1.
+    float2* y3s = y2s + (size_t)B * ld;
+    float* y1s = reinterpret_cast<float*>(y3s + (size_t)B * ld3);   // [Lg]
     float* Ahs = y1s + Lg;                                 // [Fp] sum_m |G1h|^2
     float* Ss = Ahs + Fp;                                  // [L4] this sequence's W'S window
     __shared__ double red[NT / 32];
@@ -157,11 +161,11 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     const int gl = lane % N1;                             // lane within the group
     const bool act = grp <= B;
     const bool pair = grp < B;
-    const bool hasb = pair && 2 * grp + 1 < Mc;
+    static_assert(MC % 2 == 0, "filters per CTA must pair up");
     float2* sb = bufs + (size_t)(act ? grp : 0) * BUF;
-    float* y2a = y2s + (size_t)(pair ? 2 * grp : 0) * ld + gl;
+    float2* y2p = y2s + (size_t)(pair ? grp : 0) * ld + gl;
     const bool keep = (gl & 3) == 0;                      // l = gl + N1 n2, N1 % 4 == 0
-    float* y3a = y3s + (size_t)(pair ? 2 * grp : 0) * ld3 + (keep ? 0 : gl - (gl >> 2) - 1);
+    float2* y3p = y3s + (size_t)(pair ? grp : 0) * ld3 + (keep ? 0 : gl - (gl >> 2) - 1);
     const float sc = 1.f / (A.kc * (float)Lg);
     const float lam = A.lam, rho = A.rho;
     const unsigned gmask = N1 == 32 ? 0xffffffffu : (0xffffu << (lane & 16));   // this lane group
@@ -177,17 +181,12 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
 #pragma unroll 4
             for (int n2 = 0; n2 < P; ++n2) {
                 const int o = N1 * n2;
-                float na, nb, va, vb = 0.f;
-                const int o3 = W3 * n2;
-                xprep1(A.Xin[ra + o], A.y2[ra + o], A.y3[ra + o], lam, keep, na, nb, va);
-                y2a[o] = na;
-                if (!keep) y3a[o3] = nb;
-                if (hasb) {
-                    xprep1(A.Xin[ra + Lg + o], A.y2[ra + Lg + o], A.y3[ra + Lg + o], lam, keep, na, nb, vb);
-                    y2a[ld + o] = na;
-                    if (!keep) y3a[ld3 + o3] = nb;
-                }
-                sb[n2 * RS + gl] = f2(va, vb);
+                float2 a2 = f2(A.y2[ra + o], A.y2[ra + Lg + o]);
+                float2 a3 = f2(A.y3[ra + o], A.y3[ra + Lg + o]);
+                const float2 V = xprep2(f2(A.Xin[ra + o], A.Xin[ra + Lg + o]), a2, a3, lam, keep);
+                y2p[o] = a2;
+                if (!keep) y3p[W3 * n2] = a3;
+                sb[n2 * RS + gl] = V;
             }
             fwd_step1<N1, P>(sb, gl, tw2);
         } else if (act) {
@@ -259,17 +258,12 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                     for (int n2 = 0; n2 < P; ++n2) {
                         const int o = N1 * n2;
                         const int o3 = W3 * n2;
-                        const float2 xv = sb[n2 * RS + gl];
-                        float na, nb, va, vb = 0.f;
-                        xprep1(xv.x, y2a[o], keep ? 0.f : y3a[o3], lam, keep, na, nb, va);
-                        y2a[o] = na;
-                        if (!keep) y3a[o3] = nb;
-                        if (hasb) {
-                            xprep1(xv.y, y2a[ld + o], keep ? 0.f : y3a[ld3 + o3], lam, keep, na, nb, vb);
-                            y2a[ld + o] = na;
-                            if (!keep) y3a[ld3 + o3] = nb;
-                        }
-                        sb[n2 * RS + gl] = f2(va, vb);
+                        float2 a2 = y2p[o];
+                        float2 a3 = keep ? f2(0.f, 0.f) : y3p[o3];
+                        const float2 V = xprep2(sb[n2 * RS + gl], a2, a3, lam, keep);
+                        y2p[o] = a2;
+                        if (!keep) y3p[o3] = a3;
+                        sb[n2 * RS + gl] = V;
                     }
                     fwd_step1<N1, P>(sb, gl, tw2);
                 } else {
@@ -279,17 +273,16 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                     for (int n2 = 0; n2 < P; ++n2) {
                         const int o = N1 * n2;
                         const float2 xv = sb[n2 * RS + gl];
-                        const int o3 = W3 * n2;
+                        const float2 a2 = y2p[o];
+                        const float2 a3 = keep ? f2(0.f, 0.f) : y3p[W3 * n2];
                         A.Xout[ra + o] = xv.x;
-                        A.y2[ra + o] = y2a[o];
-                        A.y3[ra + o] = keep ? 0.f : y3a[o3];
+                        A.Xout[ra + Lg + o] = xv.y;
+                        A.y2[ra + o] = a2.x;
+                        A.y2[ra + Lg + o] = a2.y;
+                        A.y3[ra + o] = a3.x;
+                        A.y3[ra + Lg + o] = a3.y;
                         s += fabsf(xv.x);
-                        if (hasb) {
-                            A.Xout[ra + Lg + o] = xv.y;
-                            A.y2[ra + Lg + o] = y2a[ld + o];
-                            A.y3[ra + Lg + o] = keep ? 0.f : y3a[ld3 + o3];
-                            s += fabsf(xv.y);
-                        }
+                        s += fabsf(xv.y);
                     }
                     absacc += (double)s;
                 }
@@ -346,18 +339,14 @@ const Variant kVariants[] = {
     {16, 31, 16, 160, 2, k_xiter<16, 31, 160, 2, 16>},
 };
 
-// row stride of the y2 / y3 rows: with two lane groups per warp (N1 = 16) the groups
-// touch rows 2 apart, which land on opposite bank halves when ld = 8 (mod 16)
-int pad_ld(int N1, int n) {
-    if (N1 == 32) return n;
-    return n + ((8 - n % 16) + 16) % 16;
-}
-
+// bytes of shared memory: slot buffers, P parts, twiddles, the interleaved y2 / y3
+// pair rows (ld, ld3 pairs each), y1, A, the W'S window
 size_t iter_smem(int N1, int P, int slots, int Mc, int ld, int ld3, int L4) {
     const int Lg = N1 * P, F = Lg / 2 + 1, Fp = (F + 1) & ~1;
     const size_t buf = ((size_t)P * (N1 + 1) + 1) & ~(size_t)1;
-    return ((size_t)slots * buf + 2 * (size_t)Fp + (size_t)P * N1) * sizeof(float2) +
-           ((size_t)Mc * ld + (size_t)Mc * ld3 + Lg + Fp + L4) * sizeof(float);
+    return ((size_t)slots * buf + 2 * (size_t)Fp + (size_t)P * N1 +
+            (size_t)(Mc / 2) * (ld + ld3)) * sizeof(float2) +
+           ((size_t)Lg + Fp + L4) * sizeof(float);
 }
 
 struct IterPlan {
@@ -387,8 +376,8 @@ void* iter_plan_create(cdlgb_ctx* c, int* status) {
         const int cs = c->M / cand.MC;
         if (cs != 1 && cs != 2 && cs != 4 && cs != 8) continue;
         if (want_cs && cs != want_cs) continue;
-        const int ld = pad_ld(cand.N1, c->Lg);
-        const int ld3 = pad_ld(cand.N1, 3 * cand.N1 / 4 * cand.P);
+        const int ld = c->Lg;
+        const int ld3 = 3 * cand.N1 / 4 * cand.P;
         const size_t sm = iter_smem(cand.N1, cand.P, (cand.MC + 1) / 2 + 1, cand.MC, ld, ld3, c->L4);
         if (sm > (cand.minb == 2 ? kCap2 : kCap1)) continue;
         v = &cand;

@@ -152,6 +152,11 @@ int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters)
 int iter_absx(void* p, const double** part, int* n);
 int iter_plan_cluster(void* p);
 int fused_has_multi(cdlgb_ctx* c);
+// fused D-step (dfused.cu)
+void* dfused_plan_create(cdlgb_ctx* c, int* status);
+void dfused_plan_free(void* p);
+int dfused_step(cdlgb_ctx* c, void* p, const float* X);
+int fused_has_dstep(cdlgb_ctx* c);
 int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 
 // ---- scan.cu ----

@@ -53,6 +53,7 @@ struct FusedPlan {
     double* absx_part;      // one partial sum of |X| per CTA
     void* warp;             // register-FFT variant (xwarp.cu) when Lg has one
     void* iter;             // multi-iteration register-FFT variant (xiter.cu)
+    void* dplan;            // fused D-step (dfused.cu)
 };
 
 struct XArgs {
@@ -554,6 +555,8 @@ int fused_setup(cdlgb_ctx* c) {
     P->F = c->F;
     if (!getenv("CDLGB_GENERIC_FFT")) {
         int st = CDLGB_OK;
+        P->dplan = dfused_plan_create(c, &st);
+        if (st != CDLGB_OK) return st;
         P->iter = iter_plan_create(c, &st);
         if (st != CDLGB_OK) return st;
         if (P->iter) return CDLGB_OK;
@@ -611,6 +614,7 @@ void fused_free(cdlgb_ctx* c) {
     if (P->absx_part) cudaFree(P->absx_part);
     warp_plan_free(P->warp);
     iter_plan_free(P->iter);
+    dfused_plan_free(P->dplan);
     delete P;
     c->fplan = nullptr;
 }
@@ -657,7 +661,16 @@ int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs) {
     return CDLGB_OK;
 }
 
-int fused_dstep(cdlgb_ctx* c) { return cdlgb_seterr(c, CDLGB_ENOTSUP, "fused D-step not built"); }
+int fused_has_dstep(cdlgb_ctx* c) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    return P && P->dplan;
+}
+
+int fused_dstep(cdlgb_ctx* c) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    if (!P || !P->dplan) return cdlgb_seterr(c, CDLGB_ENOTSUP, "no fused D-step for this size");
+    return dfused_step(c, P->dplan, c->Xb[c->xcur]);   // the current X
+}
 
 // partial sums of |X| written by the last fused X-step (one per CTA)
 int fused_absx(cdlgb_ctx* c, const double** part, int* n) {

@@ -213,6 +213,38 @@ def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, m
     np.testing.assert_allclose(out["1"]["objs"], out["0"]["objs"], rtol=1e-6)
 
 
+@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12)])
+def test_fused_dstep_against_oracle_and_cufft(pkg, built_lib, shape, monkeypatch):
+    """One D-step through the fused kernel (register FFTs, cluster sums) and through the
+    cuFFT D-step from the same state, both against the FP64 oracle: every field the
+    D-step writes is within the parity tolerance, and the fused kernel's error is within
+    twice the cuFFT path's (Lg = 928 and 496)."""
+    N, L, M, fs = shape
+    synth = pkg.synth
+    bases, _, _ = synth.plant_dataset(13, N, L, [8, 12], [0.4, 0.4])
+    S = synth.onehot(bases)
+    Lg = 4 * L + 8 * fs
+    X0 = synth.init_X0(4, N, M, Lg)
+    D0 = synth.init_D0_unit_norm(4, M, Lg, 4 * fs)
+    ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    O.code_update(ref, 15)
+    O.update_best(ref)
+    O.dict_update(ref, 1)
+    fields = ("d", "g1", "g3", "G1", "G3", "G2", "g2", "Td")
+    out = {}
+    for fusedd in ("1", "0"):
+        monkeypatch.setenv("CDLGB_DFUSED", fusedd)
+        with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+            pkg.code_update(c, 15)
+            pkg.update_best(c)
+            pkg.dict_update(c, 1)
+            out[fusedd] = {f: c.get(f) for f in fields}
+    for f in fields:
+        ef = rel(out["1"][f], getattr(ref, f))
+        ec = rel(out["0"][f], getattr(ref, f))
+        assert ef < TOL_X and ef < 2.0 * ec + 1e-6, (f, ef, ec)
+
+
 @pytest.mark.parametrize("mode", MODES)
 def test_deterministic(pkg, built_lib, mode):
     rng = np.random.default_rng(9)

@@ -313,8 +313,8 @@ struct DPlan {
 // per-slot HBM loads are not hidden.  Returns nullptr when off or without a variant.
 void* dfused_plan_create(cdlgb_ctx* c, int* status) {
     *status = CDLGB_OK;
-    const char* e = getenv("CDLGB_DFUSED");
-    if (!e || atoi(e) == 0) return nullptr;
+    const char* on = getenv("CDLGB_DFUSED");
+    if (!on || atoi(on) == 0) return nullptr;
     const Variant* v = nullptr;
     int cs = 0;
     for (const Variant& cand : kVariants) {

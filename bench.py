@@ -17,6 +17,11 @@ iteration of cdl_optimize (src/WRAPPER/wrap.jl:6-11): 15 X-steps, update_best!,
 FP64 NumPy port of src/CDL/train.jl, the reference having no host path of its own
 and Julia being absent) with a process per host core, each on its own slice of
 the sequences, and reports the same metric scaled to the full N.
+
+``--impl refstruct`` times the reference-structured CUDA baseline (baseline/refstruct.cu:
+the reference's CUDA.jl statements restated one for one, full-spectrum cuFFT C2C,
+a sync after every custom kernel), the stand-in for the reference GPU path, on the
+same workload on the GPU.
 """
 from __future__ import annotations
 
@@ -275,6 +280,38 @@ def run_gpu(args, rank: int, world: int):
                 fused=fused)
 
 
+def run_refstruct(args, config):
+    """The reference-structured CUDA baseline on the bench workload: wall time per outer
+    iteration (the baseline synchronises after every custom kernel, as CUDA.@sync)."""
+    sys.path.insert(0, os.path.join(ROOT, "baseline"))
+    import refstruct
+    pkg = _pkg()
+    wl = WORKLOAD
+    S = pkg.synth.onehot(dataset())
+    Lg = algorithmic_bytes()["Lg"]
+    X0 = pkg.synth.init_X0(wl["seed"], wl["N"], wl["M"], Lg)
+    D0 = pkg.synth.init_D0_unit_norm(wl["seed"], wl["M"], Lg, 4 * wl["filter_size"])
+    steps, warm = max(1, min(args.steps, 3)), 1
+    try:
+        rs = refstruct.RefStruct(S, X0, D0, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"])
+    except RuntimeError as e:
+        return {"impl": "refstruct", "unavailable": str(e)}
+    del X0
+    with rs:
+        rs.run_outer(warm, wl["csc_iter"], wl["cdl_iter"])
+        t0 = time.perf_counter()
+        rs.run_outer(steps, wl["csc_iter"], wl["cdl_iter"])
+        dt = time.perf_counter() - t0
+    rate = steps / dt
+    return {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 1, "steps": steps,
+            "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded planted motifs, Dirichlet(0.1) PWMs)", "config": config,
+            "impl": "refstruct",
+            "note": "reference-structured CUDA baseline (baseline/refstruct.cu): stand-in for the "
+                    "reference CUDA.jl path, which cannot run here"}
+
+
 def roofline(prof, steps, fused):
     """Roofline of the dominant kernel, from the phase timers recorded (CUDA events on
     the launching stream) during the timed region."""
@@ -417,7 +454,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--impl", default="native", choices=["native", "reference", "refstruct"])
     ap.add_argument("--fft-mode", type=int, default=0, help="0 auto, 1 cuFFT, 2 fused")
     ap.add_argument("--e2e-outer", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -468,6 +505,12 @@ def main():
                                  "sample": sample, "sample_ms_per_step": ms},
                 "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+
+    if args.impl == "refstruct":
+        if world > 1 and rank != 0:
+            return
+        print(json.dumps(run_refstruct(args, config)))
         return
 
     if world > 1:

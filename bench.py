@@ -405,6 +405,57 @@ def run_serve(args):
                        "L_padded": [int(r[4]) for r in reqs], "N": [int(r[2]) for r in reqs]}}
 
 
+def batched_requests(n: int = 64, seed: int = 91):
+    """The batched workload: n datasets, N log-uniform in [500, 20000], L in {100, 200, 500},
+    1-5 planted Dirichlet(0.1) motifs of width 8-20 at 10-40 % occupancy (K = 32, W = 16)."""
+    pkg = _pkg()
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        N = int(round(np.exp(rng.uniform(np.log(500), np.log(20000)))))
+        L = int(rng.choice([100, 200, 500]))
+        k = int(rng.integers(1, 6))
+        widths = [int(w) for w in rng.integers(8, 21, k)]
+        occ = [float(o) for o in rng.uniform(0.1, 0.4, k)]
+        bases, _, _ = pkg.synth.plant_dataset(seed * 1000 + i, N, L, widths, occ)
+        out.append(pkg.synth.onehot(bases))
+    return out
+
+
+def run_batched(args):
+    """The 64-dataset mix processed plainly (one training after another, each alone on
+    the GPU) and batched (all submitted at once to the continuous-batching server, up to
+    `serve_slots` trainings in flight); datasets/hr of both, and the largest difference
+    between a dataset's D_best alone and in the mix (the kernels are deterministic and
+    contexts share nothing, so it should be 0)."""
+    pkg = _pkg()
+    from cdlmotif_gb300 import serve
+    data = batched_requests(args.batched_n)
+    setup = pkg.CDLSetup(M=32, filter_size=16, lambda_=0.1, rho=1.0, sigma=100.0)
+    iters = args.serve_iters
+    serve.run_training(setup, data[0], iters, 1, 0)          # warm-up (plans, kernels)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    t0 = time.perf_counter()
+    alone = [serve.run_training(setup, d, iters, 1, 0) for d in data]
+    t_plain = time.perf_counter() - t0
+    res = serve.serve_stream(setup, [(0.0, d) for d in data], slots=args.serve_slots,
+                             iter_num=iters, seed=1)
+    clocks = sampler.stop()
+    mix = res.pop("results")
+    diff = max(float(np.max(np.abs(mix[i]["D_best"] - alone[i]["D_best"]))) for i in mix)
+    plain_rate = 3600.0 * len(data) / t_plain
+    return {"metric": "datasets/hr, 64-dataset mix (N log-uniform 500-20000, L in {100,200,500}, K=32, W=16)",
+            "value": res["datasets_per_hr"], "unit": "datasets/hr", "higher_is_better": True,
+            "plain_datasets_per_hr": plain_rate, "batched_over_plain": res["datasets_per_hr"] / plain_rate,
+            "plain_seconds": t_plain, "batched_makespan_s": res["makespan_s"],
+            "completed": res["completed"], "rejected": res["rejected"], "slots": args.serve_slots,
+            "outer_iterations_per_dataset": iters, "max_abs_diff_D_best_alone_vs_mix": diff,
+            "dtype": "f32", "data": "synthetic (seeded planted motifs)", "clocks": clocks,
+            "config": {"workload": "batched64", "N": [int(d.shape[0]) for d in data],
+                       "L": [int(d.shape[1] // 4) for d in data]}}
+
+
 def run_precision(args):
     """The float32 path (fused X-step, float64 objective) against the all-FP64 GPU
     reference from the same initial state, outer iteration by outer iteration: relative
@@ -466,6 +517,9 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-iters", type=int, default=3)
     ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--batched", action="store_true",
+                    help="64-dataset mix: plain (one at a time) vs batched (served) datasets/hr")
+    ap.add_argument("--batched-n", type=int, default=64)
     ap.add_argument("--precision", action="store_true",
                     help="precision study: float32 GPU path vs an all-FP64 GPU reference")
     ap.add_argument("--precision-iters", type=int, default=3)
@@ -490,6 +544,10 @@ def main():
     if args.precision:
         if rank == 0:
             print(json.dumps(run_precision(args)))
+        return
+    if args.batched:
+        if rank == 0:
+            print(json.dumps(run_batched(args)))
         return
 
     if args.impl == "reference":

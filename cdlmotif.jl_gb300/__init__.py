@@ -45,6 +45,7 @@ __all__ = ["CDLSetup", "CDL", "CDLGBError", "init_cdl", "code_update", "dict_upd
            "update_best", "objective", "cdl_train", "scan_w_gpu", "overlapping_scan",
            "posdicts2pfms", "count_matrices", "pfm2pwm", "pwm_complement",
            "save_pfms_as_transfac", "transfac_text", "FIELDS", "build", "ActivationRecord",
+           "non_overlap_scan",
            "record_training_result", "get_spatial_info", "get_pair_pfms", "select_pairs"]
 
 FIELDS = {"X": 0, "X_best": 1, "d": 2, "D_best": 3, "G1": 4, "G3": 5, "DX": 6, "Y1": 7,
@@ -317,6 +318,25 @@ def overlapping_scan(c: CDL, pwms, thresh, lens=None):
     _check(c._h, _lib.lib().cdlgb_scan_both(c._h, ptr(arr, C.c_float), ptr(lens, C.c_int32),
                                             ptr(th, C.c_float), K, maxlen, ptr(pos, C.c_int32),
                                             ptr(sc, C.c_float), ptr(uc, C.c_uint8)))
+    return pos, sc, uc
+
+
+def non_overlap_scan(c: CDL, positions, scores, lens, use_comp=None):
+    """non_overlap_scan!'s selection (src/SEARCH/scan.jl:123-174; without use_comp,
+    non_overlapping_scan_bg! :48-87) on the output of overlapping_scan: per sequence the
+    highest-scoring motifs whose spans do not overlap are kept, the other entries are
+    deleted (position 0).  Returns new (positions, scores, use_comp) arrays (N, K); the
+    count re-evaluation that follows in the reference is count_matrices /
+    posdicts2pfms on the kept positions."""
+    pos = np.array(positions, np.int32, copy=True, order="C")
+    sc = np.array(scores, np.float32, copy=True, order="C")
+    uc = None if use_comp is None else np.array(use_comp, np.uint8, copy=True, order="C")
+    lens = np.ascontiguousarray(lens, np.int32)
+    K = len(lens)
+    if pos.shape != (c.N, K) or sc.shape != (c.N, K):
+        raise ValueError("positions / scores must be (N, K)")
+    _check(c._h, _lib.lib().cdlgb_select_nonoverlapping(c._h, ptr(pos, C.c_int32), ptr(sc, C.c_float),
+                                                        ptr(uc, C.c_uint8), ptr(lens, C.c_int32), K))
     return pos, sc, uc
 
 

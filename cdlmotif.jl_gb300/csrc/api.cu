@@ -382,6 +382,12 @@ int cdlgb_scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const f
     return scan_fwd(c, pwms, lens, thresh, K, maxlen, pos_out);
 }
 
+int cdlgb_select_nonoverlapping(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_comp,
+                                const int32_t* lens, int32_t K) {
+    if (!c) return CDLGB_EINVAL;
+    return nonoverlap_select(c, pos, score, use_comp, lens, K);
+}
+
 int cdlgb_scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
                     int32_t K, int32_t maxlen, int32_t* pos_out, float* score_out,
                     uint8_t* use_comp_out) {

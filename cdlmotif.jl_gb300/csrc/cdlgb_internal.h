@@ -166,6 +166,8 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
               int K, int maxlen, int32_t* pos_out, float* score_out, uint8_t* comp_out);
 int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp,
                const int32_t* lens, int K, int maxlen, int32_t* counts_out, int32_t* nseq_out);
+int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_comp,
+                      const int32_t* lens, int K);
 void scan_free(cdlgb_ctx* c);
 
 static inline unsigned grid_for(size_t n, int block, unsigned cap = 152u * 32u) {

@@ -286,6 +286,83 @@ int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp, const 
     return CDLGB_OK;
 }
 
+namespace {
+// non_overlap_scan! (scan.jl:123-174): one thread per sequence n over its K entries
+// (k fastest).  sc is a scratch copy of the scores (taken entries are zeroed, as the
+// reference zeroes scores_n), keep a scratch of flags; the intersection test walks the
+// kept entries in the order they were taken.
+__global__ void k_nonoverlap(int32_t* __restrict__ pos, float* __restrict__ score,
+                             uint8_t* __restrict__ comp, const int32_t* __restrict__ lens,
+                             int K, int N, float* __restrict__ sc, int32_t* __restrict__ order) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    int32_t* P = pos + (size_t)n * K;
+    float* Sc = sc + (size_t)n * K;
+    int32_t* ord = order + (size_t)n * K;         // kept entries in the order taken
+    for (int k = 0; k < K; ++k) Sc[k] = P[k] != 0 ? score[(size_t)n * K + k] : 0.f;
+    int nkept = 0;
+    for (int iter = 0; iter < K; ++iter) {
+        int best = 0;
+        float bv = Sc[0];
+        for (int k = 1; k < K; ++k)
+            if (Sc[k] > bv) { bv = Sc[k]; best = k; }  // first maximum
+        if (bv == 0.f) break;
+        const int pm = P[best], pme = pm + lens[best] - 1;
+        bool hit = false;
+        for (int j = 0; j < nkept; ++j) {
+            const int q = ord[j], p = P[q], pe = p + lens[q] - 1;
+            if ((p <= pm && pm <= pe) || (p <= pme && pme <= pe) || (pm <= p && p <= pme) ||
+                (pm <= pe && pe <= pme))
+                hit = true;
+        }
+        if (!hit) ord[nkept++] = best;
+        Sc[best] = 0.f;
+    }
+    // delete what was not kept: mark kept entries in sc (1), the rest (0)
+    for (int k = 0; k < K; ++k) Sc[k] = 0.f;
+    for (int j = 0; j < nkept; ++j) Sc[ord[j]] = 1.f;
+    for (int k = 0; k < K; ++k)
+        if (Sc[k] == 0.f && P[k] != 0) {
+            P[k] = 0;
+            score[(size_t)n * K + k] = 0.f;
+            if (comp) comp[(size_t)n * K + k] = 0;
+        }
+}
+}  // namespace
+
+int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_comp,
+                      const int32_t* lens, int K) {
+    if (!c->loaded) return cdlgb_seterr(c, CDLGB_ESTATE, "no data loaded");
+    if (K <= 0 || !pos || !score || !lens)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "select_nonoverlapping: bad arguments");
+    for (int k = 0; k < K; ++k)
+        if (lens[k] < 1) return cdlgb_seterr(c, CDLGB_EINVAL, "select_nonoverlapping: lens[%d]=%d", k, lens[k]);
+    const int N = c->N;
+    const size_t KN = (size_t)K * N;
+    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, (size_t)K + 2 * KN));
+    ST_TRY(ensure(c, &c->scan_f, &c->scan_f_cap, 2 * KN));
+    ST_TRY(ensure(c, &c->scan_u, &c->scan_u_cap, KN));
+    int32_t* dlens = c->scan_i;
+    int32_t* dpos = c->scan_i + K;
+    int32_t* dord = dpos + KN;
+    float* dscore = c->scan_f;
+    float* dsc = c->scan_f + KN;
+    CU_TRY(c, cudaMemcpyAsync(dlens, lens, (size_t)K * 4, cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(dpos, pos, KN * 4, cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(dscore, score, KN * 4, cudaMemcpyHostToDevice, c->stream));
+    if (use_comp) CU_TRY(c, cudaMemcpyAsync(c->scan_u, use_comp, KN, cudaMemcpyHostToDevice, c->stream));
+    cdlgb_phase_begin(c, PH_SCAN);
+    k_nonoverlap<<<(N + 127) / 128, 128, 0, c->stream>>>(dpos, dscore, use_comp ? c->scan_u : nullptr,
+                                                         dlens, K, N, dsc, dord);
+    LAUNCH_CHECK(c, "k_nonoverlap");
+    cdlgb_phase_end(c, PH_SCAN);
+    CU_TRY(c, cudaMemcpyAsync(pos, dpos, KN * 4, cudaMemcpyDeviceToHost, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(score, dscore, KN * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (use_comp) CU_TRY(c, cudaMemcpyAsync(use_comp, c->scan_u, KN, cudaMemcpyDeviceToHost, c->stream));
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    return CDLGB_OK;
+}
+
 void scan_free(cdlgb_ctx* c) {
     if (c->scan_i) cudaFree(c->scan_i);
     if (c->scan_f) cudaFree(c->scan_f);

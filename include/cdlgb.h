@@ -161,6 +161,17 @@ int cdlgb_scan_both(cdlgb_ctx* ctx, const float* pwms, const int32_t* lens,
                     const float* thresh, int32_t K, int32_t maxlen, int32_t* pos_out,
                     float* score_out, uint8_t* use_comp_out);
 
+/* non_overlap_scan!'s selection (src/SEARCH/scan.jl:123-174; with use_comp NULL also
+ * non_overlapping_scan_bg!, :48-87), in place on host arrays in the layout of
+ * cdlgb_scan_both's outputs, (K, N) col-major: per sequence the entries are taken in
+ * decreasing score (first maximum on ties; missing and taken entries count as score 0)
+ * until the largest is 0, and an entry is kept when its span [pos, pos + lens[k] - 1]
+ * meets no kept span; entries not kept get pos 0, score 0, use_comp 0.  (Replaces the
+ * host loop; the background scans of overlapping_scan_bg!, :23-46, are
+ * cdlgb_scan_both on a context loaded with the background data.) */
+int cdlgb_select_nonoverlapping(cdlgb_ctx* ctx, int32_t* pos, float* score,
+                                uint8_t* use_comp, const int32_t* lens, int32_t K);
+
 /* The count matrices behind posdicts2pfms (src/SEARCH/helpers.jl:59-96): for each
  * motif k, the sum of the one-hot windows of length lens[k] at pos[k,n] (1-based,
  * 0 = none), reverse-complemented where use_comp[k,n] != 0 (use_comp may be NULL).

@@ -120,6 +120,46 @@ def overlapping_scan(data: np.ndarray, pwms: list, lens, thresh):
 # ----------------------------------------------------------------------------------
 # a22: posdicts2pfms (src/SEARCH/helpers.jl:59-96)
 # ----------------------------------------------------------------------------------
+def non_overlap_select(pos: np.ndarray, score: np.ndarray, use_comp, lens):
+    """non_overlap_scan! (src/SEARCH/scan.jl:123-174; non_overlapping_scan_bg! :48-87 is
+    the same loop without use_comp).  pos, score, use_comp are (N, K) == Julia (K, N)
+    with pos 0 = no entry for (k, n).  Per sequence: repeatedly take the motif of largest
+    score (Julia argmax: the first maximum; scores of motifs without an entry, and of
+    motifs already taken, count as 0) until that largest score is 0; keep it when its
+    span [p, p + len - 1] meets no kept span.  Entries not kept are deleted (pos, score,
+    use_comp set to 0).  Returns new (pos, score, use_comp) arrays."""
+    pos = np.array(pos, np.int32, copy=True)
+    score = np.array(score, np.float32, copy=True)
+    uc = None if use_comp is None else np.array(use_comp, np.uint8, copy=True)
+    N, K = pos.shape
+    lens = [int(x) for x in lens]
+    for n in range(N):
+        spans = []
+        keep = [False] * K
+        sc = [float(score[n, k]) if pos[n, k] != 0 else 0.0 for k in range(K)]
+        ps = [int(pos[n, k]) for k in range(K)]
+        best = int(np.argmax(np.array(sc, np.float32)))
+        while sc[best] != 0:
+            pm, pme = ps[best], ps[best] + lens[best] - 1
+            hit = False
+            for (p, l) in spans:
+                pe = p + l - 1
+                if p <= pm <= pe or p <= pme <= pe or pm <= p <= pme or pm <= pe <= pme:
+                    hit = True
+            if not hit:
+                keep[best] = True
+                spans.append((ps[best], lens[best]))
+            sc[best] = 0.0
+            best = int(np.argmax(np.array(sc, np.float32)))
+        for k in range(K):
+            if not keep[k] and pos[n, k] != 0:
+                pos[n, k] = 0
+                score[n, k] = 0
+                if uc is not None:
+                    uc[n, k] = 0
+    return pos, score, uc
+
+
 def count_matrices(data: np.ndarray, pos: np.ndarray, use_comp, lens) -> tuple:
     """The MSA column sums of posdicts2pfms (helpers.jl:73-89) as integers: for every
     motif k and sequence n with pos[k,n] > 0, add the one-hot window starting at base

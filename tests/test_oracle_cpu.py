@@ -137,6 +137,24 @@ def test_scan_oracle_integer_brute_force():
                 assert pos[k, n] == 0
 
 
+def test_non_overlap_select_known_answers():
+    """non_overlap_scan! (scan.jl:123-174): highest score first (ties: lower motif index),
+    a span meeting a kept span is dropped, entries with no hit stay empty."""
+    lens = [4, 4, 3, 5]
+    # (N, K): sequence 0: motif 0 at 1 (score 5), motif 1 at 3 (4, overlaps 0), motif 2 at
+    # 10 (3), motif 3 absent;  sequence 1: a tie between motifs 1 and 2 at overlapping
+    # spans -> motif 1 kept;  sequence 2: negative scores beside an absent motif (score 0
+    # wins argmax at once) -> nothing kept;  sequence 3: only negative scores -> the
+    # largest is taken, then the zeroed entry ends the loop
+    pos = np.array([[1, 3, 10, 0], [0, 5, 6, 20], [2, 9, 0, 0], [2, 9, 15, 30]], np.int32)
+    score = np.array([[5, 4, 3, 0], [0, 2, 2, 1], [-1, -2, 0, 0], [-1, -2, -3, -0.5]], np.float32)
+    comp = np.array([[1, 1, 0, 0], [0, 1, 1, 1], [1, 0, 0, 0], [1, 1, 1, 1]], np.uint8)
+    p2, s2, c2 = SO.non_overlap_select(pos, score, comp, lens)
+    np.testing.assert_array_equal(p2, [[1, 0, 10, 0], [0, 5, 0, 20], [0, 0, 0, 0], [0, 0, 0, 30]])
+    np.testing.assert_array_equal(s2, [[5, 0, 3, 0], [0, 2, 0, 1], [0, 0, 0, 0], [0, 0, 0, -0.5]])
+    np.testing.assert_array_equal(c2, [[1, 0, 0, 0], [0, 1, 0, 1], [0, 0, 0, 0], [0, 0, 0, 1]])
+
+
 def test_count_matrices_revcomp():
     S = np.zeros((1, 4 * 5), np.float32)
     for i, ch in enumerate("AACGT"):

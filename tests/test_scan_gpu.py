@@ -129,3 +129,24 @@ def test_count_rejects_out_of_range_window(pkg, built_lib):
         with pytest.raises(pkg.CDLGBError) as e:
             pkg.count_matrices(c, pos, [4])
         assert e.value.status == -1
+
+
+@pytest.mark.parametrize("K", [6, 40])
+def test_non_overlap_scan_matches_oracle(pkg, built_lib, K):
+    """non_overlap_scan! on the GPU against the oracle's restatement of the host loop,
+    on the output of overlapping_scan (with and without use_comp): identical arrays."""
+    rng = np.random.default_rng(17 + K)
+    S, _ = random_onehot(rng, 300, 60)
+    pwms, lens, thresh = _random_pwms(rng, K, 4, 12)
+    with _ctx(pkg, S) as c:
+        pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+        assert (pos > 0).sum() > 0
+        p2, s2, c2 = pkg.non_overlap_scan(c, pos, score, lens, comp)
+        rp, rs, rc = SO.non_overlap_select(pos, score, comp, lens)
+        np.testing.assert_array_equal(p2, rp)
+        np.testing.assert_array_equal(s2, rs)
+        np.testing.assert_array_equal(c2, rc)
+        assert (p2 > 0).sum() < (pos > 0).sum()          # overlaps were removed
+        p3, s3, _ = pkg.non_overlap_scan(c, pos, score, lens)
+        np.testing.assert_array_equal(p3, rp)
+        np.testing.assert_array_equal(s3, rs)

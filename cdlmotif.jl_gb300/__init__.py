@@ -147,6 +147,31 @@ class CDL:
         _check(self._h, _lib.lib().cdlgb_dims(self._h, *[C.byref(x) for x in d]))
         self.L, self.N, self.M, self.gamma, self.Lg = [x.value for x in d]
 
+    def load_fasta(self, fasta, max_entries: int = 10000) -> dict:
+        """read_fasta + data_2_dummy (src/LOAD/read.jl:2-28, src/LOAD/to_dummy.jl:27-38):
+        `fasta` is FASTA text (str or bytes) or a path; records with 'N'/'n' are dropped,
+        the first `max_entries` kept and one-hot encoded on the GPU.  Returns
+        {"N", "L", "wrong_length"} (records whose length differs from the first one's
+        are zero columns)."""
+        if isinstance(fasta, (str, os.PathLike)) and os.path.exists(fasta):
+            with open(fasta, "rb") as f:
+                text = f.read()
+        else:
+            text = fasta.encode() if isinstance(fasta, str) else bytes(fasta)
+        n, l, w = C.c_int32(), C.c_int32(), C.c_int32()
+        _check(self._h, _lib.lib().cdlgb_load_fasta(self._h, text, len(text), int(max_entries),
+                                                    C.byref(n), C.byref(l), C.byref(w)))
+        d = [C.c_int32() for _ in range(5)]
+        _check(self._h, _lib.lib().cdlgb_dims(self._h, *[C.byref(x) for x in d]))
+        self.L, self.N, self.M, self.gamma, self.Lg = [x.value for x in d]
+        return {"N": n.value, "L": l.value, "wrong_length": w.value}
+
+    def data(self) -> np.ndarray:
+        """The loaded one-hot data, (N, 4L) float32 (== Julia (4L, N))."""
+        out = np.empty((self.N, self.L), np.float32)
+        _check(self._h, _lib.lib().cdlgb_get(self._h, 17, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
     def init_state(self, X0=None, D0=None, seed: int = 0):
         X0c = None if X0 is None else np.ascontiguousarray(X0, np.float32).reshape(self.N, self.M, self.Lg)
         D0c = None if D0 is None else np.ascontiguousarray(D0, np.float32).reshape(self.M, self.Lg)

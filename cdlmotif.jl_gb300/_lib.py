@@ -41,6 +41,7 @@ SIGNATURES = {
     "cdlgb_last_error": (C.c_char_p, [_vp]),
     "cdlgb_footprint": (C.c_int, [C.POINTER(CdlgbParams), C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]),
     "cdlgb_load_data": (C.c_int, [_vp, _f32p, C.c_int32, C.c_int32]),
+    "cdlgb_load_fasta": (C.c_int, [_vp, C.c_char_p, C.c_size_t, C.c_int32, _i32p, _i32p, _i32p]),
     "cdlgb_dims": (C.c_int, [_vp, _i32p, _i32p, _i32p, _i32p, _i32p]),
     "cdlgb_init_state": (C.c_int, [_vp, _f32p, _f32p, C.c_uint64]),
     "cdlgb_code_update": (C.c_int, [_vp, C.c_int32]),

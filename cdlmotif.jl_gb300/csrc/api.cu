@@ -201,19 +201,52 @@ int cdlgb_footprint(const cdlgb_params* p, int32_t L, int32_t N, uint64_t* bytes
     return CDLGB_OK;
 }
 
+// one thread per base: code 0..3 -> the one-hot column (A, C, G, T); any other code
+// (a record whose length differs from the first) -> zeros
+__global__ void k_encode_onehot(const uint8_t* __restrict__ codes, float4* __restrict__ S, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const unsigned b = codes[i];
+        S[i] = make_float4(b == 0 ? 1.f : 0.f, b == 1 ? 1.f : 0.f, b == 2 ? 1.f : 0.f, b == 3 ? 1.f : 0.f);
+    }
+}
+
+// Uploads the data: the float one-hot matrix as given, or (codes != NULL) one byte per
+// base, expanded on the device.
+static int upload_data(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, size_t n) {
+    if (onehot) {
+        CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
+        return check_onehot(c);
+    }
+    uint8_t* d = nullptr;
+    CU_TRY(c, cudaMallocAsync((void**)&d, n / 4, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(d, codes, n / 4, cudaMemcpyHostToDevice, c->stream));
+    k_encode_onehot<<<grid_for(n / 4, 256), 256, 0, c->stream>>>(d, (float4*)c->S, n / 4);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(d, c->stream);
+    if (e != cudaSuccess) return cdlgb_seterr(c, CDLGB_ECUDA, "k_encode_onehot: %s", cudaGetErrorString(e));
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    c->onehot_exact = true;      // 0/1 by construction
+    return CDLGB_OK;
+}
+
+static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, int32_t L4, int32_t N);
+
 int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
     if (!c) return CDLGB_EINVAL;
     if (!onehot || L4 <= 0 || N <= 0)
         return cdlgb_seterr(c, CDLGB_EINVAL, "load_data: null data or bad size (4L=%d, N=%d)", L4, N);
+    return load_impl(c, onehot, nullptr, L4, N);
+}
+
+static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, int32_t L4, int32_t N) {
     // CDL_setup.jl:174
     if (L4 % 4) return cdlgb_seterr(c, CDLGB_EINVAL, "first dimension of dat must be multiple of 4s (got %d)", L4);
     CU_TRY(c, cudaSetDevice(c->dev));
     if (c->loaded && c->L4 == L4 && c->N == N) {
         // same shape as the resident dataset: keep every buffer and plan, replace the data
-        size_t n = (size_t)L4 * N;
-        CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
         c->initialized = false;
-        return check_onehot(c);
+        return upload_data(c, onehot, codes, (size_t)L4 * N);
     }
     if (c->loaded) {
         CU_TRY(c, cudaStreamSynchronize(c->stream));
@@ -249,7 +282,6 @@ int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
                             need / 1e9, budget / 1e9, N, L4, c->M);
     size_t n = (size_t)L4 * N;
     CU_TRY(c, cudaMalloc((void**)&c->S, n * 4));
-    CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
     int st = admm_alloc(c);
     if (st == CDLGB_OK && c->fused) st = fused_setup(c);
     if (st != CDLGB_OK) {
@@ -262,7 +294,68 @@ int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
         return cdlgb_seterr(c, st, "%s", msg.c_str());
     }
     c->loaded = true;
-    return check_onehot(c);
+    return upload_data(c, onehot, codes, n);
+}
+
+// read_fasta (src/LOAD/read.jl:2-28) and data_2_dummy (src/LOAD/to_dummy.jl:27-38):
+// records are the '>'-separated chunks of the text; in each, the first line (header)
+// is dropped and the remaining lines are joined (only '\n' is removed); records that
+// contain 'N' or 'n' are dropped; the first max_entries are kept and upper-cased.
+int cdlgb_load_fasta(cdlgb_ctx* c, const char* text, size_t nbytes, int32_t max_entries,
+                     int32_t* N_out, int32_t* L_out, int32_t* n_wrong_len) {
+    if (!c) return CDLGB_EINVAL;
+    if (!text || max_entries <= 0)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: null text or max_entries <= 0");
+    std::vector<std::string> reads;
+    size_t i = 0;
+    while (i < nbytes && (int)reads.size() < max_entries) {
+        size_t j = i;
+        while (j < nbytes && text[j] != '>') ++j;            // chunk [i, j)
+        if (j > i) {
+            size_t k = i;
+            while (k < j && text[k] != '\n') ++k;           // header line
+            std::string r;
+            bool has_n = false;
+            for (size_t t = k; t < j; ++t) {
+                const char ch = text[t];
+                if (ch == '\n') continue;
+                if (ch == 'N' || ch == 'n') has_n = true;
+                r.push_back(ch);
+            }
+            if (!has_n) reads.push_back(std::move(r));
+        }
+        i = j + 1;
+    }
+    if (reads.empty()) return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: no sequences");
+    const size_t L = reads[0].size();
+    if (L == 0) return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: the first sequence is empty");
+    if (L > (size_t)(1 << 28) / 4) return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: sequences too long");
+    const int32_t N = (int32_t)reads.size();
+    std::vector<uint8_t> codes((size_t)N * L);
+    int32_t wrong = 0;
+    for (int32_t n = 0; n < N; ++n) {
+        const std::string& r = reads[n];
+        uint8_t* o = codes.data() + (size_t)n * L;
+        if (r.size() != L) {           // left uninitialised by the reference; zeros here
+            ++wrong;
+            memset(o, 4, L);
+            continue;
+        }
+        for (size_t l = 0; l < L; ++l) {
+            const char u = (char)toupper((unsigned char)r[l]);
+            const uint8_t b = u == 'A' ? 0 : u == 'C' ? 1 : u == 'G' ? 2 : u == 'T' ? 3 : 255;
+            if (b == 255)     // dummy[uppercase(c)] raises a KeyError in the reference
+                return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: record %d has character 0x%02x at %zu",
+                                    n, (unsigned)(unsigned char)r[l], l);
+            o[l] = b;
+        }
+    }
+    int st = load_impl(c, nullptr, codes.data(), (int32_t)(4 * L), N);
+    if (st != CDLGB_OK) return st;
+    if (N_out) *N_out = N;
+    if (L_out) *L_out = (int32_t)L;
+    if (n_wrong_len) *n_wrong_len = wrong;
+    return CDLGB_OK;
 }
 
 int cdlgb_dims(const cdlgb_ctx* c, int32_t* L4, int32_t* N, int32_t* M, int32_t* gamma, int32_t* Lg) {
@@ -340,6 +433,14 @@ int cdlgb_code_threshold(cdlgb_ctx* c, double* thresh) {
 }
 
 int cdlgb_get(cdlgb_ctx* c, int32_t field, void* dst, size_t bytes) {
+    if (field == CDLGB_FIELD_DATA) {
+        NEED_LOADED(c);
+        if (!dst || bytes != (size_t)c->L4 * c->N * 4)
+            return cdlgb_seterr(c, CDLGB_EINVAL, "data is (4L, N) float32");
+        CU_TRY(c, cudaMemcpyAsync(dst, c->S, bytes, cudaMemcpyDeviceToHost, c->stream));
+        CU_TRY(c, cudaStreamSynchronize(c->stream));
+        return CDLGB_OK;
+    }
     NEED_INIT(c);
     if (!dst) return cdlgb_seterr(c, CDLGB_EINVAL, "dst is NULL");
     const void* src = nullptr;

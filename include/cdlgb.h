@@ -91,7 +91,8 @@ typedef enum {
     CDLGB_FIELD_G2 = 13,        /* (Lg, N) */
     CDLGB_FIELD_G2_DUAL = 14,   /* g2, (Lg, N) */
     CDLGB_FIELD_Y1_DUAL = 15,   /* y1, (Lg, N) */
-    CDLGB_FIELD_OBJ_BEST = 16   /* one float64 */
+    CDLGB_FIELD_OBJ_BEST = 16,  /* one float64 */
+    CDLGB_FIELD_DATA = 17       /* the loaded one-hot data, (4L, N) float32 */
 } cdlgb_field;
 
 /* Fill *p with the CDL_setup defaults. */
@@ -110,6 +111,18 @@ int cdlgb_footprint(const cdlgb_params* p, int32_t L, int32_t N, uint64_t* bytes
  * src/LOAD/to_dummy.jl:29-38; the reference's data_matrix_gpu).  Allocates the ADMM
  * state; fails with CDLGB_ENOMEM_BUDGET if it does not fit. */
 int cdlgb_load_data(cdlgb_ctx* ctx, const float* onehot, int32_t L4, int32_t N);
+
+/* read_fasta + data_2_dummy (src/LOAD/read.jl:2-28, src/LOAD/to_dummy.jl:27-38) into
+ * the context: the FASTA text is split into '>'-records, each record's header line is
+ * dropped and its remaining lines joined; records containing 'N' or 'n' are dropped;
+ * the first max_entries (the reference's max_num_read_fasta is 10000) are upper-cased
+ * and one-hot encoded on the device from one byte per base.  Records whose length
+ * differs from the first one's are zero columns (the reference leaves them
+ * uninitialised) and are counted in *n_wrong_len.  A character other than ACGTacgt ->
+ * CDLGB_EINVAL (the reference raises a KeyError).  Afterwards the context is loaded as
+ * by cdlgb_load_data with 4L = 4 *L_out and N = *N_out.  Output pointers may be NULL. */
+int cdlgb_load_fasta(cdlgb_ctx* ctx, const char* text, size_t nbytes, int32_t max_entries,
+                     int32_t* N_out, int32_t* L_out, int32_t* n_wrong_len);
 
 /* Dimensions of the loaded problem: L4 = 4L, gamma = 4*filter_size, Lg = L4 + 2*gamma. */
 int cdlgb_dims(const cdlgb_ctx* ctx, int32_t* L4, int32_t* N, int32_t* M,

@@ -120,6 +120,32 @@ def overlapping_scan(data: np.ndarray, pwms: list, lens, thresh):
 # ----------------------------------------------------------------------------------
 # a22: posdicts2pfms (src/SEARCH/helpers.jl:59-96)
 # ----------------------------------------------------------------------------------
+def read_fasta_onehot(text: bytes, max_entries: int = 10000):
+    """reading + read_fasta (src/LOAD/read.jl:2-28) and data_2_dummy
+    (src/LOAD/to_dummy.jl:27-38): records are the '>'-separated chunks, the header line
+    of each dropped and the remaining lines joined (only '\n' removed); records with
+    'N'/'n' are dropped, the first max_entries kept and upper-cased; the one-hot matrix
+    (N, 4L) float32 has a zero row for records whose length differs from the first one's
+    (uninitialised in the reference).  Returns (onehot, reads)."""
+    s = text.decode("latin-1") if isinstance(text, (bytes, bytearray)) else text
+    reads = []
+    for chunk in s.split(">"):
+        if chunk:
+            r = "".join(chunk.split("\n")[1:])
+            if "N" not in r and "n" not in r:
+                reads.append(r)
+    reads = [r.upper() for r in reads[:max_entries]]
+    L = len(reads[0])
+    out = np.zeros((len(reads), 4 * L), np.float32)
+    code = {"A": 0, "C": 1, "G": 2, "T": 3}
+    for n, r in enumerate(reads):
+        if len(r) != L:
+            continue
+        for i, ch in enumerate(r):
+            out[n, 4 * i + code[ch]] = 1.0
+    return out, reads
+
+
 def non_overlap_select(pos: np.ndarray, score: np.ndarray, use_comp, lens):
     """non_overlap_scan! (src/SEARCH/scan.jl:123-174; non_overlapping_scan_bg! :48-87 is
     the same loop without use_comp).  pos, score, use_comp are (N, K) == Julia (K, N)

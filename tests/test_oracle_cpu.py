@@ -155,6 +155,24 @@ def test_non_overlap_select_known_answers():
     np.testing.assert_array_equal(c2, [[1, 0, 0, 0], [0, 1, 0, 1], [0, 0, 0, 0], [0, 0, 0, 1]])
 
 
+FASTA_TEXT = (b">s1 first\nACGT\nAC\n>s2\nacgtac\n>s3 with an N\nACGNAC\n"
+              b">s4 short\nACG\n>s5\nTTTTGG\n")
+
+
+def test_read_fasta_onehot_rules():
+    """reading/read_fasta (read.jl:2-28) + data_2_dummy (to_dummy.jl:27-38): header lines
+    dropped, lines joined, records with N dropped, upper-cased, max_entries after the
+    filter, records of another length left as zero rows."""
+    S, reads = SO.read_fasta_onehot(FASTA_TEXT)
+    assert reads == ["ACGTAC", "ACGTAC", "ACG", "TTTTGG"]
+    assert S.shape == (4, 24)
+    np.testing.assert_array_equal(S[0], S[1])
+    assert S[2].sum() == 0 and S[3].sum() == 6
+    np.testing.assert_array_equal(S[0].reshape(6, 4).argmax(1), [0, 1, 2, 3, 0, 1])
+    S3, reads3 = SO.read_fasta_onehot(FASTA_TEXT, max_entries=2)
+    assert reads3 == ["ACGTAC", "ACGTAC"] and S3.shape == (2, 24)
+
+
 def test_count_matrices_revcomp():
     S = np.zeros((1, 4 * 5), np.float32)
     for i, ch in enumerate("AACGT"):

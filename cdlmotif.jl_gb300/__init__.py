@@ -45,7 +45,7 @@ __all__ = ["CDLSetup", "CDL", "CDLGBError", "init_cdl", "code_update", "dict_upd
            "update_best", "objective", "cdl_train", "scan_w_gpu", "overlapping_scan",
            "posdicts2pfms", "count_matrices", "pfm2pwm", "pwm_complement",
            "save_pfms_as_transfac", "transfac_text", "FIELDS", "build", "ActivationRecord",
-           "non_overlap_scan",
+           "non_overlap_scan", "get_thresh",
            "record_training_result", "get_spatial_info", "get_pair_pfms", "select_pairs"]
 
 FIELDS = {"X": 0, "X_best": 1, "d": 2, "D_best": 3, "G1": 4, "G3": 5, "DX": 6, "Y1": 7,
@@ -344,6 +344,18 @@ def overlapping_scan(c: CDL, pwms, thresh, lens=None):
                                             ptr(th, C.c_float), K, maxlen, ptr(pos, C.c_int32),
                                             ptr(sc, C.c_float), ptr(uc, C.c_uint8)))
     return pos, sc, uc
+
+
+def get_thresh(c: CDL, pwms, pval: float = 2.7e-4, lens=None) -> np.ndarray:
+    """get_thresh (src/SEARCH/helpers.jl:99): Float32(pvalue2score(pwm, pval)) per PWM
+    (Touzet-Varre score distribution, src/SEARCH/PWM_Touzet.jl:199-217), batched on
+    the GPU with exact integer counts.  Returns float32 (K,)."""
+    arr, lens, maxlen = _pack_pwms(pwms, lens)
+    K = len(lens)
+    out = np.zeros(K, np.float32)
+    _check(c._h, _lib.lib().cdlgb_pvalue_thresholds(c._h, ptr(arr, C.c_float), ptr(lens, C.c_int32), K,
+                                                    maxlen, float(pval), ptr(out, C.c_float)))
+    return out
 
 
 def non_overlap_scan(c: CDL, positions, scores, lens, use_comp=None):

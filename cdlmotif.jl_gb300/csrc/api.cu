@@ -483,6 +483,13 @@ int cdlgb_scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const f
     return scan_fwd(c, pwms, lens, thresh, K, maxlen, pos_out);
 }
 
+int cdlgb_pvalue_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int32_t K,
+                            int32_t maxlen, double pval, float* thresh_out) {
+    if (!c) return CDLGB_EINVAL;
+    CU_TRY(c, cudaSetDevice(c->dev));
+    return touzet_thresholds(c, pwms, lens, K, maxlen, pval, thresh_out);
+}
+
 int cdlgb_select_nonoverlapping(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_comp,
                                 const int32_t* lens, int32_t K) {
     if (!c) return CDLGB_EINVAL;

@@ -168,6 +168,8 @@ int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp,
                const int32_t* lens, int K, int maxlen, int32_t* counts_out, int32_t* nseq_out);
 int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_comp,
                       const int32_t* lens, int K);
+int touzet_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int K, int maxlen,
+                      double pval, float* thresh_out);
 void scan_free(cdlgb_ctx* c);
 
 static inline unsigned grid_for(size_t n, int block, unsigned cap = 152u * 32u) {

@@ -363,6 +363,150 @@ int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_com
     return CDLGB_OK;
 }
 
+namespace {
+// pvalue2score (src/SEARCH/PWM_Touzet.jl:199-217) with the reference's granularity
+// eps = 0.1 (a Float64) and flat background: the rounded entries floor(x / eps) eps are
+// exact multiples k eps, every score reached is K eps for an integer K, and every
+// probability is count / 4^m, so the reference's Double64 distribution Q[m]
+// (score_distribution, :79-102) is the integer count table below, exactly.  One CTA per
+// PWM: dense DP over K in shared memory, then find_largest_alpha (:130-142) over the
+// reached keys in ascending order.
+constexpr int kTouzetMaxR = 6144;     // score range per PWM (two uint64 tables in smem)
+
+__global__ void k_touzet(const int32_t* __restrict__ kq, const int32_t* __restrict__ lens,
+                         const int32_t* __restrict__ kmin, const int32_t* __restrict__ range,
+                         int maxlen, const unsigned long long* __restrict__ thr_count,
+                         int32_t* __restrict__ alpha_k, int32_t* __restrict__ status) {
+    extern __shared__ unsigned long long tab[];
+    const int p = blockIdx.x;
+    const int m = lens[p], R = range[p];
+    unsigned long long* Q0 = tab;
+    unsigned long long* Q1 = tab + kTouzetMaxR;
+    const int32_t* kp = kq + (size_t)p * 4 * maxlen;       // k[j][i] at j * maxlen + i
+    for (int s = threadIdx.x; s < R; s += blockDim.x) Q0[s] = 0ull;
+    __syncthreads();
+    if (threadIdx.x == 0) Q0[0] = 1ull;
+    __syncthreads();
+    int lo = 0;      // sum of the column minima so far
+    int width = 1;   // reached keys lie in [lo, lo + width)
+    for (int i = 0; i < m; ++i) {
+        int cmin = kp[i], cmax = kp[i];
+        for (int j = 1; j < 4; ++j) {
+            cmin = min(cmin, kp[j * maxlen + i]);
+            cmax = max(cmax, kp[j * maxlen + i]);
+        }
+        const int nw = width + (cmax - cmin);
+        for (int s = threadIdx.x; s < nw; s += blockDim.x) {
+            unsigned long long acc = 0ull;
+            for (int j = 0; j < 4; ++j) {
+                const int src = s - (kp[j * maxlen + i] - cmin);
+                if (src >= 0 && src < width) acc += Q0[src];
+            }
+            Q1[s] = acc;
+        }
+        __syncthreads();
+        for (int s = threadIdx.x; s < nw; s += blockDim.x) Q0[s] = Q1[s];
+        __syncthreads();
+        lo += cmin;
+        width = nw;
+    }
+    if (threadIdx.x == 0) {
+        if (lo != kmin[p] || width != R) {
+            status[p] = 1;
+            return;
+        }
+        // find_largest_alpha: q_sum starts at the total (4^m counts), keys ascending;
+        // q_sum >= pval  <=>  tail >= ceil(pval 4^m)  (integers, exact)
+        unsigned long long tail = 0ull;
+        for (int s = 0; s < width; ++s) tail += Q0[s];
+        int best = -1;
+        for (int s = 0; s < width; ++s) {
+            const unsigned long long v = Q0[s];
+            if (v == 0ull) continue;                       // keys never reached are absent
+            best = s;
+            if (tail < thr_count[p]) break;
+            tail -= v;
+        }
+        alpha_k[p] = lo + best;
+        status[p] = 0;
+    }
+}
+}  // namespace
+
+int touzet_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int K, int maxlen,
+                      double pval, float* thresh_out) {
+    if (K <= 0 || maxlen <= 0 || !pwms || !lens || !thresh_out)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "pvalue_thresholds: bad arguments");
+    if (!(pval >= 0.0 && pval <= 1.0)) return cdlgb_seterr(c, CDLGB_EINVAL, "pvalue must be in [0,1]");
+    const double eps = 1e-1;                                 // _granularity_
+    const size_t nk = (size_t)K * 4 * maxlen;
+    std::vector<int32_t> host((size_t)nk + 5 * (size_t)K, 0);
+    int32_t* kq = host.data();
+    int32_t* kmin = kq + nk;
+    int32_t* range = kmin + K;
+    int32_t* hl = range + K;
+    std::vector<unsigned long long> thr(K);
+    for (int p = 0; p < K; ++p) {
+        const int m = lens[p];
+        if (m < 1 || m > maxlen || m > 31)
+            return cdlgb_seterr(c, CDLGB_EINVAL, "pvalue_thresholds: lens[%d]=%d (1..31, <= maxlen)", p, m);
+        hl[p] = m;
+        long lo = 0, hi = 0;
+        for (int i = 0; i < m; ++i) {
+            int cmin = 0, cmax = 0;
+            for (int j = 0; j < 4; ++j) {
+                // pwms (K, 4, maxlen) col-major: element (p, j, i) at p + K (j + 4 i)
+                const double x = (double)pwms[p + (size_t)K * (j + 4 * (size_t)i)];
+                if (!(fabs(x) < 1e6))
+                    return cdlgb_seterr(c, CDLGB_EINVAL, "pvalue_thresholds: PWM entry %g", x);
+                // exact floor(x / eps): the double quotient corrected by exact fma residuals
+                double q = floor(x / eps);
+                if (fma(q, eps, -x) > 0.0) q -= 1.0;
+                else if (fma(q + 1.0, eps, -x) <= 0.0) q += 1.0;
+                const int k = (int)q;
+                kq[(size_t)p * 4 * maxlen + j * maxlen + i] = k;
+                if (j == 0 || k < cmin) cmin = k;
+                if (j == 0 || k > cmax) cmax = k;
+            }
+            lo += cmin;
+            hi += cmax;
+        }
+        if (hi - lo + 1 > kTouzetMaxR)
+            return cdlgb_seterr(c, CDLGB_ENOTSUP, "pvalue_thresholds: score range %ld of PWM %d exceeds %d",
+                                hi - lo + 1, p, kTouzetMaxR);
+        kmin[p] = (int32_t)lo;
+        range[p] = (int32_t)(hi - lo + 1);
+        thr[p] = (unsigned long long)ceil(ldexp(pval, 2 * m));   // pval 4^m is exact; <= 2^62
+    }
+    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, nk + 5 * (size_t)K));
+    int32_t* d_kq = c->scan_i;
+    int32_t* d_lens = d_kq + nk + 2 * (size_t)K;
+    int32_t* d_alpha = d_lens + K;
+    int32_t* d_status = d_alpha + K;
+    unsigned long long* d_thr = nullptr;
+    CU_TRY(c, cudaMallocAsync((void**)&d_thr, (size_t)K * sizeof(unsigned long long), c->stream));
+    CU_TRY(c, cudaMemcpyAsync(d_kq, host.data(), (nk + 3 * (size_t)K) * 4, cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, cudaMemcpyAsync(d_thr, thr.data(), (size_t)K * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                              c->stream));
+    const int shm = (int)(2 * (size_t)kTouzetMaxR * sizeof(unsigned long long));
+    CU_TRY(c, cudaFuncSetAttribute(k_touzet, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+    k_touzet<<<K, 256, shm, c->stream>>>(d_kq, d_lens, d_kq + nk, d_kq + nk + K, maxlen, d_thr, d_alpha,
+                                         d_status);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(d_thr, c->stream);
+    if (e != cudaSuccess) return cdlgb_seterr(c, CDLGB_ECUDA, "k_touzet: %s", cudaGetErrorString(e));
+    std::vector<int32_t> out(2 * (size_t)K);
+    CU_TRY(c, cudaMemcpyAsync(out.data(), d_alpha, 2 * (size_t)K * 4, cudaMemcpyDeviceToHost, c->stream));
+    CU_TRY(c, cudaStreamSynchronize(c->stream));
+    for (int p = 0; p < K; ++p) {
+        if (out[K + p] != 0) return cdlgb_seterr(c, CDLGB_ECUDA, "pvalue_thresholds: table mismatch for PWM %d", p);
+        // the Double64 key K eps is exact; its high part rounded to float32 (get_thresh's
+        // type_real conversion)
+        thresh_out[p] = (float)((double)out[p] * eps);
+    }
+    return CDLGB_OK;
+}
+
 void scan_free(cdlgb_ctx* c) {
     if (c->scan_i) cudaFree(c->scan_i);
     if (c->scan_f) cudaFree(c->scan_f);

@@ -174,6 +174,17 @@ int cdlgb_scan_both(cdlgb_ctx* ctx, const float* pwms, const int32_t* lens,
                     const float* thresh, int32_t K, int32_t maxlen, int32_t* pos_out,
                     float* score_out, uint8_t* use_comp_out);
 
+/* get_thresh (src/SEARCH/helpers.jl:99) = Float32(pvalue2score(pwm, pval)) for each of
+ * the K PWMs (src/SEARCH/PWM_Touzet.jl:199-217: granularity 0.1, flat background),
+ * batched on the device.  The rounded PWM entries are exact multiples of the Float64
+ * 0.1 and the background probabilities powers of two, so the score distribution is
+ * computed exactly as integer counts; the result equals the reference's Double64 one.
+ * pwms as for the scans, (K, 4, maxlen) col-major; lens[k] in 1..31; pval in [0, 1].
+ * thresh_out: K float32.  CDLGB_ENOTSUP when a PWM's rounded score range exceeds 6144
+ * steps of 0.1. */
+int cdlgb_pvalue_thresholds(cdlgb_ctx* ctx, const float* pwms, const int32_t* lens,
+                            int32_t K, int32_t maxlen, double pval, float* thresh_out);
+
 /* non_overlap_scan!'s selection (src/SEARCH/scan.jl:123-174; with use_comp NULL also
  * non_overlapping_scan_bg!, :48-87), in place on host arrays in the layout of
  * cdlgb_scan_both's outputs, (K, N) col-major: per sequence the entries are taken in

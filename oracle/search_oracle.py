@@ -146,6 +146,43 @@ def read_fasta_onehot(text: bytes, max_entries: int = 10000):
     return out, reads
 
 
+def pvalue2score(pwm_4m, pval: float, eps: float = 1e-1, bg=(0.25, 0.25, 0.25, 0.25)):
+    """pvalue2score (src/SEARCH/PWM_Touzet.jl:199-217) in exact rational arithmetic
+    (the reference's Double64 is exact here: every rounded entry is an integer multiple
+    of the Float64 eps, every probability a power of two), then get_thresh's Float32
+    (helpers.jl:99).  Literal restatement: min_score_range column order, round_pwm,
+    score_distribution(pwm_eps, worst_score(pwm_eps), Inf, bg) and find_largest_alpha."""
+    import math
+    from fractions import Fraction as Fr
+    P = [[Fr(float(x)) for x in row] for row in np.asarray(pwm_4m, np.float32)]
+    m = len(P[0])
+    e = Fr(eps)
+    rng = [max(P[j][i] for j in range(4)) - min(P[j][i] for j in range(4)) for i in range(m)]
+    order = sorted(range(m), key=lambda i: -rng[i])          # stable, as sortperm(rev=true)
+    R = [[math.floor(P[j][i] / e) * e for i in order] for j in range(4)]
+    alpha = sum(min(R[j][i] for j in range(4)) for i in range(m))
+    bgf = [Fr(b) for b in bg]
+    Q = {Fr(0): Fr(1)}
+    for i in range(m):
+        bs = sum(max(R[j][ii] for j in range(4)) for ii in range(i + 1, m))
+        Qn = {}
+        for score in sorted(Q):
+            for j in range(4):
+                t = score + R[j][i]
+                if alpha - bs <= t:                              # t <= beta - ws with beta = Inf
+                    Qn[t] = Qn.get(t, Fr(0)) + Q[score] * bgf[j]
+        Q = Qn
+    q_sum = sum(Q.values())
+    largest = None
+    for k in sorted(Q):
+        if q_sum >= Fr(pval):
+            largest = k
+        else:
+            return np.float32(float(k))
+        q_sum -= Q[k]
+    return np.float32(float(largest))
+
+
 def non_overlap_select(pos: np.ndarray, score: np.ndarray, use_comp, lens):
     """non_overlap_scan! (src/SEARCH/scan.jl:123-174; non_overlapping_scan_bg! :48-87 is
     the same loop without use_comp).  pos, score, use_comp are (N, K) == Julia (K, N)

@@ -173,6 +173,19 @@ def test_read_fasta_onehot_rules():
     assert reads3 == ["ACGTAC", "ACGTAC"] and S3.shape == (2, 24)
 
 
+def test_pvalue2score_known_answers():
+    """find_largest_alpha (PWM_Touzet.jl:130-142) returns the first key (ascending) whose
+    tail probability is below pval; with one column (2, 0, 0, 0) the rounded keys are 0
+    (probability 3/4) and floor(2 / 0.1) 0.1 = 1.9 (the Float64 0.1 is above 1/10)."""
+    pwm = np.array([[2.0], [0.0], [0.0], [0.0]], np.float32)
+    assert SO.pvalue2score(pwm, 0.25) == np.float32(1.9)
+    assert SO.pvalue2score(pwm, 0.3) == np.float32(1.9)
+    pwm2 = np.array([[1.0, 1.0], [0.0, 0.0], [0.0, 0.0], [0.0, 0.0]], np.float32)
+    # keys 0 (9/16), 0.9 (6/16: one column hit... floor(1/0.1)=9), 1.8 (1/16)
+    assert SO.pvalue2score(pwm2, 1.0 / 16) == np.float32(1.8)
+    assert SO.pvalue2score(pwm2, 0.5) == np.float32(0.9)
+
+
 def test_count_matrices_revcomp():
     S = np.zeros((1, 4 * 5), np.float32)
     for i, ch in enumerate("AACGT"):

@@ -150,3 +150,15 @@ def test_non_overlap_scan_matches_oracle(pkg, built_lib, K):
         p3, s3, _ = pkg.non_overlap_scan(c, pos, score, lens)
         np.testing.assert_array_equal(p3, rp)
         np.testing.assert_array_equal(s3, rs)
+
+
+@pytest.mark.parametrize("pval", [2.7e-4, 1e-3, 0.05])
+def test_pvalue_thresholds_match_oracle(pkg, built_lib, pval):
+    """get_thresh / pvalue2score (PWM_Touzet.jl:199-217) batched on the GPU with exact
+    integer counts, against the exact-rational restatement: identical float32."""
+    rng = np.random.default_rng(int(pval * 1e6) % 1000)
+    pwms, lens, _ = _random_pwms(rng, 12, 3, 12)
+    with _ctx(pkg, random_onehot(rng, 4, 30)[0]) as c:
+        th = pkg.get_thresh(c, pwms, pval)
+    ref = np.array([SO.pvalue2score(p, pval) for p in pwms], np.float32)
+    np.testing.assert_array_equal(th, ref)

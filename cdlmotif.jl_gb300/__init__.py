@@ -172,6 +172,23 @@ class CDL:
         _check(self._h, _lib.lib().cdlgb_get(self._h, 17, out.ctypes.data_as(C.c_void_p), out.nbytes))
         return out
 
+    def autotune(self) -> dict:
+        """Time every fused X-step variant for this dataset's shape on a prefix of the
+        sequences and keep the fastest (cdlgb_autotune).  Returns the candidates with
+        their ms per X-step and the chosen index."""
+        maxc = 16
+        ms = np.zeros(maxc, np.float64)
+        kind, cs, mc = (np.zeros(maxc, np.int32) for _ in range(3))
+        n, ch = C.c_int32(), C.c_int32()
+        _check(self._h, _lib.lib().cdlgb_autotune(self._h, maxc, ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  ptr(kind, C.c_int32), ptr(cs, C.c_int32), ptr(mc, C.c_int32),
+                                                  C.byref(n), C.byref(ch)))
+        k = n.value
+        names = {1: "multi-iteration", 2: "one-X-step"}
+        cands = [{"kernel": names[int(kind[i])], "cluster": int(cs[i]), "filters_per_cta": int(mc[i]),
+                  "ms_per_xstep": float(ms[i])} for i in range(k)]
+        return {"candidates": cands, "chosen": ch.value}
+
     def init_state(self, X0=None, D0=None, seed: int = 0):
         X0c = None if X0 is None else np.ascontiguousarray(X0, np.float32).reshape(self.N, self.M, self.Lg)
         D0c = None if D0 is None else np.ascontiguousarray(D0, np.float32).reshape(self.M, self.Lg)

@@ -55,6 +55,7 @@ SIGNATURES = {
     "cdlgb_scan_both": (C.c_int, [_vp, _f32p, _i32p, _f32p, C.c_int32, C.c_int32, _i32p, _f32p, _u8p]),
     "cdlgb_select_nonoverlapping": (C.c_int, [_vp, _i32p, _f32p, _u8p, _i32p, C.c_int32]),
     "cdlgb_pvalue_thresholds": (C.c_int, [_vp, _f32p, _i32p, C.c_int32, C.c_int32, C.c_double, _f32p]),
+    "cdlgb_autotune": (C.c_int, [_vp, C.c_int32, C.POINTER(C.c_double), _i32p, _i32p, _i32p, _i32p, _i32p]),
     "cdlgb_count_pfms": (C.c_int, [_vp, _i32p, _u8p, _i32p, C.c_int32, C.c_int32, _i32p, _i32p]),
     "cdlgb_counts_to_pfms": (C.c_int, [_i32p, _i32p, _i32p, C.c_int32, C.c_int32, C.c_float,
                                        C.c_float, C.c_int32, C.c_int32, _f32p]),

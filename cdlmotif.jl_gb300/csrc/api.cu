@@ -483,6 +483,15 @@ int cdlgb_scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const f
     return scan_fwd(c, pwms, lens, thresh, K, maxlen, pos_out);
 }
 
+int cdlgb_autotune(cdlgb_ctx* c, int32_t max_candidates, double* ms_per_xstep, int32_t* kind,
+                   int32_t* cluster, int32_t* filters, int32_t* n_candidates, int32_t* chosen) {
+    NEED_INIT(c);
+    if (!ms_per_xstep || !kind || !cluster || !filters || !n_candidates || !chosen || max_candidates <= 0)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "autotune: bad arguments");
+    if (!c->fused) return cdlgb_seterr(c, CDLGB_ENOTSUP, "autotune: the cuFFT path has no variants");
+    return fused_autotune(c, max_candidates, ms_per_xstep, kind, cluster, filters, n_candidates, chosen);
+}
+
 int cdlgb_pvalue_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int32_t K,
                             int32_t maxlen, double pval, float* thresh_out) {
     if (!c) return CDLGB_EINVAL;

@@ -151,6 +151,15 @@ void iter_plan_free(void* p);
 int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters);
 int iter_absx(void* p, const double** part, int* n);
 int iter_plan_cluster(void* p);
+int iter_plan_filters(void* p);
+int iter_plan_grid(void* p);
+void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status);
+int iter_xsteps_n(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters, int Nlim);
+int warp_xstep_n(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int Nlim);
+int warp_plan_cluster(void* p);
+int warp_plan_filters(void* p);
+int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* cs, int32_t* mc,
+                   int32_t* n_out, int32_t* chosen);
 int fused_has_multi(cdlgb_ctx* c);
 // fused D-step (dfused.cu)
 void* dfused_plan_create(cdlgb_ctx* c, int* status);

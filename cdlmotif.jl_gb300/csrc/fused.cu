@@ -20,6 +20,8 @@
 // X written once, plus the per-sequence vectors.
 #include "cdlgb_internal.h"
 
+#include <algorithm>
+
 #include <cooperative_groups.h>
 #include <math.h>
 #include <stdlib.h>
@@ -664,6 +666,123 @@ int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs) {
 int fused_has_dstep(cdlgb_ctx* c) {
     FusedPlan* P = (FusedPlan*)c->fplan;
     return P && P->dplan;
+}
+
+// The X-step autotuner: every register-FFT X-step variant that fits (multi-iteration
+// kernels with each filters-per-CTA choice, and the one-X-step kernel) is timed with
+// CUDA events on a prefix of the loaded sequences (the state of that prefix is saved
+// before and restored after every run), and the fastest is kept for this context.
+int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* cs, int32_t* mc,
+                   int32_t* n_out, int32_t* chosen) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    if (!P || (!P->iter && !P->warp))
+        return cdlgb_seterr(c, CDLGB_ENOTSUP, "autotune: no register-FFT X-step for Lg=%d", c->Lg);
+    struct Cand { int kind; void* plan; };
+    std::vector<Cand> cands;
+    auto free_all = [&](int keep) {
+        for (int i = 0; i < (int)cands.size(); ++i) {
+            if (i == keep) continue;
+            if (cands[i].kind == 1) iter_plan_free(cands[i].plan);
+            else warp_plan_free(cands[i].plan);
+        }
+    };
+    int st = CDLGB_OK;
+    for (int nth = 0;; ++nth) {
+        void* ip = iter_plan_create_nth(c, nth, 0, &st);
+        if (st != CDLGB_OK) { free_all(-1); return st; }
+        if (!ip) break;
+        cands.push_back({1, ip});
+    }
+    {
+        void* wp = warp_plan_create(c, &st);
+        if (st != CDLGB_OK) { free_all(-1); return st; }
+        if (wp) cands.push_back({2, wp});
+    }
+    if (cands.empty()) return cdlgb_seterr(c, CDLGB_ENOTSUP, "autotune: no candidate");
+    if ((int)cands.size() > maxc) {
+        free_all(-1);
+        return cdlgb_seterr(c, CDLGB_EINVAL, "autotune: %zu candidates, room for %d", cands.size(), maxc);
+    }
+    // the prefix of sequences the candidates are timed on
+    int maxcl = 1;
+    for (const Cand& k : cands) {
+        const int cl = k.kind == 1 ? iter_plan_grid(k.plan) / iter_plan_cluster(k.plan) : 0;
+        maxcl = std::max(maxcl, cl);
+    }
+    // 64 sequences per cluster of the largest grid (the steady state of a persistent
+    // grid, not its start-up), the saved state of the prefix at most 1 GB
+    const size_t per_seq = ((size_t)3 * c->M + 3) * c->Lg * sizeof(float);
+    const int Nl = (int)std::min<size_t>({(size_t)c->N, (size_t)64 * maxcl,
+                                          std::max<size_t>(1, ((size_t)1 << 30) / per_seq)});
+    const size_t lmn = (size_t)Nl * c->M * c->Lg, ln = (size_t)Nl * c->Lg;
+    float* X = c->Xb[c->xcur];
+    float* snap = nullptr;
+    cudaStream_t s = c->stream;
+    CU_TRY(c, cudaMallocAsync((void**)&snap, (3 * lmn + 3 * ln) * sizeof(float), s));
+    float* src[6] = {X, c->y2, c->y3, c->Y1, c->y1, c->DX};
+    const size_t cnt[6] = {lmn, lmn, lmn, ln, ln, ln};
+    size_t off[6];
+    {
+        size_t o = 0;
+        for (int i = 0; i < 6; ++i) { off[i] = o; o += cnt[i]; }
+    }
+    auto copy = [&](bool save) -> int {
+        for (int i = 0; i < 6; ++i) {
+            float* a = save ? snap + off[i] : src[i];
+            const float* b = save ? src[i] : snap + off[i];
+            CU_TRY(c, cudaMemcpyAsync(a, b, cnt[i] * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        }
+        return CDLGB_OK;
+    };
+    auto run = [&](const Cand& k, int iters) -> int {
+        if (k.kind == 1) return iter_xsteps_n(c, k.plan, X, X, iters, Nl);
+        for (int it = 0; it < iters; ++it) ST_TRY(warp_xstep_n(c, k.plan, X, X, Nl));
+        return CDLGB_OK;
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int best = -1;
+    double best_ms = 0.0;
+    int rc = copy(true);
+    if (rc == CDLGB_OK && cudaEventCreate(&e0) != cudaSuccess) rc = cdlgb_seterr(c, CDLGB_ECUDA, "event");
+    if (rc == CDLGB_OK && cudaEventCreate(&e1) != cudaSuccess) rc = cdlgb_seterr(c, CDLGB_ECUDA, "event");
+    // as many X-steps as a code update runs: the multi-iteration kernel loads and
+    // stores the state once per launch
+    const int kIters = std::max(1, (int)c->p.csc_iter_num);
+    for (int i = 0; rc == CDLGB_OK && i < (int)cands.size(); ++i) {
+        rc = run(cands[i], 1);                           // warm-up
+        if (rc == CDLGB_OK) rc = copy(false);
+        if (rc == CDLGB_OK) cudaEventRecord(e0, s);
+        if (rc == CDLGB_OK) rc = run(cands[i], kIters);
+        if (rc == CDLGB_OK) cudaEventRecord(e1, s);
+        if (rc == CDLGB_OK && cudaEventSynchronize(e1) != cudaSuccess)
+            rc = cdlgb_seterr(c, CDLGB_ECUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+        float t = 0.f;
+        if (rc == CDLGB_OK) cudaEventElapsedTime(&t, e0, e1);
+        if (rc == CDLGB_OK) rc = copy(false);
+        const double per = (double)t / kIters;
+        ms[i] = per;
+        kind[i] = cands[i].kind;
+        cs[i] = cands[i].kind == 1 ? iter_plan_cluster(cands[i].plan) : warp_plan_cluster(cands[i].plan);
+        mc[i] = cands[i].kind == 1 ? iter_plan_filters(cands[i].plan) : warp_plan_filters(cands[i].plan);
+        if (rc == CDLGB_OK && (best < 0 || per < best_ms)) { best = i; best_ms = per; }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFreeAsync(snap, s);
+    if (rc != CDLGB_OK) { free_all(-1); return rc; }
+    CU_TRY(c, cudaStreamSynchronize(s));
+    // keep the winner
+    iter_plan_free(P->iter);
+    warp_plan_free(P->warp);
+    P->iter = nullptr;
+    P->warp = nullptr;
+    if (cands[best].kind == 1) P->iter = cands[best].plan;
+    else P->warp = cands[best].plan;
+    free_all(best);
+    c->absx_fused = 0;           // the partial sums of |X| belong to the timing runs
+    *n_out = (int32_t)cands.size();
+    *chosen = best;
+    return CDLGB_OK;
 }
 
 int fused_dstep(cdlgb_ctx* c) {

@@ -369,6 +369,13 @@ void* iter_plan_create(cdlgb_ctx* c, int* status) {
         if (atoi(e) == 0) return nullptr;
     int want_cs = 0;
     if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
+    return iter_plan_create_nth(c, 0, want_cs, status);
+}
+
+// The nth variant (in kVariants order) that fits Lg and M, optionally only with
+// cluster size want_cs; nullptr when there is none.
+void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
+    *status = CDLGB_OK;
     IterPlan* P = nullptr;
     const Variant* v = nullptr;
     for (const Variant& cand : kVariants) {
@@ -380,6 +387,7 @@ void* iter_plan_create(cdlgb_ctx* c, int* status) {
         const int ld3 = 3 * cand.N1 / 4 * cand.P;
         const size_t sm = iter_smem(cand.N1, cand.P, (cand.MC + 1) / 2 + 1, cand.MC, ld, ld3, c->L4);
         if (sm > (cand.minb == 2 ? kCap2 : kCap1)) continue;
+        if (nth-- > 0) continue;
         v = &cand;
         P = new IterPlan();
         P->k = cand.k; P->CS = cs; P->Mc = cand.MC; P->ld = ld; P->ld3 = ld3;
@@ -434,14 +442,21 @@ void iter_plan_free(void* p) {
 }
 
 int iter_plan_cluster(void* p) { return p ? ((IterPlan*)p)->CS : 0; }
+int iter_plan_filters(void* p) { return p ? ((IterPlan*)p)->Mc : 0; }
+int iter_plan_grid(void* p) { return p ? ((IterPlan*)p)->grid : 0; }
 
 int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters) {
+    return iter_xsteps_n(c, p, Xin, Xout, iters, c->N);
+}
+
+// `iters` X-steps over the first Nlim sequences (the autotuner times on a prefix)
+int iter_xsteps_n(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters, int Nlim) {
     IterPlan* P = (IterPlan*)p;
     IArgs a;
     a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
     a.Y1 = c->Y1; a.y1 = c->y1; a.DX = c->DX; a.S = c->S;
     a.G1h = c->G1h; a.Ah = c->Ah; a.tw2 = P->tw2; a.absx_part = P->absx_part;
-    a.N = c->N; a.M = c->M; a.L4 = c->L4; a.gamma = c->gamma; a.iters = iters;
+    a.N = Nlim; a.M = c->M; a.L4 = c->L4; a.gamma = c->gamma; a.iters = iters;
     a.lam = c->p.lambda; a.rho = c->p.rho; a.kc = c->p.sherman_const_csc;
     a.ld = P->ld; a.ld3 = P->ld3;
     cudaLaunchConfig_t cfg = {};

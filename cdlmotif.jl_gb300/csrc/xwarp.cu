@@ -422,14 +422,20 @@ void warp_plan_free(void* p) {
 }
 
 int warp_plan_cluster(void* p) { return p ? ((WarpPlan*)p)->CS : 0; }
+int warp_plan_filters(void* p) { return p ? ((WarpPlan*)p)->Mc : 0; }
 
 int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout) {
+    return warp_xstep_n(c, p, Xin, Xout, c->N);
+}
+
+// one X-step over the first Nlim sequences (the autotuner times on a prefix)
+int warp_xstep_n(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int Nlim) {
     WarpPlan* P = (WarpPlan*)p;
     WArgs a;
     a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
     a.Y1 = c->Y1; a.y1 = c->y1; a.DX = c->DX; a.S = c->S;
     a.G1h = c->G1h; a.Ah = c->Ah; a.tw2 = P->tw2; a.absx_part = P->absx_part;
-    a.N = c->N; a.M = c->M; a.F = c->F; a.L4 = c->L4; a.gamma = c->gamma;
+    a.N = Nlim; a.M = c->M; a.F = c->F; a.L4 = c->L4; a.gamma = c->gamma;
     a.lam = c->p.lambda; a.rho = c->p.rho; a.kc = c->p.sherman_const_csc;
     a.Mc = P->Mc; a.B = P->B;
     cudaLaunchConfig_t cfg = {};

@@ -174,6 +174,17 @@ int cdlgb_scan_both(cdlgb_ctx* ctx, const float* pwms, const int32_t* lens,
                     const float* thresh, int32_t K, int32_t maxlen, int32_t* pos_out,
                     float* score_out, uint8_t* use_comp_out);
 
+/* Autotuner (no counterpart in the reference): times every fused X-step variant that
+ * fits this context's Lg and M -- the multi-iteration kernel with each choice of
+ * filters per CTA (hence cluster size), then the one-X-step kernel -- with CUDA events
+ * on a prefix of the loaded sequences, restoring that prefix's state after each run,
+ * and keeps the fastest for the following code updates.  Per candidate i <
+ * *n_candidates: ms_per_xstep[i], kind[i] (1 multi-iteration, 2 one X-step),
+ * cluster[i] (CTAs per cluster), filters[i] (filters per CTA); *chosen = the winner.
+ * Needs an initialised state and the fused path (CDLGB_ENOTSUP otherwise). */
+int cdlgb_autotune(cdlgb_ctx* ctx, int32_t max_candidates, double* ms_per_xstep, int32_t* kind,
+                   int32_t* cluster, int32_t* filters, int32_t* n_candidates, int32_t* chosen);
+
 /* get_thresh (src/SEARCH/helpers.jl:99) = Float32(pvalue2score(pwm, pval)) for each of
  * the K PWMs (src/SEARCH/PWM_Touzet.jl:199-217: granularity 0.1, flat background),
  * batched on the device.  The rounded PWM entries are exact multiples of the Float64

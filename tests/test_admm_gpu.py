@@ -313,3 +313,34 @@ def test_profile_counts_launches(pkg, built_lib):
         pr = c.profile_read()
         assert pr["xstep"][1] == 3 and pr["dstep"][1] == 1
         assert pr["launches"] > 0 and pr["xstep"][0] > 0
+
+
+def test_autotune_keeps_results(pkg, built_lib, monkeypatch):
+    """The autotuner times every X-step variant on a prefix of the sequences and keeps
+    the fastest; the prefix's state is restored afterwards, so a tuned training equals,
+    bit for bit, an untuned one pinned to the chosen variant (variants with other
+    cluster sizes sum the cross-filter parts in another association)."""
+    synth = pkg.synth
+    N, L, M, fs = 40, 200, 64, 16
+    bases, _, _ = synth.plant_dataset(19, N, L, [8, 12], [0.4, 0.4])
+    S = synth.onehot(bases)
+    Lg = 4 * L + 8 * fs
+    X0 = synth.init_X0(7, N, M, Lg)
+    D0 = synth.init_D0_unit_norm(7, M, Lg, 4 * fs)
+    out = []
+    with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+        info = c.autotune()
+        assert len(info["candidates"]) >= 3
+        kinds = {x["kernel"] for x in info["candidates"]}
+        assert kinds == {"multi-iteration", "one-X-step"}
+        assert all(x["ms_per_xstep"] > 0 for x in info["candidates"])
+        best = info["candidates"][info["chosen"]]
+        assert best["ms_per_xstep"] == min(x["ms_per_xstep"] for x in info["candidates"])
+        out.append((pkg.run_outer(c, 2), c.X, c.d, c.D_best))
+    monkeypatch.setenv("CDLGB_CLUSTER", str(best["cluster"]))
+    monkeypatch.setenv("CDLGB_XITER", "1" if best["kernel"] == "multi-iteration" else "0")
+    with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+        out.append((pkg.run_outer(c, 2), c.X, c.d, c.D_best))
+    np.testing.assert_allclose(out[0][0], out[1][0], rtol=1e-6)
+    for a, b in zip(out[0][1:], out[1][1:]):
+        np.testing.assert_array_equal(a, b)

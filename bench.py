@@ -193,6 +193,24 @@ def cpu_reference(steps: int, warmup: int, procs: int, per_proc: int):
 
 
 # ------------------------------------------------------------------------ GPU leg
+def max_over_ranks(x: float, world: int, device: str) -> float:
+    """The largest of every rank's x (all-reduce MAX; the process group's backend
+    decides where the tensor lives: NCCL on the GPU, gloo on the CPU)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world: int, units_per_rank: int, seconds_max: float) -> float:
+    """Whole-job rate of `world` independent replicas, each processing units_per_rank
+    outer iterations, timed by the slowest rank."""
+    return world * units_per_rank / seconds_max
+
+
 def run_gpu(args, rank: int, world: int):
     import torch
     pkg = _pkg()
@@ -238,12 +256,8 @@ def run_gpu(args, rank: int, world: int):
     ms = e0.elapsed_time(e1)
     prof = c.profile_read(reset=True)
     c.profile(False)
-    ms_t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{dev}")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ms, world, f"cuda:{dev}")
+    value = replica_rate(world, args.steps, ms_max / 1e3)
 
     # ---- end-to-end leg through the C ABI with host buffers
     E = args.e2e_outer
@@ -267,11 +281,8 @@ def run_gpu(args, rank: int, world: int):
         Db = c.get("D_best")                 # D2H of the learned filters
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
-    te = torch.tensor([t_e2e], dtype=torch.float64, device=f"cuda:{dev}")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * e_steps * E / float(te.item())
+    t_max = max_over_ranks(t_e2e, world, f"cuda:{dev}")
+    e2e_value = replica_rate(world, e_steps * E, t_max)
     h2d = S.nbytes
     d2h = Db.nbytes + 8 * E
     fused = bool(c._p.fft_mode != 1) and prof["xfused"][1] > 0

@@ -764,15 +764,20 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             for (int n0 = 0; n0 < N; n0 += c->chunk) {
                 const int cn = std::min(c->chunk, N - n0);
                 const size_t off = (size_t)n0 * M * Lg, cl = (size_t)cn * M * Lg;
-                k_dprep<<<grid_for(cl / 4, kBlock), kBlock, 0, s>>>(
-                    (const float4*)(cur_X(c) + off), (const float4*)(c->y3 + off),
-                    (const float4*)(c->g1 + off), (const float4*)(c->g3 + off),
-                    (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA, (float4*)c->sB,
-                    cl / 4, LM / 4);
-                LAUNCH_CHECK(c, "k_dprep");
-                ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
-                ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh));
-                ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh));
+                if (void* fw = c->fused ? fused_dfwd(c) : nullptr) {
+                    // Y3, H and d formed and transformed in one streaming pass
+                    ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, c->sBh, c->sCh));
+                } else {
+                    k_dprep<<<grid_for(cl / 4, kBlock), kBlock, 0, s>>>(
+                        (const float4*)(cur_X(c) + off), (const float4*)(c->y3 + off),
+                        (const float4*)(c->g1 + off), (const float4*)(c->g3 + off),
+                        (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA, (float4*)c->sB,
+                        cl / 4, LM / 4);
+                    LAUNCH_CHECK(c, "k_dprep");
+                    ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
+                    ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh));
+                    ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh));
+                }
                 k_dsolve<<<(unsigned)((size_t)nfb * cn), 128, 0, s>>>(
                     c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F, c->sVh + (size_t)n0 * F, F, M, nfb,
                     c->p.sherman_const_cdl, 1.f / (float)Lg);

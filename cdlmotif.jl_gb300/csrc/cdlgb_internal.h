@@ -166,6 +166,11 @@ void* dfused_plan_create(cdlgb_ctx* c, int* status);
 void dfused_plan_free(void* p);
 int dfused_step(cdlgb_ctx* c, void* p, const float* X);
 int fused_has_dstep(cdlgb_ctx* c);
+// streaming forward transforms of the D-step (dstream.cu)
+void* dfwd_plan_create(cdlgb_ctx* c, int* status);
+void dfwd_plan_free(void* p);
+int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh);
+void* fused_dfwd(cdlgb_ctx* c);
 int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 
 // ---- scan.cu ----

@@ -1,0 +1,183 @@
+// Forward half of the D-step (dict_update!, src/CDL/train.jl:52-57) as one streaming
+// kernel for the transform lengths with register-resident FFTs (regfft.cuh).
+//
+// For every (sequence n, filter pair a = 2s, b = 2s + 1) a lane group forms, straight
+// from the state arrays, the three packed real pairs the D-step transforms --
+//   Y3 = projectionX!(X + y3)                 (X + y3 on the rows l % 4 == 0, else 0)
+//   H  = (G1 - g1) + (G3 - g3)                (the filter-domain terms of sherman_CDL_RHS!)
+//   d  (the previous iterate)
+// -- runs the four-step FFT on each and writes the split half-spectra (f = 0..Lg/2) of
+// both filters where the per-frequency solve expects them, (n, m, f).  It replaces a
+// pass that wrote Y3 and H to HBM and three cuFFT R2C transforms (each a complex FFT
+// and a post-processing pass over the spectra).
+#include "cdlgb_internal.h"
+#include "regfft.cuh"
+
+#include <stdlib.h>
+#include <vector>
+
+namespace {
+
+struct FArgs {
+    const float* X;       // chunk (cn, M, Lg)
+    const float* y3;
+    const float* g1;
+    const float* g3;
+    const float* d;
+    const float* G1;      // (M, Lg)
+    const float* G3;
+    float2* Yh;           // chunk (cn, M, F)
+    float2* Hh;
+    float2* Dh;
+    const float2* tw2;    // [P][N1]
+    int cn, M;
+};
+
+// split the packed spectrum Z = A + i B of two real sequences held in natural order in
+// `buf` and store A[f], B[f] for f = 0..Lg/2 (lanes over f)
+template <int Lg, int N1>
+__device__ __forceinline__ void split_store(const float2* __restrict__ buf, int gl,
+                                            float2* __restrict__ oa, float2* __restrict__ ob) {
+    constexpr int F = Lg / 2 + 1;
+    for (int f = gl; f < F; f += N1) {
+        const float2 z1 = buf[f], z2 = buf[f == 0 ? 0 : Lg - f];
+        oa[f] = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+        ob[f] = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+    }
+}
+
+template <int N1, int P>
+__global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
+    constexpr int Lg = N1 * P;
+    constexpr int G = 32 / N1;
+    constexpr int RS = N1 + 1;
+    constexpr int BUF = (P * RS + 1) & ~1;
+    constexpr int F = Lg / 2 + 1;
+    extern __shared__ float4 smem4[];
+    float2* tw2 = reinterpret_cast<float2*>(smem4);        // [P][N1]
+    float2* bufs = tw2 + P * N1;                           // [groups][BUF]
+    for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int gw = (threadIdx.x >> 5) * G + lane / N1;     // lane group in the CTA
+    const int gl = lane % N1;
+    const int groups = (blockDim.x >> 5) * G;
+    const bool keep = (gl & 3) == 0;                       // l = gl + N1 n2, N1 % 4 == 0
+    float2* sb = bufs + (size_t)gw * BUF;
+    const int pairs = A.M / 2;
+    const long items = (long)A.cn * pairs;
+    const long stride = (long)gridDim.x * groups;
+    // every lane group of a warp runs the same number of rounds (the row DFT syncs the warp)
+    const long rounds = (items + stride - 1) / stride;
+    for (long r = 0; r < rounds; ++r) {
+        const long item = r * stride + (long)blockIdx.x * groups + gw;
+        const bool act = item < items;
+        const long n = act ? item / pairs : 0;
+        const int s = act ? (int)(item - n * pairs) : 0;
+        const int ma = 2 * s;
+        const size_t ra = ((size_t)n * A.M + ma) * Lg + gl;   // row of filter a at lane gl
+        const size_t pa = (size_t)ma * Lg + gl;
+        const size_t oa = ((size_t)n * A.M + ma) * F;
+        for (int which = 0; which < 3; ++which) {
+            if (act) {
+#pragma unroll 4
+                for (int n2 = 0; n2 < P; ++n2) {
+                    const int o = N1 * n2;
+                    float2 v;
+                    if (which == 0) {
+                        v = keep ? f2(A.X[ra + o] + A.y3[ra + o], A.X[ra + Lg + o] + A.y3[ra + Lg + o])
+                                 : f2(0.f, 0.f);
+                    } else if (which == 1) {
+                        v = f2((A.G1[pa + o] - A.g1[ra + o]) + (A.G3[pa + o] - A.g3[ra + o]),
+                               (A.G1[pa + Lg + o] - A.g1[ra + Lg + o]) + (A.G3[pa + Lg + o] - A.g3[ra + Lg + o]));
+                    } else {
+                        v = f2(A.d[ra + o], A.d[ra + Lg + o]);
+                    }
+                    sb[n2 * RS + gl] = v;
+                }
+                fwd_step1<N1, P>(sb, gl, tw2);
+            }
+            __syncwarp();
+            fwd_step2<N1, P>(sb, gl, act);
+            if (act) {
+                float2* out = which == 0 ? A.Yh : which == 1 ? A.Hh : A.Dh;
+                split_store<Lg, N1>(sb, gl, out + oa, out + oa + F);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+typedef void (*kern_t)(FArgs);
+struct Variant { int N1, P; kern_t k; };
+const Variant kVariants[] = {
+    {32, 29, k_dfwd<32, 29>},
+    {16, 31, k_dfwd<16, 31>},
+};
+
+struct FwdPlan {
+    kern_t k;
+    int N1, P;
+    size_t smem;
+    int grid;
+    float2* tw2;
+};
+
+}  // namespace
+
+// Returns nullptr when Lg has no register-FFT variant (or CDLGB_DSTREAM=0).
+void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
+    *status = CDLGB_OK;
+    if (const char* e = getenv("CDLGB_DSTREAM"))
+        if (atoi(e) == 0) return nullptr;
+    if (c->M % 2) return nullptr;
+    const Variant* v = nullptr;
+    for (const Variant& cand : kVariants)
+        if (cand.N1 * cand.P == c->Lg) v = &cand;
+    if (!v) return nullptr;
+    FwdPlan* P = new FwdPlan();
+    P->k = v->k; P->N1 = v->N1; P->P = v->P;
+    const int threads = 256, groups = (threads / 32) * (32 / v->N1);
+    const size_t buf = ((size_t)v->P * (v->N1 + 1) + 1) & ~(size_t)1;
+    P->smem = ((size_t)v->P * v->N1 + (size_t)groups * buf) * sizeof(float2);
+    std::vector<float2> tw2 = regfft_twiddles(v->N1, v->P);
+    cudaError_t e = regfft_upload_tables();
+    if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, P->k, threads, P->smem);
+    if (e != cudaSuccess || per_sm < 1) {
+        *status = cdlgb_seterr(c, CDLGB_ECUDA, "D-step transform setup failed: %s",
+                               e != cudaSuccess ? cudaGetErrorString(e) : "no CTA fits");
+        if (P->tw2) cudaFree(P->tw2);
+        delete P;
+        return nullptr;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    P->grid = per_sm * sms;
+    return P;
+}
+
+void dfwd_plan_free(void* p) {
+    FwdPlan* P = (FwdPlan*)p;
+    if (!P) return;
+    if (P->tw2) cudaFree(P->tw2);
+    delete P;
+}
+
+// Y3-hat, H-hat and d-hat of sequences [n0, n0 + cn) into Yh, Hh, Dh (chunk layout).
+int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh) {
+    FwdPlan* P = (FwdPlan*)p;
+    const size_t off = (size_t)n0 * c->M * c->Lg;
+    FArgs a;
+    a.X = X + off; a.y3 = c->y3 + off; a.g1 = c->g1 + off; a.g3 = c->g3 + off; a.d = c->d + off;
+    a.G1 = c->G1; a.G3 = c->G3; a.Yh = Yh; a.Hh = Hh; a.Dh = Dh; a.tw2 = P->tw2;
+    a.cn = cn; a.M = c->M;
+    P->k<<<P->grid, 256, P->smem, c->stream>>>(a);
+    LAUNCH_CHECK(c, "k_dfwd");
+    return CDLGB_OK;
+}

@@ -56,6 +56,7 @@ struct FusedPlan {
     void* warp;             // register-FFT variant (xwarp.cu) when Lg has one
     void* iter;             // multi-iteration register-FFT variant (xiter.cu)
     void* dplan;            // fused D-step (dfused.cu)
+    void* dfwd;             // streaming forward transforms of the D-step (dstream.cu)
 };
 
 struct XArgs {
@@ -559,6 +560,8 @@ int fused_setup(cdlgb_ctx* c) {
         int st = CDLGB_OK;
         P->dplan = dfused_plan_create(c, &st);
         if (st != CDLGB_OK) return st;
+        P->dfwd = dfwd_plan_create(c, &st);
+        if (st != CDLGB_OK) return st;
         P->iter = iter_plan_create(c, &st);
         if (st != CDLGB_OK) return st;
         if (P->iter) return CDLGB_OK;
@@ -617,6 +620,7 @@ void fused_free(cdlgb_ctx* c) {
     warp_plan_free(P->warp);
     iter_plan_free(P->iter);
     dfused_plan_free(P->dplan);
+    dfwd_plan_free(P->dfwd);
     delete P;
     c->fplan = nullptr;
 }
@@ -661,6 +665,11 @@ int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs) {
     LAUNCH_CHECK(c, "k_xstep_fused");
     cdlgb_phase_end(c, PH_XFUSED);
     return CDLGB_OK;
+}
+
+void* fused_dfwd(cdlgb_ctx* c) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    return P ? P->dfwd : nullptr;
 }
 
 int fused_has_dstep(cdlgb_ctx* c) {

@@ -214,11 +214,12 @@ def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, m
 
 
 @pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12)])
-def test_fused_dstep_against_oracle_and_cufft(pkg, built_lib, shape, monkeypatch):
-    """One D-step through the fused kernel (register FFTs, cluster sums) and through the
-    cuFFT D-step from the same state, both against the FP64 oracle: every field the
-    D-step writes is within the parity tolerance, and the fused kernel's error is within
-    twice the cuFFT path's (Lg = 928 and 496)."""
+def test_dstep_variants_against_oracle(pkg, built_lib, shape, monkeypatch):
+    """One D-step from the same state through each D-step implementation -- the default
+    (streaming register-FFT forward transforms + cuFFT inverse), the all-cuFFT one, and
+    the opt-in fused kernel -- against the FP64 oracle: every field the D-step writes is
+    within the parity tolerance, and within twice the all-cuFFT path's error
+    (Lg = 928 and 496)."""
     N, L, M, fs = shape
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(13, N, L, [8, 12], [0.4, 0.4])
@@ -231,18 +232,22 @@ def test_fused_dstep_against_oracle_and_cufft(pkg, built_lib, shape, monkeypatch
     O.update_best(ref)
     O.dict_update(ref, 1)
     fields = ("d", "g1", "g3", "G1", "G3", "G2", "g2", "Td")
-    out = {}
-    for fusedd in ("1", "0"):
-        monkeypatch.setenv("CDLGB_DFUSED", fusedd)
+    envs = {"stream": {"CDLGB_DSTREAM": "1", "CDLGB_DFUSED": "0"},
+            "cufft": {"CDLGB_DSTREAM": "0", "CDLGB_DFUSED": "0"},
+            "fused": {"CDLGB_DSTREAM": "1", "CDLGB_DFUSED": "1"}}
+    err = {}
+    for name, env in envs.items():
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
         with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
             pkg.code_update(c, 15)
             pkg.update_best(c)
             pkg.dict_update(c, 1)
-            out[fusedd] = {f: c.get(f) for f in fields}
-    for f in fields:
-        ef = rel(out["1"][f], getattr(ref, f))
-        ec = rel(out["0"][f], getattr(ref, f))
-        assert ef < TOL_X and ef < 2.0 * ec + 1e-6, (f, ef, ec)
+            err[name] = {f: rel(c.get(f), getattr(ref, f)) for f in fields}
+    for name in ("stream", "fused"):
+        for f in fields:
+            e, ec = err[name][f], err["cufft"][f]
+            assert e < TOL_X and e < 2.0 * ec + 1e-6, (name, f, e, ec)
 
 
 @pytest.mark.parametrize("mode", MODES)

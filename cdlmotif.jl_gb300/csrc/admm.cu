@@ -782,7 +782,11 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                     c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F, c->sVh + (size_t)n0 * F, F, M, nfb,
                     c->p.sherman_const_cdl, 1.f / (float)Lg);
                 LAUNCH_CHECK(c, "k_dsolve");
-                ST_TRY(c2r(c, (long long)M * cn, c->sBh, c->d + off));
+                if (void* fw = c->fused ? fused_dfwd(c) : nullptr) {
+                    ST_TRY(dinv_run(c, fw, c->sBh, n0, cn));
+                } else {
+                    ST_TRY(c2r(c, (long long)M * cn, c->sBh, c->d + off));
+                }
             }
             ST_TRY(c2r(c, N, c->sVh, c->Td));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,

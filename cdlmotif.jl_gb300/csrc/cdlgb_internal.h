@@ -171,6 +171,7 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status);
 void dfwd_plan_free(void* p);
 int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh);
 void* fused_dfwd(cdlgb_ctx* c);
+int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn);
 int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 
 // ---- scan.cu ----

@@ -1,5 +1,6 @@
-// Forward half of the D-step (dict_update!, src/CDL/train.jl:52-57) as one streaming
-// kernel for the transform lengths with register-resident FFTs (regfft.cuh).
+// The D-step's transforms (dict_update!, src/CDL/train.jl:52-62) as streaming kernels
+// for the transform lengths with register-resident FFTs (regfft.cuh): k_dfwd (below)
+// and the inverse k_dinv (further down, d = irfft(d-hat) per filter pair).
 //
 // For every (sequence n, filter pair a = 2s, b = 2s + 1) a lane group forms, straight
 // from the state arrays, the three packed real pairs the D-step transforms --
@@ -109,18 +110,88 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
     }
 }
 
+// Inverse: for every (n, filter pair) the two half-spectra dh[a], dh[b] (already scaled
+// by 1/Lg) are packed into one full spectrum Z = Dh_a + i Dh_b (Z[f], and Z[Lg - f] =
+// conj(Dh_a[f]) + i conj(Dh_b[f])), inverted with the register four-step FFT, and
+// d[a] = Re, d[b] = Im written (as a C2R per filter, the imaginary parts of the
+// half-spectrum's f = 0 and f = Lg/2 bins are dropped).
+struct IArgsD {
+    const float2* Dh;     // chunk (cn, M, F)
+    float* d;             // chunk (cn, M, Lg)
+    const float2* tw2;
+    int cn, M;
+};
+
+template <int N1, int P>
+__global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
+    constexpr int Lg = N1 * P;
+    constexpr int G = 32 / N1;
+    constexpr int RS = N1 + 1;
+    constexpr int BUF = (P * RS + 1) & ~1;
+    constexpr int F = Lg / 2 + 1;
+    constexpr int half = Lg / 2;
+    extern __shared__ float4 smem4[];
+    float2* tw2 = reinterpret_cast<float2*>(smem4);
+    float2* bufs = tw2 + P * N1;
+    for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int gw = (threadIdx.x >> 5) * G + lane / N1;
+    const int gl = lane % N1;
+    const int groups = (blockDim.x >> 5) * G;
+    float2* sb = bufs + (size_t)gw * BUF;
+    const int pairs = A.M / 2;
+    const long items = (long)A.cn * pairs;
+    const long stride = (long)gridDim.x * groups;
+    const long rounds = (items + stride - 1) / stride;
+    for (long r = 0; r < rounds; ++r) {
+        const long item = r * stride + (long)blockIdx.x * groups + gw;
+        const bool act = item < items;
+        const long n = act ? item / pairs : 0;
+        const int s = act ? (int)(item - n * pairs) : 0;
+        const size_t ia = ((size_t)n * A.M + 2 * s) * F;
+        if (act) {
+            for (int f = gl; f < F; f += N1) {
+                const float2 a = A.Dh[ia + f], b = A.Dh[ia + F + f];
+                if (f == 0 || f == half) {
+                    sb[f] = f2(a.x, b.x);
+                } else {
+                    sb[f] = f2(a.x - b.y, a.y + b.x);
+                    sb[Lg - f] = f2(a.x + b.y, b.x - a.y);
+                }
+            }
+        }
+        __syncwarp();
+        inv_step2<N1, P, false>(sb, gl, act, tw2);
+        if (act) {
+            inv_step1<N1, P, true>(sb, gl, tw2);
+            const size_t ra = ((size_t)n * A.M + 2 * s) * Lg + gl;
+#pragma unroll 4
+            for (int n2 = 0; n2 < P; ++n2) {
+                const float2 v = sb[n2 * RS + gl];
+                A.d[ra + N1 * n2] = v.x;
+                A.d[ra + Lg + N1 * n2] = v.y;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 typedef void (*kern_t)(FArgs);
-struct Variant { int N1, P; kern_t k; };
+typedef void (*kinv_t)(IArgsD);
+struct Variant { int N1, P; kern_t k; kinv_t ki; };
 const Variant kVariants[] = {
-    {32, 29, k_dfwd<32, 29>},
-    {16, 31, k_dfwd<16, 31>},
+    {32, 29, k_dfwd<32, 29>, k_dinv<32, 29>},
+    {16, 31, k_dfwd<16, 31>, k_dinv<16, 31>},
 };
 
 struct FwdPlan {
     kern_t k;
+    kinv_t ki;
     int N1, P;
     size_t smem;
-    int grid;
+    int grid, grid_inv;
     float2* tw2;
 };
 
@@ -137,7 +208,7 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
         if (cand.N1 * cand.P == c->Lg) v = &cand;
     if (!v) return nullptr;
     FwdPlan* P = new FwdPlan();
-    P->k = v->k; P->N1 = v->N1; P->P = v->P;
+    P->k = v->k; P->ki = v->ki; P->N1 = v->N1; P->P = v->P;
     const int threads = 256, groups = (threads / 32) * (32 / v->N1);
     const size_t buf = ((size_t)v->P * (v->N1 + 1) + 1) & ~(size_t)1;
     P->smem = ((size_t)v->P * v->N1 + (size_t)groups * buf) * sizeof(float2);
@@ -146,9 +217,11 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->ki, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    int per_sm = 0, per_sm_inv = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, P->k, threads, P->smem);
-    if (e != cudaSuccess || per_sm < 1) {
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_inv, P->ki, threads, P->smem);
+    if (e != cudaSuccess || per_sm < 1 || per_sm_inv < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "D-step transform setup failed: %s",
                                e != cudaSuccess ? cudaGetErrorString(e) : "no CTA fits");
         if (P->tw2) cudaFree(P->tw2);
@@ -159,6 +232,7 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     P->grid = per_sm * sms;
+    P->grid_inv = per_sm_inv * sms;
     return P;
 }
 
@@ -179,5 +253,15 @@ int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, 
     a.cn = cn; a.M = c->M;
     P->k<<<P->grid, 256, P->smem, c->stream>>>(a);
     LAUNCH_CHECK(c, "k_dfwd");
+    return CDLGB_OK;
+}
+
+// d of sequences [n0, n0 + cn) from the half-spectra Dh (chunk layout), as C2R would.
+int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn) {
+    FwdPlan* P = (FwdPlan*)p;
+    IArgsD a;
+    a.Dh = Dh; a.d = c->d + (size_t)n0 * c->M * c->Lg; a.tw2 = P->tw2; a.cn = cn; a.M = c->M;
+    P->ki<<<P->grid_inv, 256, P->smem, c->stream>>>(a);
+    LAUNCH_CHECK(c, "k_dinv");
     return CDLGB_OK;
 }

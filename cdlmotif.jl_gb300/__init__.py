@@ -45,7 +45,8 @@ __all__ = ["CDLSetup", "CDL", "CDLGBError", "init_cdl", "code_update", "dict_upd
            "update_best", "objective", "cdl_train", "scan_w_gpu", "overlapping_scan",
            "posdicts2pfms", "count_matrices", "pfm2pwm", "pwm_complement",
            "save_pfms_as_transfac", "transfac_text", "FIELDS", "build", "ActivationRecord",
-           "non_overlap_scan", "get_thresh",
+           "non_overlap_scan", "get_thresh", "extension", "extend", "trim_pfms", "masked_trim",
+           "scores_reevaluation",
            "record_training_result", "get_spatial_info", "get_pair_pfms", "select_pairs"]
 
 FIELDS = {"X": 0, "X_best": 1, "d": 2, "D_best": 3, "G1": 4, "G3": 5, "DX": 6, "Y1": 7,
@@ -426,6 +427,132 @@ def posdicts2pfms(c: CDL, positions: np.ndarray, lens, use_comp=None, pseudocoun
     if st != 0:
         raise CDLGBError(st, "counts_to_pfms")
     return [out[k, : lens[k], :].T.copy() for k in range(K)]
+
+
+_BG = (0.25, 0.25, 0.25, 0.25)
+
+
+def extension(c: CDL, positions, lens, use_comp=None, bg=_BG, pseudocount=5.0,
+              perc_no_less_than=0.95, ic_extension_thresh=0.075):
+    """extension! (src/SEARCH/extend.jl:31-81 without use_comp, :122-173 with it) for
+    every motif at once on the GPU.  positions (N, K) 1-based, 0 = none; use_comp (N, K)
+    or None.  Returns (positions, lens, dec, inc): the new starts (0 for sequences
+    dropped by the extension), the new lengths and the columns added on each side."""
+    pos = np.array(positions, np.int32, copy=True, order="C")
+    ln = np.array(lens, np.int32, copy=True)
+    K = len(ln)
+    if pos.shape != (c.N, K):
+        raise ValueError("positions must be (N, K)")
+    uc = None if use_comp is None else np.ascontiguousarray(use_comp, np.uint8)
+    bgv = np.ascontiguousarray(bg, np.float32)
+    dec = np.zeros(K, np.int32)
+    inc = np.zeros(K, np.int32)
+    _check(c._h, _lib.lib().cdlgb_extend_positions(
+        c._h, ptr(pos, C.c_int32), ptr(uc, C.c_uint8), ptr(ln, C.c_int32), K, ptr(bgv, C.c_float),
+        float(pseudocount), float(perc_no_less_than), float(ic_extension_thresh),
+        ptr(dec, C.c_int32), ptr(inc, C.c_int32)))
+    return pos, ln, dec, inc
+
+
+def extend(c: CDL, positions, lens, filter_size: int, use_comp=None, bg=_BG, pseudocount=5.0,
+           perc_no_less_than=0.95, ic_extension_thresh=0.075, pseudocounts_r=0.0295,
+           smoothing=True, re_evaluate_pfm=True) -> dict:
+    """extend! (src/SEARCH/extend.jl:175-211): extension of every motif, then the motifs
+    with no positions left or a length <= filter_size + 2 are dropped, then (with
+    re_evaluate_pfm, the reference's default) the PFMs are re-evaluated from the new
+    positions by posdicts2pfms.  Returns {"positions" (N, K'), "lens", "use_comp",
+    "pfms" (list or None), "keep" (bool (K,))}."""
+    pos, ln, _, _ = extension(c, positions, lens, use_comp, bg, pseudocount, perc_no_less_than,
+                              ic_extension_thresh)
+    keep = ((pos > 0).sum(axis=0) > 0) & (ln > filter_size + 2)
+    pos = np.ascontiguousarray(pos[:, keep])
+    ln = ln[keep]
+    uc = None if use_comp is None else np.ascontiguousarray(np.asarray(use_comp)[:, keep])
+    pfms = None
+    if re_evaluate_pfm:
+        pfms = posdicts2pfms(c, pos, ln, uc, pseudocounts_r, pseudocount, smoothing) if len(ln) else []
+    return {"positions": pos, "lens": ln, "use_comp": uc, "pfms": pfms, "keep": keep}
+
+
+def trim_pfms(pfms, bg=_BG, mask_len=(8, 4, 2, 1), mask_thresh=(0.625, 0.525, 0.345, 0.2)):
+    """trim_this_pfm_by_masking! (src/SEARCH/trim.jl:1-36) for a list of (4, w) PFMs,
+    in the library's host code.  Returns (front, back) int32 arrays: the columns to
+    trim at each end."""
+    K = len(pfms)
+    lens = np.array([np.asarray(p).shape[1] for p in pfms], np.int32)
+    maxlen = max(1, int(lens.max()) if K else 1)
+    arr = np.zeros((K, maxlen, 4), np.float32)
+    for k, p in enumerate(pfms):
+        arr[k, : lens[k], :] = np.asarray(p, np.float32).T
+    bgv = np.ascontiguousarray(bg, np.float32)
+    ml = np.ascontiguousarray(mask_len, np.int32)
+    mt = np.ascontiguousarray(mask_thresh, np.float32)
+    front = np.zeros(K, np.int32)
+    back = np.zeros(K, np.int32)
+    if K == 0:
+        return front, back
+    st = _lib.lib().cdlgb_trim_pfms(ptr(arr, C.c_float), ptr(lens, C.c_int32), K, maxlen,
+                                    ptr(bgv, C.c_float), ptr(ml, C.c_int32), ptr(mt, C.c_float),
+                                    len(ml), ptr(front, C.c_int32), ptr(back, C.c_int32))
+    if st != 0:
+        raise CDLGBError(st, "trim_pfms")
+    return front, back
+
+
+def masked_trim(pfms, filter_size: int, positions=None, use_comp=None, bg=_BG,
+                mask_len=(8, 4, 2, 1), mask_thresh=(0.625, 0.525, 0.345, 0.2),
+                after_merged=False, update_positions=True, c: CDL | None = None,
+                pval_thresh=2.7e-4) -> dict:
+    """masked_trim! (src/SEARCH/trim.jl:38-77): every PFM trimmed by masking, every
+    position moved by the columns trimmed at the front (at the back for
+    reverse-complemented entries when after_merged), then the motifs of length
+    <= filter_size + 1 or without positions dropped.  With a context ``c`` the
+    re-evaluation that follows in the reference (pwms = pfm2pwm, thresh = get_thresh at
+    pval_thresh) is done too.  use_comp is returned unfiltered, as the reference leaves
+    it (trim.jl:71-74).  Returns {"pfms", "lens", "positions", "keep", "front", "back",
+    "pwms", "thresh"}."""
+    front, back = trim_pfms(pfms, bg, mask_len, mask_thresh)
+    new = [np.asarray(p, np.float32)[:, f: np.asarray(p).shape[1] - b]
+           if f + b < np.asarray(p).shape[1] else np.zeros((4, 0), np.float32)
+           for p, f, b in zip(pfms, front, back)]
+    pos = None
+    if positions is not None:
+        pos = np.array(positions, np.int32, copy=True)
+        for k in range(len(new)):
+            on = pos[:, k] > 0
+            shift = np.full(pos.shape[0], front[k], np.int32)
+            if after_merged and use_comp is not None:
+                shift = np.where(np.asarray(use_comp)[:, k] != 0, back[k], front[k]).astype(np.int32)
+            pos[on, k] += shift[on]
+    keep = np.array([p.shape[1] > filter_size + 1 for p in new], bool)
+    if pos is not None:
+        keep &= (pos > 0).sum(axis=0) > 0
+    new = [p for p, kk in zip(new, keep) if kk]
+    lens = np.array([p.shape[1] for p in new], np.int32)
+    out = {"pfms": new, "lens": lens, "keep": keep, "front": front, "back": back,
+           "positions": (np.ascontiguousarray(pos[:, keep]) if (pos is not None and update_positions)
+                         else None),
+           "use_comp": use_comp, "pwms": None, "thresh": None}
+    if c is not None and len(new):
+        pwms = [pfm2pwm(p, bg) for p in new]
+        out["pwms"] = pwms
+        out["thresh"] = get_thresh(c, pwms, pval_thresh)
+    return out
+
+
+def scores_reevaluation(c: CDL, pwms, positions, lens=None) -> np.ndarray:
+    """scores_reevaluation (src/SEARCH/helpers.jl:151-172) on the GPU: the Float32 score
+    of every entry's forward window.  pwms: list of (4, w); positions (N, K).
+    Returns scores (N, K), 0 where there is no entry."""
+    arr, ln, maxlen = _pack_pwms(pwms, lens)
+    K = len(ln)
+    pos = np.ascontiguousarray(positions, np.int32)
+    if pos.shape != (c.N, K):
+        raise ValueError("positions must be (N, K)")
+    out = np.zeros((c.N, K), np.float32)
+    _check(c._h, _lib.lib().cdlgb_rescore_positions(c._h, ptr(arr, C.c_float), ptr(pos, C.c_int32),
+                                                    ptr(ln, C.c_int32), K, maxlen, ptr(out, C.c_float)))
+    return out
 
 
 # ---------------------------------------------------------------------------- code -> counts

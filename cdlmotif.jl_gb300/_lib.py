@@ -59,6 +59,11 @@ SIGNATURES = {
     "cdlgb_count_pfms": (C.c_int, [_vp, _i32p, _u8p, _i32p, C.c_int32, C.c_int32, _i32p, _i32p]),
     "cdlgb_counts_to_pfms": (C.c_int, [_i32p, _i32p, _i32p, C.c_int32, C.c_int32, C.c_float,
                                        C.c_float, C.c_int32, C.c_int32, _f32p]),
+    "cdlgb_extend_positions": (C.c_int, [_vp, _i32p, _u8p, _i32p, C.c_int32, _f32p, C.c_float,
+                                         C.c_float, C.c_float, _i32p, _i32p]),
+    "cdlgb_rescore_positions": (C.c_int, [_vp, _f32p, _i32p, _i32p, C.c_int32, C.c_int32, _f32p]),
+    "cdlgb_trim_pfms": (C.c_int, [_f32p, _i32p, C.c_int32, C.c_int32, _f32p, _i32p, _f32p,
+                                  C.c_int32, _i32p, _i32p]),
     "cdlgb_transfac_format": (C.c_int64, [_f32p, C.c_int32, C.c_int32, C.c_char_p, C.c_size_t]),
     "cdlgb_set_stream": (C.c_int, [_vp, _vp]),
     "cdlgb_profile": (C.c_int, [_vp, C.c_int32]),

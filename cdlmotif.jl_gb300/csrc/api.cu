@@ -519,6 +519,20 @@ int cdlgb_count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp,
     return count_pfms(c, pos, use_comp, lens, K, maxlen, counts_out, nseq_out);
 }
 
+int cdlgb_extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_t* lens,
+                           int32_t K, const float* bg, float pseudocount, float perc_no_less_than,
+                           float ic_extension_thresh, int32_t* dec_out, int32_t* inc_out) {
+    NEED_LOADED(c);
+    return extend_positions(c, pos, use_comp, lens, K, bg, pseudocount, perc_no_less_than,
+                            ic_extension_thresh, dec_out, inc_out);
+}
+
+int cdlgb_rescore_positions(cdlgb_ctx* c, const float* pwms, const int32_t* pos,
+                            const int32_t* lens, int32_t K, int32_t maxlen, float* score_out) {
+    NEED_LOADED(c);
+    return rescore_positions(c, pwms, pos, lens, K, maxlen, score_out);
+}
+
 // ------------------------------------------------------------------ instrumentation
 int cdlgb_set_stream(cdlgb_ctx* c, void* stream) {
     if (!c) return CDLGB_EINVAL;

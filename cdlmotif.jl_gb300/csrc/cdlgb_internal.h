@@ -186,6 +186,12 @@ int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_com
 int touzet_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int K, int maxlen,
                       double pval, float* thresh_out);
 void scan_free(cdlgb_ctx* c);
+// ---- refine.cu ----
+int extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_t* lens, int K,
+                     const float* bg, float pseudocount, float perc_no_less_than,
+                     float ic_extension_thresh, int32_t* dec_out, int32_t* inc_out);
+int rescore_positions(cdlgb_ctx* c, const float* pwms, const int32_t* pos, const int32_t* lens,
+                      int K, int maxlen, float* score_out);
 
 static inline unsigned grid_for(size_t n, int block, unsigned cap = 152u * 32u) {
     size_t g = (n + block - 1) / block;

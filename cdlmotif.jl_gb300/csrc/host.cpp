@@ -7,7 +7,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
+#include <vector>
 
 #include "cdlgb.h"
 
@@ -133,6 +135,76 @@ int64_t cdlgb_transfac_format(const float* pfm, int32_t w, int32_t reverse_compl
         out[n] = 0;
     }
     return (int64_t)s.size();
+}
+
+namespace {
+// median of a Float32 window as the reference's median computes it: NaN if any entry is
+// NaN, else the middle of the sorted values, middle(a, b) = a/2 + b/2 for an even count
+float median_f32(std::vector<float> v) {
+    for (float x : v)
+        if (x != x) return x;
+    std::sort(v.begin(), v.end());
+    const size_t n = v.size();
+    if (n & 1) return v[n / 2];
+    volatile float a = v[n / 2 - 1] / 2.f;
+    volatile float b = v[n / 2] / 2.f;
+    return a + b;
+}
+}  // namespace
+
+int cdlgb_trim_pfms(const float* pfms, const int32_t* lens, int32_t K, int32_t maxlen,
+                    const float* bg, const int32_t* mask_len, const float* mask_thresh,
+                    int32_t nmask, int32_t* front_out, int32_t* back_out) {
+    if (!pfms || !lens || !bg || !front_out || !back_out || K <= 0 || maxlen <= 0 || nmask < 0 ||
+        (nmask > 0 && (!mask_len || !mask_thresh)))
+        return CDLGB_EINVAL;
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        if (w < 0 || w > maxlen) return CDLGB_EINVAL;
+        // get_ic_col_multiple (helpers.jl:135-138): per column, in Float32,
+        // ((s1 + s2) + s3) + s4 with s_a = p * log2(p / bg[a]) (log2 rounded from double)
+        std::vector<float> ic((size_t)w);
+        for (int j = 0; j < w; ++j) {
+            volatile float acc = 0.f;
+            for (int a = 0; a < 4; ++a) {
+                volatile float p = pfms[(size_t)a + 4 * ((size_t)j + (size_t)maxlen * k)];
+                volatile float q = p / bg[a];
+                volatile float lg = (float)log2((double)q);
+                volatile float t = p * lg;
+                acc = acc + t;
+            }
+            ic[j] = acc;
+        }
+        // trim_this_pfm_by_masking! (trim.jl:1-36): for each mask, mark window starts
+        // from the front while the window's median IC is below the mask threshold, and
+        // window ends from the back likewise; already marked columns are skipped.
+        std::vector<char> trim((size_t)w, 0);
+        for (int m = 0; m < nmask; ++m) {
+            const int ml = mask_len[m];
+            const float mt = mask_thresh[m];
+            if (ml < 1) return CDLGB_EINVAL;
+            for (int i = 0; i + ml <= w; ++i) {
+                if (trim[i]) continue;
+                if (median_f32(std::vector<float>(ic.begin() + i, ic.begin() + i + ml)) < mt)
+                    trim[i] = 1;
+                else
+                    break;
+            }
+            for (int j = w - 1; j >= ml - 1; --j) {
+                if (trim[j]) continue;
+                if (median_f32(std::vector<float>(ic.begin() + (j - ml + 1), ic.begin() + j + 1)) < mt)
+                    trim[j] = 1;
+                else
+                    break;
+            }
+        }
+        int front = 0, back = 0;
+        for (int j = 0; j < w && trim[j]; ++j) ++front;
+        for (int j = w - 1; j >= 0 && trim[j]; --j) ++back;
+        front_out[k] = front;
+        back_out[k] = back;
+    }
+    return CDLGB_OK;
 }
 
 }  // extern "C"

@@ -223,6 +223,39 @@ int cdlgb_counts_to_pfms(const int32_t* counts, const int32_t* nseq, const int32
                          float pseudo_count, int32_t smoothing, int32_t less_pseudocount,
                          float* pfm_out);
 
+/* extension! of extend! (src/SEARCH/extend.jl:31-81 without use_comp, 122-173 with it)
+ * for K motifs at once: starting from each motif's positions, add a column on the left
+ * and one on the right while the column's information content (its one-hot counts over
+ * the motif's sequences plus `pseudocount`, against bg[4]) stays above
+ * ic_extension_thresh; a sequence whose new column would leave 1..L is dropped when
+ * that column is accepted.  pos: (K, N) col-major, 1-based, 0 = no entry, updated in
+ * place (dropped entries become 0, the rest move to the new start); use_comp (K, N) or
+ * NULL (the variant without complements); lens: K, updated in place (+ columns added).
+ * dec_out / inc_out (K, may be NULL): columns added on the left / right.  Errors:
+ * CDLGB_EINVAL where the reference would not return (a motif whose empty column keeps
+ * scoring above the threshold) or would raise (a reverse-complemented column that is not
+ * one-hot). */
+int cdlgb_extend_positions(cdlgb_ctx* ctx, int32_t* pos, const uint8_t* use_comp, int32_t* lens,
+                           int32_t K, const float* bg, float pseudocount, float perc_no_less_than,
+                           float ic_extension_thresh, int32_t* dec_out, int32_t* inc_out);
+
+/* scores_reevaluation (src/SEARCH/helpers.jl:151-172): score_out[k, n] = the Float32 sum
+ * of pwm_k .* the forward one-hot window at pos[k, n] (the reference ignores use_comp
+ * here), summed base-major, nucleotide inner; 0 where pos is 0.  pwms (K, 4, maxlen)
+ * col-major as for the scans; pos and score_out (K, N) col-major. */
+int cdlgb_rescore_positions(cdlgb_ctx* ctx, const float* pwms, const int32_t* pos,
+                            const int32_t* lens, int32_t K, int32_t maxlen, float* score_out);
+
+/* trim_this_pfm_by_masking! (src/SEARCH/trim.jl:1-36) for K pfms (4, maxlen, K) col-major
+ * of lengths lens: the per-column information content against bg[4] (Float32, as
+ * get_ic_col_multiple), then for each of the nmask masks the window starts from the
+ * front and window ends from the back whose median IC is below mask_thresh[m] are
+ * marked until the first window that is not; front_out[k] / back_out[k] = the leading /
+ * trailing marked columns (the trimmed pfm is columns front+1 .. lens-back).  Host only. */
+int cdlgb_trim_pfms(const float* pfms, const int32_t* lens, int32_t K, int32_t maxlen,
+                    const float* bg, const int32_t* mask_len, const float* mask_thresh,
+                    int32_t nmask, int32_t* front_out, int32_t* back_out);
+
 /* One transfac file body as save_pfms_as_transfac writes it
  * (src/SAVE/save_learned_results.jl:186-196): pfm (4, w) col-major, values printed
  * as pfm*1000 in Julia's shortest Float32 form.  reverse_complement != 0 writes the

@@ -266,6 +266,215 @@ def counts_to_pfms(counts, nseq, lens, pseudocounts_r=0.0295, pseudo_count=5.0,
     return pfms
 
 
+# ----------------------------------------------------------------------------------
+# (f) motif refinement: extend! / masked_trim! / scores_reevaluation
+# ----------------------------------------------------------------------------------
+def _log2_f32(q) -> np.float32:
+    """Float32 log2 correctly rounded: evaluated in float64 and rounded (the reference's
+    Float32 log2 evaluates in Float64 and rounds too)."""
+    return f32(np.log2(np.float64(q)))
+
+
+def ic_col_single(col, bg) -> np.float32:
+    """get_ic_col_single (src/SEARCH/helpers.jl:127-133): s += p[i] * log2(p[i] / bg[i])
+    in Float32, i = 1..4 in order."""
+    s = f32(0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for i in range(4):
+            p = f32(col[i])
+            s = f32(s + f32(p * _log2_f32(f32(p / f32(bg[i])))))
+    return s
+
+
+_DUMMY_COMP = {(1, 0, 0, 0): (0, 0, 0, 1), (0, 1, 0, 0): (0, 0, 1, 0),
+               (0, 0, 1, 0): (0, 1, 0, 0), (0, 0, 0, 1): (1, 0, 0, 0)}
+
+
+def _dummy_comp(v):
+    """dummy_comp (src/SEARCH/helpers.jl:18-41): a Dict lookup, so anything but one of
+    the four one-hot vectors raises KeyError."""
+    return np.array(_DUMMY_COMP[tuple(int(x) if float(x) in (0.0, 1.0) else x for x in v)], f32)
+
+
+def extension(data: np.ndarray, pos_col, mlen: int, comp_col, bg=(0.25,) * 4, pseudocount=5.0,
+              perc_no_less_than=0.95, ic_extension_thresh=0.075):
+    """extension! for one motif (src/SEARCH/extend.jl:31-81 when comp_col is None,
+    :122-173 otherwise), restated statement by statement with its per-sequence
+    `included` flags.  data (N, 4L) one-hot; pos_col (N,) 1-based positions, 0 = not a
+    key; comp_col (N,) use_comp flags or None.  Returns (new pos_col, new length,
+    dec, inc).  The reference's num_included is decremented only inside
+    explore_sides! (a local copy), so the usage bound of :74 / :165 compares the
+    unchanged entry count.  Raises RuntimeError after 2L + 4 rounds (the reference
+    does not return then) and KeyError where dummy_comp does."""
+    N, L4 = data.shape
+    L = L4 // 4
+    keys = [n for n in range(N) if pos_col[n] != 0]
+    P = {n: int(pos_col[n]) for n in keys}
+    C = None if comp_col is None else {n: bool(comp_col[n]) for n in keys}
+    ps = f32(pseudocount)
+    thr = f32(ic_extension_thresh)
+    len_pos = len(keys)
+    dec = inc = 0
+    included = [True] * len_pos
+    num_included = len_pos
+    usage_lowerbdd = int(np.floor(f32(f32(perc_no_less_than) * f32(len_pos))))
+    explore_left = explore_right = True
+    len_inc = 0
+
+    def explore_sides(offset, right):
+        this_col = np.zeros(4, f32)
+        inc_right = mlen - 1 + offset
+        to_exclude = []
+        for ind, k in enumerate(keys):
+            if not included[ind]:
+                continue
+            if C is None:
+                pos = P[k] + inc_right if right else P[k] - offset
+            else:
+                pos = P[k] + inc_right if ((right and not C[k]) or (not right and C[k])) else P[k] - offset
+            if pos < 1 or pos > L:
+                to_exclude.append(ind)
+                continue
+            dat = data[k, 4 * (pos - 1):4 * pos].astype(f32)
+            if C is not None and C[k]:
+                dat = _dummy_comp(dat)
+            this_col = (this_col + dat).astype(f32)
+        tot = f32(f32(f32(this_col[0] + this_col[1]) + this_col[2]) + this_col[3])
+        col = ((this_col + ps).astype(f32) / f32(tot + f32(f32(4) * ps))).astype(f32)
+        return ic_col_single(col, bg), to_exclude
+
+    rounds = 0
+    while True:
+        rounds += 1
+        if rounds > 2 * L + 4:
+            raise RuntimeError("extension does not terminate")
+        if explore_left:
+            ic, ex = explore_sides(dec + 1, False)
+            if ic <= thr:
+                explore_left = False
+            else:
+                for i in ex:
+                    included[i] = False
+                len_inc += 1
+                dec += 1
+        if explore_right:
+            ic, ex = explore_sides(inc + 1, True)
+            if ic <= thr:
+                explore_right = False
+            else:
+                for i in ex:
+                    included[i] = False
+                len_inc += 1
+                inc += 1
+        if not explore_left and not explore_right:
+            break
+        if num_included <= usage_lowerbdd:
+            break
+    out = np.array(pos_col, np.int32, copy=True)
+    if dec > 0 or inc > 0:
+        out[:] = 0
+        for ind, k in enumerate(keys):
+            if included[ind]:
+                out[k] = P[k] - inc if (C is not None and C[k]) else P[k] - dec
+    return out, mlen + len_inc, dec, inc
+
+
+def extend_positions(data, pos, use_comp, lens, bg=(0.25,) * 4, pseudocount=5.0,
+                     perc_no_less_than=0.95, ic_extension_thresh=0.075):
+    """extension! for every motif (the loop of extend!, src/SEARCH/extend.jl:180-196).
+    pos, use_comp (N, K) == Julia (K, N).  Returns (pos, lens, dec, inc)."""
+    pos = np.array(pos, np.int32, copy=True)
+    K = pos.shape[1]
+    lens_out = np.array(lens, np.int32, copy=True)
+    dec = np.zeros(K, np.int32)
+    inc = np.zeros(K, np.int32)
+    for k in range(K):
+        cc = None if use_comp is None else use_comp[:, k]
+        pos[:, k], lens_out[k], dec[k], inc[k] = extension(
+            data, pos[:, k], int(lens[k]), cc, bg, pseudocount, perc_no_less_than,
+            ic_extension_thresh)
+    return pos, lens_out, dec, inc
+
+
+def _median_f32(v):
+    """median of a Float32 vector: NaN if any, else the middle value, or
+    middle(a, b) = a/2 + b/2 of the two middle values."""
+    v = np.asarray(v, f32)
+    if np.any(np.isnan(v)):
+        return f32(np.nan)
+    v = np.sort(v)
+    n = len(v)
+    if n % 2:
+        return v[n // 2]
+    return f32(f32(v[n // 2 - 1] / f32(2)) + f32(v[n // 2] / f32(2)))
+
+
+def ic_cols(pfm, bg=(0.25,) * 4) -> np.ndarray:
+    """get_ic_col_multiple (src/SEARCH/helpers.jl:135-138): per column
+    ((s1 + s2) + s3) + s4, s_a = p * log2(p / bg[a]) in Float32."""
+    pfm = np.asarray(pfm, f32)
+    return np.array([ic_col_single(pfm[:, j], bg) for j in range(pfm.shape[1])], f32)
+
+
+def trim_pfm_by_masking(pfm, bg=(0.25,) * 4, mask_len=(8, 4, 2, 1),
+                        mask_thresh=(0.625, 0.525, 0.345, 0.2)):
+    """trim_this_pfm_by_masking! (src/SEARCH/trim.jl:1-36).  Returns (front, back)."""
+    ic = ic_cols(pfm, bg)
+    n = len(ic)
+    trim = [False] * n
+    for ml, mt in zip(mask_len, mask_thresh):
+        mt = f32(mt)
+        for i in range(0, n - ml + 1):
+            if trim[i]:
+                continue
+            if _median_f32(ic[i:i + ml]) < mt:
+                trim[i] = True
+            else:
+                break
+        for j in range(n - 1, ml - 2, -1):
+            if trim[j]:
+                continue
+            if _median_f32(ic[j - ml + 1:j + 1]) < mt:
+                trim[j] = True
+            else:
+                break
+    front = 0
+    for t in trim:
+        if not t:
+            break
+        front += 1
+    back = 0
+    for t in reversed(trim):
+        if not t:
+            break
+        back += 1
+    return front, back
+
+
+def scores_reevaluation(data, pwms, pos, lens) -> np.ndarray:
+    """scores_reevaluation (src/SEARCH/helpers.jl:151-172): per entry the sum of
+    pwm .* the forward window (use_comp is not consulted), restated in memory order
+    (base-major, nucleotide inner) with a rounded product and a rounded sum per term.
+    pwms: list of (4, w); pos (N, K).  Returns scores (N, K), 0 where pos is 0."""
+    N, L4 = data.shape
+    K = pos.shape[1]
+    out = np.zeros((N, K), f32)
+    for k in range(K):
+        w = int(lens[k])
+        pw = np.asarray(pwms[k], f32)[:, :w]
+        for n in range(N):
+            p = int(pos[n, k])
+            if p <= 0:
+                continue
+            win = data[n, 4 * (p - 1):4 * (p - 1 + w)].astype(f32)
+            s = f32(0)
+            for i in range(w):
+                for a in range(4):
+                    s = f32(s + f32(pw[a, i] * win[4 * i + a]))
+            out[n, k] = s
+    return out
+
+
 def pfm2pwm(pfm, bg=(0.25, 0.25, 0.25, 0.25)):
     """src/SEARCH/helpers.jl:12-13."""
     bgv = np.asarray(bg, dtype=np.asarray(pfm).dtype).reshape(4, 1)

@@ -46,7 +46,7 @@ __all__ = ["CDLSetup", "CDL", "CDLGBError", "init_cdl", "code_update", "dict_upd
            "posdicts2pfms", "count_matrices", "pfm2pwm", "pwm_complement",
            "save_pfms_as_transfac", "transfac_text", "FIELDS", "build", "ActivationRecord",
            "non_overlap_scan", "get_thresh", "extension", "extend", "trim_pfms", "masked_trim",
-           "scores_reevaluation",
+           "scores_reevaluation", "fisher_evalues", "filter_using_evalue",
            "record_training_result", "get_spatial_info", "get_pair_pfms", "select_pairs"]
 
 FIELDS = {"X": 0, "X_best": 1, "d": 2, "D_best": 3, "G1": 4, "G3": 5, "DX": 6, "Y1": 7,
@@ -172,6 +172,35 @@ class CDL:
         out = np.empty((self.N, self.L), np.float32)
         _check(self._h, _lib.lib().cdlgb_get(self._h, 17, out.ctypes.data_as(C.c_void_p), out.nbytes))
         return out
+
+    def make_background(self, k: int = 3, seed: int = 0):
+        """The background of the e-value filter on the device: every sequence k-let
+        shuffled (the reference runs `fasta-shuffle-letters -kmer 3`,
+        src/SETUP/LOAD_setup.jl:8)."""
+        _check(self._h, _lib.lib().cdlgb_make_background(self._h, int(k), int(seed) & (2**64 - 1)))
+
+    def background(self) -> np.ndarray:
+        """The background one-hot matrix (N, 4L) float32."""
+        out = np.empty((self.N, self.L), np.float32)      # self.L holds 4L
+        _check(self._h, _lib.lib().cdlgb_get(self._h, 18, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def select_data(self, which: int):
+        """0: scans / counts / refinement read the data; 1: they read the background."""
+        _check(self._h, _lib.lib().cdlgb_select_data(self._h, int(which)))
+
+    def on_background(self):
+        """Context manager: the scan family reads the background inside the block."""
+        import contextlib
+
+        @contextlib.contextmanager
+        def cm():
+            self.select_data(1)
+            try:
+                yield self
+            finally:
+                self.select_data(0)
+        return cm()
 
     def autotune(self) -> dict:
         """Time every fused X-step variant for this dataset's shape on a prefix of the
@@ -553,6 +582,51 @@ def scores_reevaluation(c: CDL, pwms, positions, lens=None) -> np.ndarray:
     _check(c._h, _lib.lib().cdlgb_rescore_positions(c._h, ptr(arr, C.c_float), ptr(pos, C.c_int32),
                                                     ptr(ln, C.c_int32), K, maxlen, ptr(out, C.c_float)))
     return out
+
+
+def fisher_evalues(hits, hits_bg, N: int) -> np.ndarray:
+    """filter_using_evalue!'s e-values (src/SEARCH/e_value_filter.jl:15-23):
+    K * pvalue(FisherExactTest(a, N, b, N)) per motif, in the library's host code."""
+    a = np.ascontiguousarray(hits, np.int32)
+    b = np.ascontiguousarray(hits_bg, np.int32)
+    out = np.zeros(len(a), np.float64)
+    if len(a) == 0:
+        return out
+    st = _lib.lib().cdlgb_fisher_evalues(ptr(a, C.c_int32), ptr(b, C.c_int32), len(a), int(N),
+                                         ptr(out, C.c_double))
+    if st != 0:
+        raise CDLGBError(st, "fisher_evalues")
+    return out
+
+
+def filter_using_evalue(c: CDL, pwms, thresh, positions, lens=None, cpu=False, non_overlap=False,
+                        e_value_thresh_1=0.5, e_value_thresh_2=1e-3,
+                        get_evalues_only=False):
+    """filter_using_evalue! (src/SEARCH/e_value_filter.jl:1-44) on c's background
+    (make it first with c.make_background()): the motifs are scanned on the background
+    (cpu=False: the forward GPU scan of scan_w_gpu!; cpu=True: the two-strand scan of
+    overlapping_scan_bg!, then with non_overlap the selection of
+    non_overlapping_scan_bg!), the sequences hit in the data (positions (N, K), 0 = none)
+    and in the background are compared by Fisher's exact test, and a motif passes when
+    its e-value is below the threshold (Float32 e_value_thresh_2 with cpu, else
+    e_value_thresh_1) and its length is above 5.  Returns the e-values when
+    get_evalues_only, else {"evalues", "keep", "hits", "hits_bg"}."""
+    _, ln, _ = _pack_pwms(pwms, lens)
+    with c.on_background():
+        if not cpu:
+            bg_pos = scan_w_gpu(c, pwms, thresh, ln)
+        else:
+            bg_pos, bg_sc, _ = overlapping_scan(c, pwms, thresh, ln)
+            if non_overlap:
+                bg_pos, _, _ = non_overlap_scan(c, bg_pos, bg_sc, ln, None)
+    hits = (np.asarray(positions) > 0).sum(axis=0).astype(np.int32)
+    hits_bg = (bg_pos > 0).sum(axis=0).astype(np.int32)
+    ev = fisher_evalues(hits, hits_bg, c.N)
+    if get_evalues_only:
+        return ev
+    thr = float(np.float32(e_value_thresh_2 if cpu else e_value_thresh_1))
+    keep = (ev < thr) & (ln > 5)
+    return {"evalues": ev, "keep": keep, "hits": hits, "hits_bg": hits_bg}
 
 
 # ---------------------------------------------------------------------------- code -> counts

@@ -64,6 +64,9 @@ SIGNATURES = {
     "cdlgb_rescore_positions": (C.c_int, [_vp, _f32p, _i32p, _i32p, C.c_int32, C.c_int32, _f32p]),
     "cdlgb_trim_pfms": (C.c_int, [_f32p, _i32p, C.c_int32, C.c_int32, _f32p, _i32p, _f32p,
                                   C.c_int32, _i32p, _i32p]),
+    "cdlgb_make_background": (C.c_int, [_vp, C.c_int32, C.c_uint64]),
+    "cdlgb_select_data": (C.c_int, [_vp, C.c_int32]),
+    "cdlgb_fisher_evalues": (C.c_int, [_i32p, _i32p, C.c_int32, C.c_int32, _f64p]),
     "cdlgb_transfac_format": (C.c_int64, [_f32p, C.c_int32, C.c_int32, C.c_char_p, C.c_size_t]),
     "cdlgb_set_stream": (C.c_int, [_vp, _vp]),
     "cdlgb_profile": (C.c_int, [_vp, C.c_int32]),

@@ -174,6 +174,7 @@ int cdlgb_destroy(cdlgb_ctx* c) {
     fused_free(c);
     scan_free(c);
     if (c->S) cudaFree(c->S);
+    if (c->S_bg) cudaFree(c->S_bg);
     Ring* r = (Ring*)c->ring;
     if (r) {
         for (int i = 0; i < 2 * kRing; ++i) cudaEventDestroy(r->ev[i]);
@@ -246,6 +247,7 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
     if (c->loaded && c->L4 == L4 && c->N == N) {
         // same shape as the resident dataset: keep every buffer and plan, replace the data
         c->initialized = false;
+        c->bg_valid = c->use_bg = 0;
         return upload_data(c, onehot, codes, (size_t)L4 * N);
     }
     if (c->loaded) {
@@ -253,7 +255,9 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
         admm_free(c);
         fused_free(c);
         if (c->S) cudaFree(c->S);
-        c->S = nullptr;
+        if (c->S_bg) cudaFree(c->S_bg);
+        c->S = c->S_bg = nullptr;
+        c->bg_valid = c->use_bg = 0;
         c->loaded = c->initialized = false;
     }
     const cdlgb_params& p = c->p;
@@ -433,11 +437,14 @@ int cdlgb_code_threshold(cdlgb_ctx* c, double* thresh) {
 }
 
 int cdlgb_get(cdlgb_ctx* c, int32_t field, void* dst, size_t bytes) {
-    if (field == CDLGB_FIELD_DATA) {
+    if (field == CDLGB_FIELD_DATA || field == CDLGB_FIELD_BACKGROUND) {
         NEED_LOADED(c);
         if (!dst || bytes != (size_t)c->L4 * c->N * 4)
             return cdlgb_seterr(c, CDLGB_EINVAL, "data is (4L, N) float32");
-        CU_TRY(c, cudaMemcpyAsync(dst, c->S, bytes, cudaMemcpyDeviceToHost, c->stream));
+        if (field == CDLGB_FIELD_BACKGROUND && !c->bg_valid)
+            return cdlgb_seterr(c, CDLGB_ESTATE, "no background made (cdlgb_make_background)");
+        CU_TRY(c, cudaMemcpyAsync(dst, field == CDLGB_FIELD_DATA ? c->S : c->S_bg, bytes,
+                                  cudaMemcpyDeviceToHost, c->stream));
         CU_TRY(c, cudaStreamSynchronize(c->stream));
         return CDLGB_OK;
     }
@@ -531,6 +538,20 @@ int cdlgb_rescore_positions(cdlgb_ctx* c, const float* pwms, const int32_t* pos,
                             const int32_t* lens, int32_t K, int32_t maxlen, float* score_out) {
     NEED_LOADED(c);
     return rescore_positions(c, pwms, pos, lens, K, maxlen, score_out);
+}
+
+int cdlgb_make_background(cdlgb_ctx* c, int32_t k, uint64_t seed) {
+    NEED_LOADED(c);
+    return make_background(c, k, (unsigned long long)seed);
+}
+
+int cdlgb_select_data(cdlgb_ctx* c, int32_t which) {
+    NEED_LOADED(c);
+    if (which != 0 && which != 1) return cdlgb_seterr(c, CDLGB_EINVAL, "select_data: which=%d", which);
+    if (which == 1 && !c->bg_valid)
+        return cdlgb_seterr(c, CDLGB_ESTATE, "no background made (cdlgb_make_background)");
+    c->use_bg = which;
+    return CDLGB_OK;
 }
 
 // ------------------------------------------------------------------ instrumentation

@@ -39,6 +39,10 @@ struct cdlgb_ctx {
     // one-hot data, (N, L4) == Julia (4L, N)
     float* S = nullptr;
     int onehot_exact = 0;
+    // k-let shuffled background of S (same layout) and which of the two the scan family
+    // reads (the ADMM always reads S)
+    float* S_bg = nullptr;
+    int bg_valid = 0, use_bg = 0;
 
     // LMN state
     float* Xb[2] = {nullptr, nullptr};
@@ -186,6 +190,10 @@ int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_com
 int touzet_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int K, int maxlen,
                       double pval, float* thresh_out);
 void scan_free(cdlgb_ctx* c);
+// ---- background.cu ----
+int make_background(cdlgb_ctx* c, int k, unsigned long long seed);
+// the one-hot data the scans, counts and motif refinement read
+static inline const float* scan_data(const cdlgb_ctx* c) { return c->use_bg ? c->S_bg : c->S; }
 // ---- refine.cu ----
 int extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_t* lens, int K,
                      const float* bg, float pseudocount, float perc_no_less_than,

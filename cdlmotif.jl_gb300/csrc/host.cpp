@@ -207,4 +207,34 @@ int cdlgb_trim_pfms(const float* pfms, const int32_t* lens, int32_t K, int32_t m
     return CDLGB_OK;
 }
 
+int cdlgb_fisher_evalues(const int32_t* hits, const int32_t* hits_bg, int32_t K, int32_t N,
+                         double* evalues_out) {
+    if (!hits || !hits_bg || !evalues_out || K <= 0 || N < 0) return CDLGB_EINVAL;
+    for (int i = 0; i < K; ++i) {
+        const long a = hits[i], b = hits_bg[i];
+        if (a < 0 || a > N || b < 0 || b > N) return CDLGB_EINVAL;
+        // table [a N; b N]: X ~ Hypergeometric(r1 = a + N successes, r2 = b + N failures,
+        // c1 = a + b draws), observed a; P(X = j) = C(r1, j) C(r2, c1 - j) / C(r1 + r2, c1)
+        const double r1 = (double)(a + N), r2 = (double)(b + N), c1 = (double)(a + b);
+        const long lo = (long)std::max(0.0, c1 - r2), hi = (long)std::min(c1, r1);
+        auto lp = [&](long j) {
+            return -lgamma((double)j + 1.0) - lgamma(r1 - (double)j + 1.0) -
+                   lgamma(c1 - (double)j + 1.0) - lgamma(r2 - c1 + (double)j + 1.0);
+        };
+        double mx = -INFINITY;
+        for (long j = lo; j <= hi; ++j) mx = std::max(mx, lp(j));
+        double left = 0.0, right = 0.0, total = 0.0;
+        for (long j = lo; j <= hi; ++j) {
+            const double t = exp(lp(j) - mx);
+            total += t;
+            if (j <= a) left += t;
+            if (j >= a) right += t;
+        }
+        double p = 2.0 * std::min(left, right) / total;
+        if (p > 1.0) p = 1.0;
+        evalues_out[i] = p * (double)K;
+    }
+    return CDLGB_OK;
+}
+
 }  // extern "C"

@@ -242,7 +242,7 @@ int extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_
     int32_t* dout = c->scan_i + K;
     int32_t* dpos = c->scan_i + 5 * K;
     ExtArgs a;
-    a.S = c->S; a.pos = dpos; a.comp = use_comp ? c->scan_u : nullptr; a.lens = dlens;
+    a.S = scan_data(c); a.pos = dpos; a.comp = use_comp ? c->scan_u : nullptr; a.lens = dlens;
     a.list = reinterpret_cast<int2*>(c->scan_f); a.out = dout;
     a.bg0 = bg[0]; a.bg1 = bg[1]; a.bg2 = bg[2]; a.bg3 = bg[3];
     a.ps = pseudocount; a.perc = perc_no_less_than; a.ic_thresh = ic_extension_thresh;
@@ -307,7 +307,7 @@ int rescore_positions(cdlgb_ctx* c, const float* pwms, const int32_t* pos, const
     CU_TRY(c, cudaMemcpyAsync(dpwm, pwms, npwm * 4, cudaMemcpyHostToDevice, c->stream));
     cdlgb_phase_begin(c, PH_SCAN);
     k_rescore<<<dim3((unsigned)((N + 255) / 256), (unsigned)K), 256, 0, c->stream>>>(
-        c->S, dpwm, dpos, dlens, K, maxlen, N, L, dsc);
+        scan_data(c), dpwm, dpos, dlens, K, maxlen, N, L, dsc);
     LAUNCH_CHECK(c, "k_rescore");
     cdlgb_phase_end(c, PH_SCAN);
     CU_TRY(c, cudaMemcpyAsync(score_out, dsc, KN * 4, cudaMemcpyDeviceToHost, c->stream));

@@ -204,7 +204,7 @@ int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* 
     if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
     if (shm > 48 * 1024)
         CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    k_scan_fwd<<<N, kScanThreads, shm, c->stream>>>(c->S, c->scan_f, c->scan_i,
+    k_scan_fwd<<<N, kScanThreads, shm, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
                                                      c->scan_f + (size_t)K * 4 * maxlen, K, maxlen,
                                                      L, dpos);
     LAUNCH_CHECK(c, "k_scan_fwd");
@@ -227,7 +227,7 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
     if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
     if (shm > 48 * 1024)
         CU_TRY(c, cudaFuncSetAttribute(k_scan_both, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    k_scan_both<<<N, kScanThreads, shm, c->stream>>>(c->S, c->scan_f, c->scan_i,
+    k_scan_both<<<N, kScanThreads, shm, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
                                                       c->scan_f + (size_t)K * 4 * maxlen, K,
                                                       maxlen, L, dpos, dscore, c->scan_u);
     LAUNCH_CHECK(c, "k_scan_both");
@@ -276,7 +276,7 @@ int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp, const 
     int chunks = (N + 1023) / 1024;
     if (chunks > 64) chunks = 64;
     size_t shm = (size_t)(4 * maxlen + 1) * 4;
-    k_count<<<dim3(K, chunks), 256, shm, c->stream>>>(c->S, dpos, use_comp ? c->scan_u : nullptr,
+    k_count<<<dim3(K, chunks), 256, shm, c->stream>>>(scan_data(c), dpos, use_comp ? c->scan_u : nullptr,
                                                       dlens, K, maxlen, L, N, dcnt, dnseq);
     LAUNCH_CHECK(c, "k_count");
     CU_TRY(c, cudaMemcpyAsync(counts_out, dcnt, ncnt * 4, cudaMemcpyDeviceToHost, c->stream));

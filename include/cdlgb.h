@@ -92,7 +92,8 @@ typedef enum {
     CDLGB_FIELD_G2_DUAL = 14,   /* g2, (Lg, N) */
     CDLGB_FIELD_Y1_DUAL = 15,   /* y1, (Lg, N) */
     CDLGB_FIELD_OBJ_BEST = 16,  /* one float64 */
-    CDLGB_FIELD_DATA = 17       /* the loaded one-hot data, (4L, N) float32 */
+    CDLGB_FIELD_DATA = 17,      /* the loaded one-hot data, (4L, N) float32 */
+    CDLGB_FIELD_BACKGROUND = 18 /* the shuffled background (cdlgb_make_background), (4L, N) float32 */
 } cdlgb_field;
 
 /* Fill *p with the CDL_setup defaults. */
@@ -255,6 +256,32 @@ int cdlgb_rescore_positions(cdlgb_ctx* ctx, const float* pwms, const int32_t* po
 int cdlgb_trim_pfms(const float* pfms, const int32_t* lens, int32_t K, int32_t maxlen,
                     const float* bg, const int32_t* mask_len, const float* mask_thresh,
                     int32_t nmask, int32_t* front_out, int32_t* back_out);
+
+/* The background data of the e-value filter.  The reference shuffles its FASTA file
+ * with MEME's `fasta-shuffle-letters -kmer 3` (src/SETUP/LOAD_setup.jl:5-14), an external
+ * program.  This replaces it on the device: every loaded sequence is shuffled keeping its
+ * length, its first and last (k-1)-mers and the count of every k-mer (Euler-path shuffle,
+ * Altschul & Erickson, with Wilson's random arborescence; splitmix64 numbers keyed by
+ * (seed, sequence), so the result is reproducible).  A column with no base is a fifth
+ * symbol.  k in 1..4 (the reference uses 3).  The result stays on the device next to
+ * the data; read it with cdlgb_get(CDLGB_FIELD_BACKGROUND). */
+int cdlgb_make_background(cdlgb_ctx* ctx, int32_t k, uint64_t seed);
+
+/* Which one-hot matrix the scans (cdlgb_scan_fwd / _both), cdlgb_count_pfms,
+ * cdlgb_extend_positions and cdlgb_rescore_positions read: 0 = the loaded data (the
+ * default; reset by every load), 1 = the background.  The ADMM always reads the data.
+ * The reference scans its background through the same scan functions
+ * (src/SEARCH/e_value_filter.jl:2-13). */
+int cdlgb_select_data(cdlgb_ctx* ctx, int32_t which);
+
+/* filter_using_evalue!'s e-values (src/SEARCH/e_value_filter.jl:15-23): for motif k with
+ * a = hits[k] sequences hit in the data and b = hits_bg[k] in the background (both out
+ * of N), evalues_out[k] = K * pvalue(FisherExactTest(a, N, b, N)), the two-sided
+ * "central" p-value min(1, 2 min(P(X <= a), P(X >= a))) of X ~ Hypergeometric(a + N
+ * successes, b + N failures, a + b draws) (HypothesisTests 0.10.10 over Distributions
+ * 0.25.54), in double precision.  Host only. */
+int cdlgb_fisher_evalues(const int32_t* hits, const int32_t* hits_bg, int32_t K, int32_t N,
+                         double* evalues_out);
 
 /* One transfac file body as save_pfms_as_transfac writes it
  * (src/SAVE/save_learned_results.jl:186-196): pfm (4, w) col-major, values printed

@@ -475,6 +475,150 @@ def scores_reevaluation(data, pwms, pos, lens) -> np.ndarray:
     return out
 
 
+# ----------------------------------------------------------------------------------
+# (f) background + e-value filter (src/SETUP/LOAD_setup.jl:5-14,
+#     src/SEARCH/e_value_filter.jl:1-65)
+# ----------------------------------------------------------------------------------
+_M64 = (1 << 64) - 1
+_GOLDEN = 0x9E3779B97F4A7C15
+
+
+def _mix64(z: int) -> int:
+    """splitmix64's output function (Steele, Lea & Flood 2014)."""
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+    return z ^ (z >> 31)
+
+
+class SplitMix:
+    """Per-sequence splitmix64 stream: state = mix(seed ^ golden * (n + 1)); each draw
+    adds the golden gamma and mixes; below(m) = ((z >> 32) * m) >> 32."""
+
+    def __init__(self, seed: int, n: int):
+        self.s = _mix64((seed ^ ((_GOLDEN * (n + 1)) & _M64)) & _M64)
+
+    def below(self, m: int) -> int:
+        self.s = (self.s + _GOLDEN) & _M64
+        return ((_mix64(self.s) >> 32) * m) >> 32
+
+
+def _fisher_yates(a: list, m: int, rng: SplitMix):
+    for i in range(m - 1, 0, -1):
+        j = rng.below(i + 1)
+        a[i], a[j] = a[j], a[i]
+
+
+def onehot_symbols(data: np.ndarray) -> np.ndarray:
+    """(N, 4L) one-hot -> (N, L) symbols 0..3 (A C G T), 4 where the column is not a
+    one-hot vector."""
+    N, L4 = data.shape
+    oh = data.reshape(N, L4 // 4, 4)
+    ones = (oh == 1).sum(axis=2)
+    zeros = (oh == 0).sum(axis=2)
+    sym = np.argmax(oh == 1, axis=2).astype(np.int64)
+    sym[~((ones == 1) & (zeros == 3))] = 4
+    return sym
+
+
+def klet_shuffle_seq(sym, k: int, rng: SplitMix) -> list:
+    """k-let preserving shuffle of one symbol sequence (alphabet of 5): the Euler-path
+    method of Altschul & Erickson with Wilson's random arborescence towards the last
+    (k-1)-mer, in the draw order of the device kernel: the last exits of the vertices in
+    increasing vertex order (loop-erased walks), then for each vertex in increasing
+    order a Fisher-Yates shuffle of its other exits (all exits for the last vertex),
+    then the walk from the first (k-1)-mer."""
+    sym = [int(x) for x in sym]
+    L = len(sym)
+    if k == 1:
+        a = list(sym)
+        _fisher_yates(a, L, rng)
+        return a
+    E = L - k + 1
+    if E <= 0:
+        return list(sym)
+    V = 5 ** (k - 1)
+    v0 = 0
+    for j in range(k - 1):
+        v0 = v0 * 5 + sym[j]
+    exits = [[] for _ in range(V)]
+    u = v0
+    for i in range(E):
+        w = sym[i + k - 1]
+        exits[u].append(w)
+        u = (u * 5 + w) % V
+    vend = u
+    intree = [False] * V
+    intree[vend] = True
+    nxt = [0] * V
+    for v in range(V):
+        if not exits[v] or intree[v]:
+            continue
+        u = v
+        while not intree[u]:
+            nxt[u] = rng.below(len(exits[u]))
+            u = (u * 5 + exits[u][nxt[u]]) % V
+        u = v
+        while not intree[u]:
+            intree[u] = True
+            u = (u * 5 + exits[u][nxt[u]]) % V
+    for v in range(V):
+        e = exits[v]
+        m = len(e)
+        if m == 0:
+            continue
+        if v != vend:
+            e[nxt[v]], e[m - 1] = e[m - 1], e[nxt[v]]
+            _fisher_yates(e, m - 1, rng)
+        else:
+            _fisher_yates(e, m, rng)
+    out = sym[: k - 1]
+    cur = [0] * V
+    u = v0
+    for _ in range(E):
+        w = exits[u][cur[u]]
+        cur[u] += 1
+        out.append(w)
+        u = (u * 5 + w) % V
+    return out
+
+
+def make_background(data: np.ndarray, k: int = 3, seed: int = 0) -> np.ndarray:
+    """Every sequence of the (N, 4L) one-hot data k-let shuffled (sequence n with the
+    stream SplitMix(seed, n)); symbol 4 becomes a zero column.  Returns (N, 4L)."""
+    sym = onehot_symbols(data)
+    N, L = sym.shape
+    out = np.zeros((N, L, 4), np.float32)
+    for n in range(N):
+        s = klet_shuffle_seq(sym[n], k, SplitMix(seed, n))
+        for i, x in enumerate(s):
+            if x < 4:
+                out[n, i, x] = 1.0
+    return out.reshape(N, 4 * L)
+
+
+def kmer_counts(sym_row, k: int) -> dict:
+    out = {}
+    for i in range(len(sym_row) - k + 1):
+        key = tuple(int(x) for x in sym_row[i:i + k])
+        out[key] = out.get(key, 0) + 1
+    return out
+
+
+def fisher_evalue_exact(a: int, b: int, N: int, K: int) -> float:
+    """K * pvalue(FisherExactTest(a, N, b, N)) (src/SEARCH/e_value_filter.jl:19-23) from
+    exact rationals: X ~ Hypergeometric(a + N, b + N, a + b), central two-sided
+    p = min(1, 2 min(P(X <= a), P(X >= a)))."""
+    from fractions import Fraction
+    from math import comb
+    r1, r2, c1 = a + N, b + N, a + b
+    lo, hi = max(0, c1 - r2), min(c1, r1)
+    den = comb(r1 + r2, c1)
+    left = sum(comb(r1, j) * comb(r2, c1 - j) for j in range(lo, a + 1))
+    right = sum(comb(r1, j) * comb(r2, c1 - j) for j in range(a, hi + 1))
+    p = min(Fraction(1), 2 * min(Fraction(left, den), Fraction(right, den)))
+    return float(p * K)
+
+
 def pfm2pwm(pfm, bg=(0.25, 0.25, 0.25, 0.25)):
     """src/SEARCH/helpers.jl:12-13."""
     bgv = np.asarray(bg, dtype=np.asarray(pfm).dtype).reshape(4, 1)

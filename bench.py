@@ -467,6 +467,113 @@ def run_batched(args):
                        "L": [int(d.shape[1] // 4) for d in data]}}
 
 
+def search_inputs(wl=WORKLOAD, K=32, N=None):
+    """The search-stage inputs on the bench dataset: the planted motifs' cores (two
+    columns trimmed per side, so that extend! has columns to find) and random
+    Dirichlet(1) PWMs of widths 8..16, K in all."""
+    pkg = _pkg()
+    n = wl["N"] if N is None else N
+    bases, motifs, _ = pkg.synth.plant_dataset(wl["seed"], n, wl["L"], wl["widths"], wl["occ"])
+    pwms = []
+    for m in motifs:
+        core = m[:, 2:-2]
+        pwms.append(np.log2(((core + 0.05) / 1.2) / 0.25).astype(np.float32))
+    rng = np.random.default_rng(17)
+    while len(pwms) < K:
+        w = int(rng.integers(8, 17))
+        pfm = rng.dirichlet(np.ones(4), size=w).T
+        pwms.append(np.log2(((pfm + 0.02) / 1.08) / 0.25).astype(np.float32))
+    return bases, pwms
+
+
+def search_round(pkg, c, pwms, thresh, filter_size=4, times=None):
+    """One round of find_motif's refinement loop (src/WRAPPER/wrap.jl:88-98) through
+    the package: overlapping_scan!, non_overlap_scan!, extend! (extension + PFMs),
+    masked_trim! (trim + PWMs + Touzet thresholds)."""
+    def tick(name, t0):
+        if times is not None:
+            times[name] = times.get(name, 0.0) + time.perf_counter() - t0
+        return time.perf_counter()
+    lens = np.array([p.shape[1] for p in pwms], np.int32)
+    t = time.perf_counter()
+    pos, sc, uc = pkg.overlapping_scan(c, pwms, thresh)
+    t = tick("overlapping_scan", t)
+    pos, sc, uc = pkg.non_overlap_scan(c, pos, sc, lens, uc)
+    t = tick("non_overlap_scan", t)
+    ext = pkg.extend(c, pos, lens, filter_size, use_comp=uc, smoothing=False)
+    t = tick("extend", t)
+    out = pkg.masked_trim(ext["pfms"], filter_size, ext["positions"], ext["use_comp"], c=c)
+    tick("masked_trim", t)
+    return out
+
+
+def run_search(args):
+    """Motif-search stage on the bench dataset (N = 20000, L = 200): search rounds/s
+    through the package's public calls (host arrays in and out, as a caller sees them),
+    per-call times, the one-off background shuffle and e-value filter, and the oracle
+    on a sample of sequences as the CPU figure."""
+    pkg = _pkg()
+    wl = WORKLOAD
+    K = args.search_k
+    bases, pwms = search_inputs(wl, K)
+    S = pkg.synth.onehot(bases)
+    c = pkg.CDL(pkg.CDLSetup(M=2, filter_size=2))
+    c.load_data(S)
+    thresh = pkg.get_thresh(c, pwms)
+    for _ in range(args.warmup):
+        search_round(pkg, c, pwms, thresh)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    times = {}
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out = search_round(pkg, c, pwms, thresh, times=times)
+    dt = time.perf_counter() - t0
+    clocks = sampler.stop()
+    t1 = time.perf_counter()
+    c.make_background(k=3, seed=1)
+    t_bg = time.perf_counter() - t1
+    lens = np.array([p.shape[1] for p in pwms], np.int32)
+    pos, _, _ = pkg.overlapping_scan(c, pwms, thresh)
+    t1 = time.perf_counter()
+    ev = pkg.filter_using_evalue(c, pwms, thresh, pos, cpu=True, non_overlap=True)
+    t_ev = time.perf_counter() - t1
+    c.close()
+    res = {"metric": f"motif search rounds/s at N={wl['N']}, L={wl['L']}, K={K} (overlapping_scan! + "
+                     "non_overlap_scan! + extend! + masked_trim! with thresholds)",
+           "value": args.steps / dt, "unit": "round/s", "higher_is_better": True,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+           "phases_ms_per_step": {k: 1e3 * v / args.steps for k, v in times.items()},
+           "motifs_after_round": int(len(out["pfms"])),
+           "background_k3_ms": 1e3 * t_bg, "evalue_filter_ms": 1e3 * t_ev,
+           "evalue_filter_kept": int(ev["keep"].sum()),
+           "dtype": "f32 scores / int32 counts", "data": "synthetic (seeded planted motifs)",
+           "clocks": clocks,
+           "config": {"workload": f"search_n{wl['N']}_l{wl['L']}_k{K}", "N": wl["N"], "L": wl["L"],
+                      "K": K, "filter_size_for_length_filters": 4,
+                      "timing": "wall clock around host-array calls (each call returns its results)"}}
+    if not args.no_cpu:
+        res["cpu_baseline"] = search_cpu_baseline(S, pwms, thresh, args.search_cpu_n)
+    return res
+
+
+def search_cpu_baseline(S, pwms, thresh, n_sample):
+    """The oracle's scans, non-overlap selection, extension and counts on the first
+    n_sample sequences, scaled to N (thresholds, trims and PFMs are per motif, left out)."""
+    from oracle import search_oracle as SO
+    lens = np.array([p.shape[1] for p in pwms], np.int32)
+    Ss = S[:n_sample]
+    t0 = time.perf_counter()
+    rp, rs, rc = SO.overlapping_scan(Ss, pwms, lens, thresh)
+    pos, sc, uc = SO.non_overlap_select(rp.T, rs.T, rc.T, lens)
+    npos, nl, _, _ = SO.extend_positions(Ss, pos, uc, lens)
+    SO.count_matrices(Ss, npos.T, uc.T, nl)
+    dt = time.perf_counter() - t0
+    return {"value": (n_sample / S.shape[0]) / dt, "unit": "round/s", "cores": 1, "kind": "port",
+            "sample": f"{n_sample} of {S.shape[0]} sequences, one round, NumPy/Python oracle; "
+                      "rate scaled by N"}
+
+
 def run_precision(args):
     """The float32 path (fused X-step, float64 objective) against the all-FP64 GPU
     reference from the same initial state, outer iteration by outer iteration: relative
@@ -534,6 +641,10 @@ def main():
     ap.add_argument("--precision", action="store_true",
                     help="precision study: float32 GPU path vs an all-FP64 GPU reference")
     ap.add_argument("--precision-iters", type=int, default=3)
+    ap.add_argument("--search", action="store_true",
+                    help="motif-search stage: scans, non-overlap selection, extension, trim")
+    ap.add_argument("--search-k", type=int, default=32)
+    ap.add_argument("--search-cpu-n", type=int, default=2000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.n:
@@ -551,6 +662,10 @@ def main():
     if args.serve:
         if rank == 0:
             print(json.dumps(run_serve(args)))
+        return
+    if args.search:
+        if rank == 0:
+            print(json.dumps(run_search(args)))
         return
     if args.precision:
         if rank == 0:

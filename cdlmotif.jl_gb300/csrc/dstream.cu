@@ -47,6 +47,44 @@ __device__ __forceinline__ void split_store(const float2* __restrict__ buf, int 
     }
 }
 
+// one of the three transforms of k_dfwd for the lane group's (sequence, filter pair):
+// WHICH 0: Y3 = projectionX!(X + y3) (rows l % 4 == 0 only), 1: H = (G1 - g1) + (G3 - g3),
+// 2: the previous d.  The state is read through the read-only path; P rows per column.
+template <int N1, int P, int WHICH>
+__device__ __forceinline__ void dfwd_one(const FArgs& A, float2* sb, int gl, const float2* tw2,
+                                         bool act, bool keep, size_t ra, size_t pa, size_t oa) {
+    constexpr int Lg = N1 * P;
+    constexpr int RS = N1 + 1;
+    constexpr int F = Lg / 2 + 1;
+    if (act) {
+#pragma unroll 8
+        for (int n2 = 0; n2 < P; ++n2) {
+            const int o = N1 * n2;
+            float2 v;
+            if (WHICH == 0) {
+                v = keep ? f2(__ldg(A.X + ra + o) + __ldg(A.y3 + ra + o),
+                              __ldg(A.X + ra + Lg + o) + __ldg(A.y3 + ra + Lg + o))
+                         : f2(0.f, 0.f);
+            } else if (WHICH == 1) {
+                v = f2((__ldg(A.G1 + pa + o) - __ldg(A.g1 + ra + o)) + (__ldg(A.G3 + pa + o) - __ldg(A.g3 + ra + o)),
+                       (__ldg(A.G1 + pa + Lg + o) - __ldg(A.g1 + ra + Lg + o)) +
+                           (__ldg(A.G3 + pa + Lg + o) - __ldg(A.g3 + ra + Lg + o)));
+            } else {
+                v = f2(__ldg(A.d + ra + o), __ldg(A.d + ra + Lg + o));
+            }
+            sb[n2 * RS + gl] = v;
+        }
+        fwd_step1<N1, P>(sb, gl, tw2);
+    }
+    __syncwarp();
+    fwd_step2<N1, P>(sb, gl, act);
+    if (act) {
+        float2* out = WHICH == 0 ? A.Yh : WHICH == 1 ? A.Hh : A.Dh;
+        split_store<Lg, N1>(sb, gl, out + oa, out + oa + F);
+    }
+    __syncwarp();
+}
+
 template <int N1, int P>
 __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
     constexpr int Lg = N1 * P;
@@ -80,33 +118,9 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
         const size_t ra = ((size_t)n * A.M + ma) * Lg + gl;   // row of filter a at lane gl
         const size_t pa = (size_t)ma * Lg + gl;
         const size_t oa = ((size_t)n * A.M + ma) * F;
-        for (int which = 0; which < 3; ++which) {
-            if (act) {
-#pragma unroll 4
-                for (int n2 = 0; n2 < P; ++n2) {
-                    const int o = N1 * n2;
-                    float2 v;
-                    if (which == 0) {
-                        v = keep ? f2(A.X[ra + o] + A.y3[ra + o], A.X[ra + Lg + o] + A.y3[ra + Lg + o])
-                                 : f2(0.f, 0.f);
-                    } else if (which == 1) {
-                        v = f2((A.G1[pa + o] - A.g1[ra + o]) + (A.G3[pa + o] - A.g3[ra + o]),
-                               (A.G1[pa + Lg + o] - A.g1[ra + Lg + o]) + (A.G3[pa + Lg + o] - A.g3[ra + Lg + o]));
-                    } else {
-                        v = f2(A.d[ra + o], A.d[ra + Lg + o]);
-                    }
-                    sb[n2 * RS + gl] = v;
-                }
-                fwd_step1<N1, P>(sb, gl, tw2);
-            }
-            __syncwarp();
-            fwd_step2<N1, P>(sb, gl, act);
-            if (act) {
-                float2* out = which == 0 ? A.Yh : which == 1 ? A.Hh : A.Dh;
-                split_store<Lg, N1>(sb, gl, out + oa, out + oa + F);
-            }
-            __syncwarp();
-        }
+        dfwd_one<N1, P, 0>(A, sb, gl, tw2, act, keep, ra, pa, oa);
+        dfwd_one<N1, P, 1>(A, sb, gl, tw2, act, keep, ra, pa, oa);
+        dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, ra, pa, oa);
     }
 }
 

@@ -201,33 +201,95 @@ __global__ void k_sub(const float* __restrict__ a, const float* __restrict__ b,
 }
 
 // Per (f, n): the Sherman-Morrison dictionary solve (cdl_kernels.jl:2-33, train.jl:52-61),
-// with T = sum_m Y3h * rfft(d_old) for Td (train.jl:56).
-__global__ void k_dsolve(const float2* __restrict__ Yh, float2* __restrict__ Hh,
-                         const float2* __restrict__ Dh, const float2* __restrict__ Zh,
-                         float2* __restrict__ Th, int F, int M, int nfb, float kd, float scale) {
-    int fb = blockIdx.x % nfb;
-    size_t n = blockIdx.x / nfb;
-    int f = fb * blockDim.x + threadIdx.x;
-    if (f >= F) return;
-    size_t base = n * M * F + f;
+// with T = sum_m Y3h * rfft(d_old) for Td (train.jl:56).  A CTA takes 32 bins of one
+// sequence; warp w sums filters w, w + 8, w + 16, ... (lane = bin), the eight partial
+// sums are added in warp order, and Y3h, Hh stay in shared memory between the sums and
+// the update, so every spectrum is read from HBM once (STAGE; without it, for M too
+// large for shared memory, the update reads them again).
+constexpr int kDsBins = 32, kDsWarps = 8;
+template <bool STAGE>
+__global__ void __launch_bounds__(kDsBins * kDsWarps) k_dsolve(
+    const float2* __restrict__ Yh, float2* __restrict__ Hh, const float2* __restrict__ Dh,
+    const float2* __restrict__ Zh, float2* __restrict__ Th, int F, int M, int nfb, float kd,
+    float scale) {
+    extern __shared__ float4 ds_smem[];
+    const int Ms = STAGE ? M : 0;
+    float2* ys = reinterpret_cast<float2*>(ds_smem);       // [M][kDsBins]
+    float2* hs = ys + (size_t)Ms * kDsBins;                // [M][kDsBins]
+    float* pB = reinterpret_cast<float*>(hs + (size_t)Ms * kDsBins);  // [kDsWarps][kDsBins]
+    float2* pQ = reinterpret_cast<float2*>(pB + kDsWarps * kDsBins);  // [kDsWarps][kDsBins]
+    float2* pT = pQ + kDsWarps * kDsBins;
+    const int fb = blockIdx.x % nfb;
+    const size_t n = blockIdx.x / nfb;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int f = fb * kDsBins + lane;
+    const bool on = f < F;
+    const size_t base = n * M * F + (on ? f : 0);
     float B = 0.f;
     float2 Q = make_float2(0.f, 0.f), T = make_float2(0.f, 0.f);
-    for (int m = 0; m < M; ++m) {
-        float2 y = Yh[base + (size_t)m * F];
+    for (int m = w; m < M; m += kDsWarps) {
+        float2 y = make_float2(0.f, 0.f), h = y, d = y;
+        if (on) {
+            y = Yh[base + (size_t)m * F];
+            h = Hh[base + (size_t)m * F];
+            d = Dh[base + (size_t)m * F];
+        }
+        if (STAGE) {
+            ys[m * kDsBins + lane] = y;
+            hs[m * kDsBins + lane] = h;
+        }
         B = fmaf(y.x, y.x, fmaf(y.y, y.y, B));
-        Q = cfma(y, Hh[base + (size_t)m * F], Q);
-        T = cfma(y, Dh[base + (size_t)m * F], T);
+        Q = cfma(y, h, Q);
+        T = cfma(y, d, T);
     }
-    float2 z = Zh[n * F + f];
-    float inv = 1.f / (B + kd);
-    float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
-    float2 W = make_float2(z.x - beta.x, z.y - beta.y);
-    for (int m = 0; m < M; ++m) {
-        float2 y = Yh[base + (size_t)m * F];
-        float2 h = cjfma(y, W, Hh[base + (size_t)m * F]);
+    pB[w * kDsBins + lane] = B;
+    pQ[w * kDsBins + lane] = Q;
+    pT[w * kDsBins + lane] = T;
+    __syncthreads();
+    B = 0.f;
+    Q = T = make_float2(0.f, 0.f);
+    for (int v = 0; v < kDsWarps; ++v) {
+        B += pB[v * kDsBins + lane];
+        Q = make_float2(Q.x + pQ[v * kDsBins + lane].x, Q.y + pQ[v * kDsBins + lane].y);
+        T = make_float2(T.x + pT[v * kDsBins + lane].x, T.y + pT[v * kDsBins + lane].y);
+    }
+    if (!on) return;
+    const float2 z = Zh[n * F + f];
+    const float inv = 1.f / (B + kd);
+    const float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
+    const float2 W = make_float2(z.x - beta.x, z.y - beta.y);
+    for (int m = w; m < M; m += kDsWarps) {
+        const float2 h = STAGE ? cjfma(ys[m * kDsBins + lane], W, hs[m * kDsBins + lane])
+                               : cjfma(Yh[base + (size_t)m * F], W, Hh[base + (size_t)m * F]);
         Hh[base + (size_t)m * F] = make_float2(h.x * scale, h.y * scale);
     }
-    Th[n * F + f] = make_float2(T.x * scale, T.y * scale);
+    if (w == 0) Th[n * F + f] = make_float2(T.x * scale, T.y * scale);
+}
+
+size_t dsolve_smem(int M, bool stage) {
+    return (stage ? (size_t)2 * M * kDsBins * sizeof(float2) : 0) +
+           (size_t)kDsWarps * kDsBins * (4 + 8 + 8);
+}
+
+// launches k_dsolve for cn sequences, staging the spectra when they fit shared memory
+int dsolve_launch(cdlgb_ctx* c, int cn, const float2* Yh, float2* Hh, const float2* Dh,
+                  const float2* Zh, float2* Th) {
+    const int F = c->F, M = c->M;
+    const int nfb = (F + kDsBins - 1) / kDsBins;
+    const size_t sm = dsolve_smem(M, true);
+    const bool stage = sm <= (size_t)200 * 1024;
+    if (stage && sm > 48 * 1024)
+        CU_TRY(c, cudaFuncSetAttribute(k_dsolve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const dim3 g((unsigned)((size_t)nfb * cn)), b(kDsBins * kDsWarps);
+    if (stage)
+        k_dsolve<true><<<g, b, sm, c->stream>>>(Yh, Hh, Dh, Zh, Th, F, M, nfb, c->p.sherman_const_cdl,
+                                                1.f / (float)c->Lg);
+    else
+        k_dsolve<false><<<g, b, dsolve_smem(M, false), c->stream>>>(Yh, Hh, Dh, Zh, Th, F, M, nfb,
+                                                                    c->p.sherman_const_cdl,
+                                                                    1.f / (float)c->Lg);
+    LAUNCH_CHECK(c, "k_dsolve");
+    return CDLGB_OK;
 }
 
 // G2' = (W'S + sigma (Td + g2)) / (W'W_ll + sigma)  (update_g2!, cdl_kernels.jl:68-77);
@@ -760,7 +822,6 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
             LAUNCH_CHECK(c, "k_sub");
             ST_TRY(r2c(c, N, c->sU, c->sUh));
-            const int nfb = (F + 127) / 128;
             for (int n0 = 0; n0 < N; n0 += c->chunk) {
                 const int cn = std::min(c->chunk, N - n0);
                 const size_t off = (size_t)n0 * M * Lg, cl = (size_t)cn * M * Lg;
@@ -778,10 +839,8 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                     ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh));
                     ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh));
                 }
-                k_dsolve<<<(unsigned)((size_t)nfb * cn), 128, 0, s>>>(
-                    c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F, c->sVh + (size_t)n0 * F, F, M, nfb,
-                    c->p.sherman_const_cdl, 1.f / (float)Lg);
-                LAUNCH_CHECK(c, "k_dsolve");
+                ST_TRY(dsolve_launch(c, cn, c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F,
+                                     c->sVh + (size_t)n0 * F));
                 if (void* fw = c->fused ? fused_dfwd(c) : nullptr) {
                     ST_TRY(dinv_run(c, fw, c->sBh, n0, cn));
                 } else {

@@ -166,8 +166,9 @@ __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
         const int s = act ? (int)(item - n * pairs) : 0;
         const size_t ia = ((size_t)n * A.M + 2 * s) * F;
         if (act) {
+#pragma unroll 5
             for (int f = gl; f < F; f += N1) {
-                const float2 a = A.Dh[ia + f], b = A.Dh[ia + F + f];
+                const float2 a = __ldg(A.Dh + ia + f), b = __ldg(A.Dh + ia + F + f);
                 if (f == 0 || f == half) {
                     sb[f] = f2(a.x, b.x);
                 } else {

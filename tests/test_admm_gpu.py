@@ -185,7 +185,9 @@ def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
 def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, monkeypatch):
     """All X-steps of a code update in one launch (state on chip) against one launch
     per X-step (state through HBM): the same operations in the same order, so every
-    field the X-step writes agrees bit for bit (Lg = 928 = 32 * 29 and 496 = 16 * 31)."""
+    field the X-step writes agrees bit for bit (Lg = 928 = 32 * 29 and 496 = 16 * 31).
+    The D-steps in between see the same X and y3, so d, g1, g3 and G1 agree bit for bit
+    too."""
     N, L, M, fs, cs = shape
     if cs:
         monkeypatch.setenv("CDLGB_CLUSTER", cs)
@@ -205,9 +207,10 @@ def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, m
                 objs.append(pkg.update_best(c)[0])
                 pkg.dict_update(c, 1)
             pkg.code_update(c, 4)
-            out[multi] = {f: c.get(f) for f in ("X", "X_best", "y2", "y3", "DX", "Y1", "y1")}
+            out[multi] = {f: c.get(f) for f in ("X", "X_best", "y2", "y3", "DX", "Y1", "y1",
+                                                "d", "g1", "g3", "G1")}
             out[multi]["objs"] = np.array(objs)
-    for f in ("X", "X_best", "y2", "y3", "DX", "Y1", "y1"):
+    for f in ("X", "X_best", "y2", "y3", "DX", "Y1", "y1", "d", "g1", "g3", "G1"):
         np.testing.assert_array_equal(out["1"][f], out["0"][f], err_msg=f)
     # the objective's sum of |X| is associated differently (FP32 partial sums per lane)
     np.testing.assert_allclose(out["1"]["objs"], out["0"]["objs"], rtol=1e-6)

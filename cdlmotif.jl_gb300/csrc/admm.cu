@@ -41,18 +41,15 @@ __device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {  // conj
 }
 
 // ---------------------------------------------------------------- init kernels
-__global__ void k_randn_masked(float* __restrict__ X, size_t n, int Lg, uint64_t seed) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x) {
-        int l = (int)(i % (size_t)Lg);
-        float v = 0.f;
-        if ((l & 3) == 0) {
-            uint64_t h = splitmix64(seed * 0x2545F4914F6CDD1Dull ^ (uint64_t)i);
-            float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
-            float u2 = ((float)(h & 0xFFFFFFull) + 0.5f) * (1.0f / 16777216.0f);
-            v = sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
-        }
-        X[i] = v;
+// X0 = randn masked to the rows (l-1) % 4 == 0 (CDL_setup.jl:191-192).  Lg % 4 == 0, so
+// those rows are the .x components of the float4s; element 4 j draws from counter 4 j.
+__global__ void k_randn_masked(float4* __restrict__ X, size_t n4, uint64_t seed) {
+    for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n4;
+         j += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t h = splitmix64(seed * 0x2545F4914F6CDD1Dull ^ (uint64_t)(4 * j));
+        const float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
+        const float u2 = ((float)(h & 0xFFFFFFull) + 0.5f) * (1.0f / 16777216.0f);
+        X[j] = make_float4(sqrtf(-2.f * logf(u1)) * cospif(2.f * u2), 0.f, 0.f, 0.f);
     }
 }
 
@@ -676,11 +673,13 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     if (X0) {
         CU_TRY(c, cudaMemcpyAsync(X, X0, LMN * 4, cudaMemcpyHostToDevice, s));
     } else {
-        k_randn_masked<<<grid_for(LMN, kBlock), kBlock, 0, s>>>(X, LMN, Lg, seed);
+        k_randn_masked<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)X, LMN / 4, seed);
         LAUNCH_CHECK(c, "k_randn_masked");
     }
-    k_mask4<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)X, LMN / 4);
-    LAUNCH_CHECK(c, "k_mask4");
+    if (X0) {      // a given X0 is masked here; the drawn one already is
+        k_mask4<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)X, LMN / 4);
+        LAUNCH_CHECK(c, "k_mask4");
+    }
     // D0 (CDL_setup.jl:182-183), masked by P_D
     std::vector<float> D(LM, 0.f);
     if (D0) {

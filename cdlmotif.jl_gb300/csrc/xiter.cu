@@ -332,11 +332,16 @@ constexpr size_t kCap1 = 220 * 1024;   // one CTA per SM
 // (N1, P, filters per CTA): threads = 32 ceil((MC/2 + 1) / (32 / N1)) rounded to a warp
 struct Variant { int N1, P, MC, threads, minb; kern_t k; };
 // in order of preference (measured at L=200, K=64: 16 filters per CTA, one CTA per SM,
-// 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms)
+// 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms).  Lg = 32 P for the
+// primes 17..31 covers L = 104, 120, 152, 200, 216 at W = 16 (Lg = 4L + 8W).
 const Variant kVariants[] = {
     {32, 29, 16, 288, 1, k_xiter<32, 29, 288, 1, 16>},
     {32, 29, 8, 160, 2, k_xiter<32, 29, 160, 2, 8>},
     {16, 31, 16, 160, 2, k_xiter<16, 31, 160, 2, 16>},
+    {32, 17, 16, 288, 1, k_xiter<32, 17, 288, 1, 16>},
+    {32, 19, 16, 288, 1, k_xiter<32, 19, 288, 1, 16>},
+    {32, 23, 16, 288, 1, k_xiter<32, 23, 288, 1, 16>},
+    {32, 31, 16, 288, 1, k_xiter<32, 31, 288, 1, 16>},
 };
 
 // bytes of shared memory: slot buffers, P parts, twiddles, the interleaved y2 / y3

@@ -37,9 +37,15 @@ def footprint_bytes(setup: CDLSetup, L: int, N: int, fft_mode: int = 0) -> int:
     return int(b.value)
 
 
+# transform lengths of the multi-iteration X-step kernel's variants (csrc/xiter.cu)
+REGISTER_LG = (496, 544, 608, 736, 928, 992)
+
+
 def friendly_length(L: int, filter_size: int) -> int:
-    """Smallest L' >= L whose transform length 4L' + 8W factors into primes <= 31 with a
-    power of two of at least 16 (the sizes the fused in-kernel FFTs handle best)."""
+    """A padded length L' >= L for serving: the smallest whose transform length
+    4L' + 8W is one of the multi-iteration kernel's (REGISTER_LG) if that costs at most
+    8 % more transform columns, else the smallest whose transform length factors into
+    primes <= 31 with a power of two of at least 16 (the generic in-kernel FFTs)."""
     def ok(n):
         if n % 16:
             return False
@@ -47,6 +53,10 @@ def friendly_length(L: int, filter_size: int) -> int:
             while n % p == 0:
                 n //= p
         return n == 1
+    lg = 4 * L + 8 * filter_size
+    for n in REGISTER_LG:
+        if lg <= n <= 1.08 * lg and (n - 8 * filter_size) % 4 == 0:
+            return (n - 8 * filter_size) // 4
     Lp = L
     while not ok(4 * Lp + 8 * filter_size):
         Lp += 1

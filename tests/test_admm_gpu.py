@@ -180,6 +180,30 @@ def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
         assert rel(c.DX[:, g:g + L4], ref.DX[:, g:g + L4]) < 10 * TOL_X
 
 
+@pytest.mark.parametrize("L,M", [(104, 32), (120, 32), (152, 64), (216, 32)])
+def test_multi_iteration_other_lengths(pkg, built_lib, L, M):
+    """The multi-iteration kernel at the other register-FFT lengths Lg = 32 P (P = 17,
+    19, 23, 31; W = 16): it is among the candidates for the shape, and 2 outer
+    iterations on 5 sequences match the FP64 oracle at the stated tolerance."""
+    fs = 16
+    synth = pkg.synth
+    bases, _, _ = synth.plant_dataset(17, 5, L, [8, 12], [0.4, 0.4])
+    S = synth.onehot(bases)
+    Lg = 4 * L + 8 * fs
+    X0 = synth.init_X0(4, 5, M, Lg)
+    D0 = synth.init_D0_unit_norm(4, M, Lg, 4 * fs)
+    ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    objs_ref = O.run_outer(ref, 2)
+    with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+        objs = pkg.run_outer(c, 2)
+        np.testing.assert_allclose(objs, objs_ref, rtol=TOL_OBJ)
+        assert rel(c.X, ref.X) < TOL_X and rel(c.d, ref.d) < TOL_X
+        assert rel(c.G1, ref.G1) < TOL_X and rel(c.D_best, ref.D_best) < TOL_X
+    with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
+        kinds = [x["kernel"] for x in c.autotune()["candidates"]]
+        assert "multi-iteration" in kinds
+
+
 @pytest.mark.parametrize("shape", [(5, 200, 64, 16, "4"), (5, 200, 64, 16, "8"),
                                    (7, 100, 16, 12, "")])
 def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, monkeypatch):

@@ -199,6 +199,10 @@ struct Variant { int N1, P; kern_t k; kinv_t ki; };
 const Variant kVariants[] = {
     {32, 29, k_dfwd<32, 29>, k_dinv<32, 29>},
     {16, 31, k_dfwd<16, 31>, k_dinv<16, 31>},
+    {32, 17, k_dfwd<32, 17>, k_dinv<32, 17>},
+    {32, 19, k_dfwd<32, 19>, k_dinv<32, 19>},
+    {32, 23, k_dfwd<32, 23>, k_dinv<32, 23>},
+    {32, 31, k_dfwd<32, 31>, k_dinv<32, 31>},
 };
 
 struct FwdPlan {

@@ -178,6 +178,17 @@ void* fused_dfwd(cdlgb_ctx* c);
 int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn);
 int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 
+// a scan-family scratch buffer of at least n elements (reallocated when too small)
+template <typename T>
+inline int ensure_scratch(cdlgb_ctx* c, T** p, size_t* cap, size_t n) {
+    if (*cap >= n) return CDLGB_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    CU_TRY(c, cudaMalloc((void**)p, n * sizeof(T)));
+    *cap = n;
+    return CDLGB_OK;
+}
 // ---- scan.cu ----
 int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
              int K, int maxlen, int32_t* pos_out);

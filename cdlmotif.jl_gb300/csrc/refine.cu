@@ -204,17 +204,6 @@ __global__ void k_rescore(const float* __restrict__ S, const float* __restrict__
     score[(size_t)n * K + k] = s;
 }
 
-template <typename T>
-int grow(cdlgb_ctx* c, T** p, size_t* cap, size_t n) {
-    if (*cap >= n) return CDLGB_OK;
-    if (*p) cudaFree(*p);
-    *p = nullptr;
-    *cap = 0;
-    CU_TRY(c, cudaMalloc((void**)p, n * sizeof(T)));
-    *cap = n;
-    return CDLGB_OK;
-}
-
 }  // namespace
 
 int extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_t* lens, int K,
@@ -235,9 +224,9 @@ int extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_
         if (pos[i] < 0 || pos[i] > L)
             return cdlgb_seterr(c, CDLGB_EINVAL, "extend: pos[%zu]=%d outside 0..L=%d", i, pos[i], L);
     // device scratch: lens (K) + out (4K) + pos (KN) ints, use_comp (KN) bytes, list (KN) int2
-    ST_TRY(grow(c, &c->scan_i, &c->scan_i_cap, (size_t)5 * K + KN));
-    ST_TRY(grow(c, &c->scan_u, &c->scan_u_cap, KN));
-    ST_TRY(grow(c, &c->scan_f, &c->scan_f_cap, 2 * KN));
+    ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)5 * K + KN));
+    ST_TRY(ensure_scratch(c, &c->scan_u, &c->scan_u_cap, KN));
+    ST_TRY(ensure_scratch(c, &c->scan_f, &c->scan_f_cap, 2 * KN));
     int32_t* dlens = c->scan_i;
     int32_t* dout = c->scan_i + K;
     int32_t* dpos = c->scan_i + 5 * K;
@@ -296,8 +285,8 @@ int rescore_positions(cdlgb_ctx* c, const float* pwms, const int32_t* pos, const
                                 i, pos[i], lens[k], L);
     }
     const size_t npwm = (size_t)K * 4 * maxlen;
-    ST_TRY(grow(c, &c->scan_i, &c->scan_i_cap, (size_t)K + KN));
-    ST_TRY(grow(c, &c->scan_f, &c->scan_f_cap, npwm + KN));
+    ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)K + KN));
+    ST_TRY(ensure_scratch(c, &c->scan_f, &c->scan_f_cap, npwm + KN));
     int32_t* dlens = c->scan_i;
     int32_t* dpos = c->scan_i + K;
     float* dpwm = c->scan_f;

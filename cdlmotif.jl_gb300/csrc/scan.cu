@@ -154,17 +154,6 @@ __global__ void k_count(const float* __restrict__ data, const int32_t* __restric
     if (threadIdx.x == 0 && cnt[4 * maxlen]) atomicAdd(&nseq[k], cnt[4 * maxlen]);
 }
 
-template <typename T>
-int ensure(cdlgb_ctx* c, T** p, size_t* cap, size_t n) {
-    if (*cap >= n) return CDLGB_OK;
-    if (*p) cudaFree(*p);
-    *p = nullptr;
-    *cap = 0;
-    CU_TRY(c, cudaMalloc((void**)p, n * sizeof(T)));
-    *cap = n;
-    return CDLGB_OK;
-}
-
 int check_pwm_args(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
                    int K, int maxlen) {
     if (!c->loaded) return cdlgb_seterr(c, CDLGB_ESTATE, "no data loaded");
@@ -181,8 +170,8 @@ int check_pwm_args(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const f
 int upload_pwms(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh, int K,
                 int maxlen, size_t extra_i) {
     size_t nf = (size_t)K * 4 * maxlen + K;
-    ST_TRY(ensure(c, &c->scan_f, &c->scan_f_cap, nf + (size_t)K * c->N));
-    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, (size_t)K + extra_i));
+    ST_TRY(ensure_scratch(c, &c->scan_f, &c->scan_f_cap, nf + (size_t)K * c->N));
+    ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)K + extra_i));
     CU_TRY(c, cudaMemcpyAsync(c->scan_f, pwms, (size_t)K * 4 * maxlen * 4, cudaMemcpyHostToDevice,
                               c->stream));
     CU_TRY(c, cudaMemcpyAsync(c->scan_f + (size_t)K * 4 * maxlen, thresh, (size_t)K * 4,
@@ -220,7 +209,7 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
     const int N = c->N, L = c->L4 / 4;
     cdlgb_phase_begin(c, PH_SCAN);
     ST_TRY(upload_pwms(c, pwms, lens, thresh, K, maxlen, (size_t)K * N));
-    ST_TRY(ensure(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));
+    ST_TRY(ensure_scratch(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));
     int32_t* dpos = c->scan_i + K;
     float* dscore = c->scan_f + (size_t)K * 4 * maxlen + K;
     size_t shm = (size_t)4 * L * sizeof(float);
@@ -262,8 +251,8 @@ int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp, const 
         }
     }
     size_t ncnt = (size_t)4 * maxlen * K;
-    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, (size_t)K + (size_t)K * N + ncnt + K));
-    ST_TRY(ensure(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));
+    ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)K + (size_t)K * N + ncnt + K));
+    ST_TRY(ensure_scratch(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));
     int32_t* dlens = c->scan_i;
     int32_t* dpos = c->scan_i + K;
     int32_t* dcnt = dpos + (size_t)K * N;
@@ -339,9 +328,9 @@ int nonoverlap_select(cdlgb_ctx* c, int32_t* pos, float* score, uint8_t* use_com
         if (lens[k] < 1) return cdlgb_seterr(c, CDLGB_EINVAL, "select_nonoverlapping: lens[%d]=%d", k, lens[k]);
     const int N = c->N;
     const size_t KN = (size_t)K * N;
-    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, (size_t)K + 2 * KN));
-    ST_TRY(ensure(c, &c->scan_f, &c->scan_f_cap, 2 * KN));
-    ST_TRY(ensure(c, &c->scan_u, &c->scan_u_cap, KN));
+    ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)K + 2 * KN));
+    ST_TRY(ensure_scratch(c, &c->scan_f, &c->scan_f_cap, 2 * KN));
+    ST_TRY(ensure_scratch(c, &c->scan_u, &c->scan_u_cap, KN));
     int32_t* dlens = c->scan_i;
     int32_t* dpos = c->scan_i + K;
     int32_t* dord = dpos + KN;
@@ -478,7 +467,7 @@ int touzet_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int 
         range[p] = (int32_t)(hi - lo + 1);
         thr[p] = (unsigned long long)ceil(ldexp(pval, 2 * m));   // pval 4^m is exact; <= 2^62
     }
-    ST_TRY(ensure(c, &c->scan_i, &c->scan_i_cap, nk + 5 * (size_t)K));
+    ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, nk + 5 * (size_t)K));
     int32_t* d_kq = c->scan_i;
     int32_t* d_lens = d_kq + nk + 2 * (size_t)K;
     int32_t* d_alpha = d_lens + K;

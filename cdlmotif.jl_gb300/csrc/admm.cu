@@ -198,7 +198,10 @@ __global__ void k_sub(const float* __restrict__ a, const float* __restrict__ b,
 }
 
 // Per (f, n): the Sherman-Morrison dictionary solve (cdl_kernels.jl:2-33, train.jl:52-61),
-// with T = sum_m Y3h * rfft(d_old) for Td (train.jl:56).  A CTA takes 32 bins of one
+// with T = sum_m Y3h * rfft(d_old) for Td (train.jl:56).  Dh holds rfft(d_old) on entry
+// (the imaginary parts of its f = 0 and f = Lg/2 bins, which a real transform has as
+// zero, are read as zero) and the new d-hat times scale_out on exit; Th = T * scale.
+// A CTA takes 32 bins of one
 // sequence; warp w sums filters w, w + 8, w + 16, ... (lane = bin), the eight partial
 // sums are added in warp order, and Y3h, Hh stay in shared memory between the sums and
 // the update, so every spectrum is read from HBM once (STAGE; without it, for M too
@@ -206,9 +209,9 @@ __global__ void k_sub(const float* __restrict__ a, const float* __restrict__ b,
 constexpr int kDsBins = 32, kDsWarps = 8;
 template <bool STAGE>
 __global__ void __launch_bounds__(kDsBins * kDsWarps) k_dsolve(
-    const float2* __restrict__ Yh, float2* __restrict__ Hh, const float2* __restrict__ Dh,
+    const float2* __restrict__ Yh, const float2* __restrict__ Hh, float2* __restrict__ Dh,
     const float2* __restrict__ Zh, float2* __restrict__ Th, int F, int M, int nfb, float kd,
-    float scale) {
+    float scale, float scale_out) {
     extern __shared__ float4 ds_smem[];
     const int Ms = STAGE ? M : 0;
     float2* ys = reinterpret_cast<float2*>(ds_smem);       // [M][kDsBins]
@@ -230,6 +233,7 @@ __global__ void __launch_bounds__(kDsBins * kDsWarps) k_dsolve(
             y = Yh[base + (size_t)m * F];
             h = Hh[base + (size_t)m * F];
             d = Dh[base + (size_t)m * F];
+            if (f == 0 || f == F - 1) d.y = 0.f;
         }
         if (STAGE) {
             ys[m * kDsBins + lane] = y;
@@ -258,7 +262,7 @@ __global__ void __launch_bounds__(kDsBins * kDsWarps) k_dsolve(
     for (int m = w; m < M; m += kDsWarps) {
         const float2 h = STAGE ? cjfma(ys[m * kDsBins + lane], W, hs[m * kDsBins + lane])
                                : cjfma(Yh[base + (size_t)m * F], W, Hh[base + (size_t)m * F]);
-        Hh[base + (size_t)m * F] = make_float2(h.x * scale, h.y * scale);
+        Dh[base + (size_t)m * F] = make_float2(h.x * scale_out, h.y * scale_out);
     }
     if (w == 0) Th[n * F + f] = make_float2(T.x * scale, T.y * scale);
 }
@@ -268,9 +272,10 @@ size_t dsolve_smem(int M, bool stage) {
            (size_t)kDsWarps * kDsBins * (4 + 8 + 8);
 }
 
-// launches k_dsolve for cn sequences, staging the spectra when they fit shared memory
-int dsolve_launch(cdlgb_ctx* c, int cn, const float2* Yh, float2* Hh, const float2* Dh,
-                  const float2* Zh, float2* Th) {
+// launches k_dsolve for cn sequences, staging the spectra when they fit shared memory;
+// the new d-hat replaces Dh, times scale_out
+int dsolve_launch(cdlgb_ctx* c, int cn, const float2* Yh, const float2* Hh, float2* Dh,
+                  const float2* Zh, float2* Th, float scale_out) {
     const int F = c->F, M = c->M;
     const int nfb = (F + kDsBins - 1) / kDsBins;
     const size_t sm = dsolve_smem(M, true);
@@ -278,13 +283,14 @@ int dsolve_launch(cdlgb_ctx* c, int cn, const float2* Yh, float2* Hh, const floa
     if (stage && sm > 48 * 1024)
         CU_TRY(c, cudaFuncSetAttribute(k_dsolve<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const dim3 g((unsigned)((size_t)nfb * cn)), b(kDsBins * kDsWarps);
+    const float scale = 1.f / (float)c->Lg;
     if (stage)
         k_dsolve<true><<<g, b, sm, c->stream>>>(Yh, Hh, Dh, Zh, Th, F, M, nfb, c->p.sherman_const_cdl,
-                                                1.f / (float)c->Lg);
+                                                scale, scale_out);
     else
         k_dsolve<false><<<g, b, dsolve_smem(M, false), c->stream>>>(Yh, Hh, Dh, Zh, Th, F, M, nfb,
-                                                                    c->p.sherman_const_cdl,
-                                                                    1.f / (float)c->Lg);
+                                                                    c->p.sherman_const_cdl, scale,
+                                                                    scale_out);
     LAUNCH_CHECK(c, "k_dsolve");
     return CDLGB_OK;
 }
@@ -586,6 +592,7 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     size_t b = 0;
     b += (size_t)N * L4 * 4;                    // data
     b += 7 * LMN * 4;                           // X x2, y2, y3, d, g1, g3
+    if (fused) b += (size_t)N * M * F * 8;      // the previous D-step's d-hat
     b += 8 * LN * 4;                            // Y1 y1 DX Td G2 g2 + 2 scratch
     b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
     b += 2 * N * F * 8;                         // LN spectra
@@ -611,6 +618,9 @@ int admm_alloc(cdlgb_ctx* c) {
     ST_TRY(A((void**)&c->d, LMN * 4));
     ST_TRY(A((void**)&c->g1, LMN * 4));
     ST_TRY(A((void**)&c->g3, LMN * 4));
+    // the previous D-step's d-hat (fused path): (N, M, F) complex
+    if (c->fused) ST_TRY(A((void**)&c->Dhs, (size_t)c->N * c->M * c->F * 8));
+    c->dh_valid = 0;
     ST_TRY(A((void**)&c->Y1, LN * 4));
     ST_TRY(A((void**)&c->y1, LN * 4));
     ST_TRY(A((void**)&c->DX, LN * 4));
@@ -650,7 +660,7 @@ void admm_free(cdlgb_ctx* c) {
                     &c->y1, &c->DX, &c->Td, &c->G2, &c->g2, &c->sU, &c->G1, &c->G3,
                     &c->dsum, &c->Dbest, &c->vbar, &c->Ah, &c->sA, &c->sB, &c->part};
     for (auto p : fl) { if (*p) cudaFree(*p); *p = nullptr; }
-    float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh};
+    float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh, &c->Dhs};
     for (auto p : cl) { if (*p) cudaFree(*p); *p = nullptr; }
     if (c->dred) cudaFree(c->dred);
     if (c->dscalar) cudaFree(c->dscalar);
@@ -668,6 +678,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     c->xcur = 0;
     c->best_is_cur = 1;
     c->absx_fused = 0;
+    c->dh_valid = 0;
     float* X = c->Xb[0];
     // X0 (CDL_setup.jl:191-192): given, or standard normal; then masked to the 4-stride
     if (X0) {
@@ -811,6 +822,7 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
         cdlgb_phase_begin(c, PH_DSTEP);
         if (c->fused && fused_has_dstep(c)) {
             // transforms, solve, d, duals and G2 in one launch; then the means over n
+            c->dh_valid = 0;
             ST_TRY(fused_dstep(c));
             size_t pl4 = LM / 4;
             dim3 g((unsigned)((pl4 + 255) / 256), (unsigned)c->nchunk);
@@ -821,12 +833,19 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
             LAUNCH_CHECK(c, "k_sub");
             ST_TRY(r2c(c, N, c->sU, c->sUh));
+            void* fw = c->fused && c->Dhs ? fused_dfwd(c) : nullptr;
             for (int n0 = 0; n0 < N; n0 += c->chunk) {
                 const int cn = std::min(c->chunk, N - n0);
                 const size_t off = (size_t)n0 * M * Lg, cl = (size_t)cn * M * Lg;
-                if (void* fw = c->fused ? fused_dfwd(c) : nullptr) {
-                    // Y3, H and d formed and transformed in one streaming pass
-                    ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, c->sBh, c->sCh));
+                if (fw) {
+                    // Y3 and H formed and transformed in one streaming pass; rfft(d_old)
+                    // is the previous D-step's d-hat, kept in Dhs (transformed from d
+                    // only when there is none)
+                    float2* Dh = c->Dhs + (size_t)n0 * M * F;
+                    ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, c->sBh, c->dh_valid ? nullptr : Dh));
+                    ST_TRY(dsolve_launch(c, cn, c->sAh, c->sBh, Dh, c->sUh + (size_t)n0 * F,
+                                         c->sVh + (size_t)n0 * F, 1.f));
+                    ST_TRY(dinv_run(c, fw, Dh, n0, cn, 1.f / (float)Lg));
                 } else {
                     k_dprep<<<grid_for(cl / 4, kBlock), kBlock, 0, s>>>(
                         (const float4*)(cur_X(c) + off), (const float4*)(c->y3 + off),
@@ -837,15 +856,12 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                     ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
                     ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh));
                     ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh));
-                }
-                ST_TRY(dsolve_launch(c, cn, c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F,
-                                     c->sVh + (size_t)n0 * F));
-                if (void* fw = c->fused ? fused_dfwd(c) : nullptr) {
-                    ST_TRY(dinv_run(c, fw, c->sBh, n0, cn));
-                } else {
-                    ST_TRY(c2r(c, (long long)M * cn, c->sBh, c->d + off));
+                    ST_TRY(dsolve_launch(c, cn, c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F,
+                                         c->sVh + (size_t)n0 * F, 1.f / (float)Lg));
+                    ST_TRY(c2r(c, (long long)M * cn, c->sCh, c->d + off));
                 }
             }
+            c->dh_valid = fw != nullptr;
             ST_TRY(c2r(c, N, c->sVh, c->Td));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
                                                          c->gamma, LN, c->p.sigma);

@@ -49,6 +49,11 @@ struct cdlgb_ctx {
     int xcur = 0;                   // Xb[xcur] holds X
     int best_is_cur = 1;            // X_best aliases Xb[xcur] (else Xb[1-xcur])
     float *y2 = nullptr, *y3 = nullptr, *d = nullptr, *g1 = nullptr, *g3 = nullptr;
+    // fused path: the last D-step's d-hat (N, M, F), rfft(d) for the next D-step's Td sum,
+    // valid while dh_valid is set (a D-step through the streaming transforms sets it;
+    // initialisation and the other D-step paths clear it)
+    float2* Dhs = nullptr;
+    int dh_valid = 0;
     // LN state
     float *Y1 = nullptr, *y1 = nullptr, *DX = nullptr, *Td = nullptr, *G2 = nullptr, *g2 = nullptr;
     // LM state
@@ -174,8 +179,8 @@ int fused_has_dstep(cdlgb_ctx* c);
 void* dfwd_plan_create(cdlgb_ctx* c, int* status);
 void dfwd_plan_free(void* p);
 int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh);
+int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn, float scale);
 void* fused_dfwd(cdlgb_ctx* c);
-int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn);
 int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 
 // a scan-family scratch buffer of at least n elements (reallocated when too small)

@@ -120,19 +120,20 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
         const size_t oa = ((size_t)n * A.M + ma) * F;
         dfwd_one<N1, P, 0>(A, sb, gl, tw2, act, keep, ra, pa, oa);
         dfwd_one<N1, P, 1>(A, sb, gl, tw2, act, keep, ra, pa, oa);
-        dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, ra, pa, oa);
+        if (A.Dh) dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, ra, pa, oa);   // uniform
     }
 }
 
-// Inverse: for every (n, filter pair) the two half-spectra dh[a], dh[b] (already scaled
-// by 1/Lg) are packed into one full spectrum Z = Dh_a + i Dh_b (Z[f], and Z[Lg - f] =
+// Inverse: for every (n, filter pair) the two half-spectra dh[a], dh[b] (scaled by 1/Lg
+// as they are read) are packed into one full spectrum Z = Dh_a + i Dh_b (Z[f], and Z[Lg - f] =
 // conj(Dh_a[f]) + i conj(Dh_b[f])), inverted with the register four-step FFT, and
 // d[a] = Re, d[b] = Im written (as a C2R per filter, the imaginary parts of the
 // half-spectrum's f = 0 and f = Lg/2 bins are dropped).
 struct IArgsD {
-    const float2* Dh;     // chunk (cn, M, F)
+    const float2* Dh;     // chunk (cn, M, F), unscaled
     float* d;             // chunk (cn, M, Lg)
     const float2* tw2;
+    float scale;          // 1 / Lg, applied as the spectrum is read
     int cn, M;
 };
 
@@ -168,7 +169,9 @@ __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
         if (act) {
 #pragma unroll 5
             for (int f = gl; f < F; f += N1) {
-                const float2 a = __ldg(A.Dh + ia + f), b = __ldg(A.Dh + ia + F + f);
+                float2 a = __ldg(A.Dh + ia + f), b = __ldg(A.Dh + ia + F + f);
+                a = f2(a.x * A.scale, a.y * A.scale);
+                b = f2(b.x * A.scale, b.y * A.scale);
                 if (f == 0 || f == half) {
                     sb[f] = f2(a.x, b.x);
                 } else {
@@ -262,7 +265,8 @@ void dfwd_plan_free(void* p) {
     delete P;
 }
 
-// Y3-hat, H-hat and d-hat of sequences [n0, n0 + cn) into Yh, Hh, Dh (chunk layout).
+// Y3-hat, H-hat and d-hat of sequences [n0, n0 + cn) into Yh, Hh, Dh (chunk layout); with
+// Dh null, d-hat is not formed.
 int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh) {
     FwdPlan* P = (FwdPlan*)p;
     const size_t off = (size_t)n0 * c->M * c->Lg;
@@ -276,10 +280,11 @@ int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, 
 }
 
 // d of sequences [n0, n0 + cn) from the half-spectra Dh (chunk layout), as C2R would.
-int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn) {
+int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn, float scale) {
     FwdPlan* P = (FwdPlan*)p;
     IArgsD a;
     a.Dh = Dh; a.d = c->d + (size_t)n0 * c->M * c->Lg; a.tw2 = P->tw2; a.cn = cn; a.M = c->M;
+    a.scale = scale;
     P->ki<<<P->grid_inv, 256, P->smem, c->stream>>>(a);
     LAUNCH_CHECK(c, "k_dinv");
     return CDLGB_OK;

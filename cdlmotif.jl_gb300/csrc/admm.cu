@@ -592,7 +592,8 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     size_t b = 0;
     b += (size_t)N * L4 * 4;                    // data
     b += 7 * LMN * 4;                           // X x2, y2, y3, d, g1, g3
-    if (fused) b += (size_t)N * M * F * 8;      // the previous D-step's d-hat
+    if (fused) b += (size_t)N * M * F * 8 * 3;  // d-hat, g1-hat, g3-hat (spectral D-step)
+    if (fused) b += (size_t)dspec_slots(N, chunk_for(N, (int)M, (int)Lg)) * 3 * M * F * 8;
     b += 8 * LN * 4;                            // Y1 y1 DX Td G2 g2 + 2 scratch
     b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
     b += 2 * N * F * 8;                         // LN spectra
@@ -618,9 +619,21 @@ int admm_alloc(cdlgb_ctx* c) {
     ST_TRY(A((void**)&c->d, LMN * 4));
     ST_TRY(A((void**)&c->g1, LMN * 4));
     ST_TRY(A((void**)&c->g3, LMN * 4));
-    // the previous D-step's d-hat (fused path): (N, M, F) complex
-    if (c->fused) ST_TRY(A((void**)&c->Dhs, (size_t)c->N * c->M * c->F * 8));
+    // the previous D-step's d-hat (fused path): (N, M, F) complex; with the spectral
+    // D-step also g1-hat and g3-hat, G3-hat and the sums' spectra
+    if (c->fused) {
+        const size_t nmf = (size_t)c->N * c->M * c->F;
+        ST_TRY(A((void**)&c->Dhs, nmf * 8));
+        if (c->M <= dspec_max_m()) {
+            ST_TRY(A((void**)&c->g1h, nmf * 8));
+            ST_TRY(A((void**)&c->g3h, nmf * 8));
+            ST_TRY(A((void**)&c->G3h, (size_t)c->M * c->F * 8));
+            ST_TRY(A((void**)&c->sumspec, (size_t)3 * c->M * c->F * 8));
+        }
+    }
     c->dh_valid = 0;
+    c->dspec = 0;
+    c->time_stale = 0;
     ST_TRY(A((void**)&c->Y1, LN * 4));
     ST_TRY(A((void**)&c->y1, LN * 4));
     ST_TRY(A((void**)&c->DX, LN * 4));
@@ -640,6 +653,7 @@ int admm_alloc(cdlgb_ctx* c) {
     // cuFFT-path scratch for one chunk of sequences (init's DX, the D-step, and the
     // X-step when no fused kernel covers Lg)
     c->chunk = chunk_for(c->N, c->M, c->Lg);
+    if (c->g1h) ST_TRY(A((void**)&c->spart, dspec_part_bytes(c->M, c->F, dspec_slots(c->N, c->chunk))));
     const size_t cLMN = (size_t)c->chunk * c->M * c->Lg, cSp = (size_t)c->chunk * c->M * c->F;
     ST_TRY(A((void**)&c->sA, cLMN * 4));
     ST_TRY(A((void**)&c->sAh, cSp * 8));
@@ -660,7 +674,8 @@ void admm_free(cdlgb_ctx* c) {
                     &c->y1, &c->DX, &c->Td, &c->G2, &c->g2, &c->sU, &c->G1, &c->G3,
                     &c->dsum, &c->Dbest, &c->vbar, &c->Ah, &c->sA, &c->sB, &c->part};
     for (auto p : fl) { if (*p) cudaFree(*p); *p = nullptr; }
-    float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh, &c->Dhs};
+    float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh, &c->Dhs,
+                     &c->g1h, &c->g3h, &c->G3h, &c->spart, &c->sumspec};
     for (auto p : cl) { if (*p) cudaFree(*p); *p = nullptr; }
     if (c->dred) cudaFree(c->dred);
     if (c->dscalar) cudaFree(c->dscalar);
@@ -735,6 +750,19 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     CU_TRY(c, cudaMemsetAsync(c->g2, 0, LN * 4, s));
     CU_TRY(c, cudaMemsetAsync(c->Td, 0, LN * 4, s));
     ST_TRY(refresh_G1h(c));
+    // spectral D-step: d-hat = D-hat broadcast, g1-hat = g3-hat = 0
+    c->dspec = 0;
+    c->time_stale = 0;
+    if (c->g1h && c->fused && fused_dfwd(c) && !fused_has_dstep(c)) {
+        const char* e = getenv("CDLGB_DSPEC");
+        if (!e || atoi(e) != 0) c->dspec = 1;
+    }
+    if (c->dspec) {
+        const size_t nmf = (size_t)N * M * c->F;
+        ST_TRY(dspec_bcast(c, c->Dhs, c->G1h));
+        CU_TRY(c, cudaMemsetAsync(c->g1h, 0, nmf * 8, s));
+        CU_TRY(c, cudaMemsetAsync(c->g3h, 0, nmf * 8, s));
+    }
     // DX = real(ifft(sum_m D-hat .* X-hat)) (CDL_setup.jl:197-203); G2 = DX
     for (int n0 = 0; n0 < N; n0 += c->chunk) {
         const int cn = std::min(c->chunk, N - n0);
@@ -820,6 +848,38 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
     const int F = c->F, M = c->M, N = c->N, Lg = c->Lg;
     for (int it = 0; it < iters; ++it) {
         cdlgb_phase_begin(c, PH_DSTEP);
+        if (c->dspec) {
+            // the state in the frequency domain: only Y3 is transformed (dspec.cu)
+            k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
+            LAUNCH_CHECK(c, "k_sub");
+            ST_TRY(r2c(c, N, c->sU, c->sUh));
+            ST_TRY(r2c(c, M, c->G3, c->G3h));
+            void* fw = fused_dfwd(c);
+            int slot0 = 0;
+            for (int n0 = 0; n0 < N; n0 += c->chunk) {
+                const int cn = std::min(c->chunk, N - n0);
+                ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, nullptr, nullptr));
+                ST_TRY(dspec_launch(c, c->sAh, c->G3h, n0, n0 + cn, slot0));
+                slot0 += dspec_slots(cn, cn);
+            }
+            ST_TRY(c2r(c, N, c->sVh, c->Td));
+            k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
+                                                         c->gamma, LN, c->p.sigma);
+            LAUNCH_CHECK(c, "k_dg2");
+            // the three sums over n, back in the time domain: part as one chunk
+            ST_TRY(dspec_sums(c, c->sumspec));
+            ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part));
+            c->time_stale = 1;
+            int flen = 4 * c->p.filter_size;
+            k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
+                                                                   LM, Lg, flen, N, 1);
+            LAUNCH_CHECK(c, "k_dfinish");
+            k_dprox<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->vbar, c->G1, Lg, M, flen);
+            LAUNCH_CHECK(c, "k_dprox");
+            ST_TRY(refresh_G1h(c));
+            cdlgb_phase_end(c, PH_DSTEP);
+            continue;
+        }
         if (c->fused && fused_has_dstep(c)) {
             // transforms, solve, d, duals and G2 in one launch; then the means over n
             c->dh_valid = 0;
@@ -952,5 +1012,25 @@ int admm_code_threshold(cdlgb_ctx* c, double* thr) {
     CU_TRY(c, cudaMemcpyAsync(c->hscalar, c->dscalar, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CU_TRY(c, cudaStreamSynchronize(s));
     *thr = c->hscalar[2] * (double)c->p.std_threshold_multiplier;
+    return CDLGB_OK;
+}
+
+// d, g1, g3 in the time domain from the spectral state (for readers of those fields);
+// the spectra are copied to scratch first (the inverse transform may overwrite its input)
+int admm_sync_time_state(cdlgb_ctx* c) {
+    if (!c->dspec || !c->time_stale) return CDLGB_OK;
+    const int M = c->M, Lg = c->Lg, F = c->F;
+    const float2* src[3] = {c->Dhs, c->g1h, c->g3h};
+    float* dst[3] = {c->d, c->g1, c->g3};
+    for (int q = 0; q < 3; ++q)
+        for (int n0 = 0; n0 < c->N; n0 += c->chunk) {
+            const int cn = std::min(c->chunk, c->N - n0);
+            const size_t sp = (size_t)cn * M * F, tp = (size_t)cn * M * Lg;
+            CU_TRY(c, cudaMemcpyAsync(c->sAh, src[q] + (size_t)n0 * M * F, sp * 8,
+                                      cudaMemcpyDeviceToDevice, c->stream));
+            ST_TRY(c2r(c, (long long)M * cn, c->sAh, dst[q] + (size_t)n0 * M * Lg));
+            ST_TRY(dspec_scale(c, dst[q] + (size_t)n0 * M * Lg, tp, 1.f / (float)Lg));
+        }
+    c->time_stale = 0;
     return CDLGB_OK;
 }

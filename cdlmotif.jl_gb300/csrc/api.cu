@@ -450,6 +450,8 @@ int cdlgb_get(cdlgb_ctx* c, int32_t field, void* dst, size_t bytes) {
     }
     NEED_INIT(c);
     if (!dst) return cdlgb_seterr(c, CDLGB_EINVAL, "dst is NULL");
+    if (field == CDLGB_FIELD_D || field == CDLGB_FIELD_G1_DUAL || field == CDLGB_FIELD_G3_DUAL)
+        ST_TRY(admm_sync_time_state(c));
     const void* src = nullptr;
     size_t want = 0;
     const size_t LMN = c->LMN * 4, LN = c->LN * 4, LM = c->LM * 4;

@@ -1,0 +1,241 @@
+// The D-step with the per-sequence dictionary state held as half-spectra.
+//
+// dict_update! (src/CDL/train.jl:46-89) transforms Y3, H = (G1 - g1) + (G3 - g3) and d to
+// the frequency domain, solves per frequency, returns d to the time domain, updates the
+// duals g1 += d - G1 and g3 += d - G3 (:70, :72) and averages d + g1, d + g3 and d over
+// the sequences (:76, :83; and D_best, :91-98).  Every one of those steps after the
+// solve is linear, and nothing outside the D-step reads d, g1 or g3.  So they are kept
+// as half-spectra d-hat, g1-hat, g3-hat (N, M, F): H-hat = (G1-hat - g1-hat) +
+// (G3-hat - g3-hat) is formed per element, the dual updates are g1-hat += d-hat - G1-hat
+// and g3-hat += d-hat - G3-hat, and only the three averages -- (M, F) spectra -- are
+// returned to the time domain for the projections.  A D-step then transforms only Y3.
+// The same operations in the same order as the time-domain statements, applied to the
+// transforms; results differ from the time-domain path by FP32 rounding.
+#include "cdlgb_internal.h"
+
+namespace {
+
+__device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cfma2(float2 a, float2 b, float2 c) {   // a*b + c
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ float2 cjfma2(float2 a, float2 b, float2 c) {  // conj(a)*b + c
+    return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, c.y)));
+}
+
+struct SArgs {
+    const float2* Yh;     // scratch (c1 - c0, M, F): Y3-hat of sequences [c0, c1)
+    const float2* G1h;    // (M, F)
+    const float2* G3h;    // (M, F)
+    float2* Dh;           // (N, M, F): rfft(d_old) in, the new d-hat out
+    float2* g1h;          // (N, M, F)
+    float2* g3h;          // (N, M, F)
+    const float2* Zh;     // (N, F): rfft(G2 - g2)
+    float2* Th;           // (N, F): scale * sum_m Y3h rfft(d_old)
+    float2* part;         // (slots, 3, M, F): sums of d + g1, d + g3, d over a sub-range
+    int N, M, F, c0, c1, slot0;
+    float kd, scale;
+};
+
+constexpr int kBins = 32, kWarps = 16;
+constexpr int kSub = 64;     // sub-ranges (CTAs along y) per launch
+
+// grid (ceil(F / 32), kSub): a CTA takes 32 bins and sub-range s of the sequences
+// [c0, c1), in order, and writes that sub-range's sums to slot slot0 + s; warp w owns
+// filters w, w + 16, ...
+template <int MW>
+__global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
+    extern __shared__ float4 sm4[];
+    const int M = A.M, F = A.F;
+    const int j = blockIdx.y, cn = A.c1 - A.c0;
+    const int n0 = A.c0 + (int)((int64_t)cn * j / gridDim.y);
+    const int n1 = A.c0 + (int)((int64_t)cn * (j + 1) / gridDim.y);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int f = blockIdx.x * kBins + lane;
+    const bool on = f < F;
+    const bool edge = f == 0 || f == F - 1;
+    float2* G1s = reinterpret_cast<float2*>(sm4);          // [M][32]
+    float2* G3s = G1s + (size_t)M * kBins;                 // [M][32]
+    float* pB = reinterpret_cast<float*>(G3s + (size_t)M * kBins);   // [kWarps][32]
+    float2* pQ = reinterpret_cast<float2*>(pB + kWarps * kBins);     // [kWarps][32]
+    float2* pT = pQ + kWarps * kBins;                                // [kWarps][32]
+    for (int i = threadIdx.x; i < M * kBins; i += blockDim.x) {
+        const int m = i / kBins, ff = blockIdx.x * kBins + i % kBins;
+        G1s[i] = ff < F ? A.G1h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        G3s[i] = ff < F ? A.G3h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+    }
+    float2 s1[MW], s3[MW], sd[MW];
+#pragma unroll
+    for (int k = 0; k < MW; ++k) s1[k] = s3[k] = sd[k] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const bool live = on;                                  // lanes past F load bin 0
+    const int fl = live ? f : 0;
+    for (int n = n0; n < n1; ++n) {
+        const size_t base = (size_t)n * M * F + fl;
+        const size_t ybase = (size_t)(n - A.c0) * M * F + fl;
+        // every load of this sequence first (independent), then the arithmetic
+        float2 yv[MW], g1v[MW], g3v[MW], dv[MW];
+#pragma unroll
+        for (int k = 0; k < MW; ++k) {
+            const int m = min(w + kWarps * k, M - 1);      // in bounds; unused when m >= M
+            yv[k] = A.Yh[ybase + (size_t)m * F];
+            g1v[k] = A.g1h[base + (size_t)m * F];
+            g3v[k] = A.g3h[base + (size_t)m * F];
+            dv[k] = A.Dh[base + (size_t)m * F];
+        }
+        float2 hv[MW];
+        float B = 0.f;
+        float2 Q = make_float2(0.f, 0.f), T = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < MW; ++k) {
+            const int m = w + kWarps * k;
+            const bool use = live && m < M;
+            const int ms = use ? m : 0;
+            const float2 y = use ? yv[k] : make_float2(0.f, 0.f);
+            float2 d = use ? dv[k] : make_float2(0.f, 0.f);
+            if (edge) d.y = 0.f;
+            // H = (G1 - g1) + (G3 - g3)  (train.jl:52-54)
+            const float2 h = use ? cadd2(csub2(G1s[ms * kBins + lane], g1v[k]), csub2(G3s[ms * kBins + lane], g3v[k]))
+                                 : make_float2(0.f, 0.f);
+            hv[k] = h;
+            B = fmaf(y.x, y.x, fmaf(y.y, y.y, B));
+            Q = cfma2(y, h, Q);
+            T = cfma2(y, d, T);
+        }
+        pB[w * kBins + lane] = B;
+        pQ[w * kBins + lane] = Q;
+        pT[w * kBins + lane] = T;
+        __syncthreads();
+        B = 0.f;
+        Q = T = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int v = 0; v < kWarps; ++v) {
+            B += pB[v * kBins + lane];
+            Q = cadd2(Q, pQ[v * kBins + lane]);
+            T = cadd2(T, pT[v * kBins + lane]);
+        }
+        __syncthreads();                                   // partials read before reuse
+        if (on) {
+            const float2 z = A.Zh[(size_t)n * F + f];
+            const float inv = 1.f / (B + A.kd);
+            const float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
+            const float2 W = csub2(z, beta);
+#pragma unroll
+            for (int k = 0; k < MW; ++k) {
+                const int m = w + kWarps * k;
+                if (m >= M) continue;
+                float2 dh = cjfma2(yv[k], W, hv[k]);
+                if (edge) dh.y = 0.f;                      // the transform of a real d
+                const size_t i = (size_t)n * M * F + (size_t)m * F + f;
+                // g1 += d - G1, g3 += d - G3 with the G's before the update (train.jl:70, 72)
+                const float2 g1n = cadd2(g1v[k], csub2(dh, G1s[m * kBins + lane]));
+                const float2 g3n = cadd2(g3v[k], csub2(dh, G3s[m * kBins + lane]));
+                A.Dh[i] = dh;
+                A.g1h[i] = g1n;
+                A.g3h[i] = g3n;
+                s1[k] = cadd2(s1[k], cadd2(dh, g1n));
+                s3[k] = cadd2(s3[k], cadd2(dh, g3n));
+                sd[k] = cadd2(sd[k], dh);
+            }
+            if (w == 0) A.Th[(size_t)n * F + f] = make_float2(T.x * A.scale, T.y * A.scale);
+        }
+    }
+    if (!on) return;
+#pragma unroll
+    for (int k = 0; k < MW; ++k) {
+        const int m = w + kWarps * k;
+        if (m >= M) continue;
+        const size_t pi = (size_t)m * F + f;
+        const size_t q = (size_t)(A.slot0 + j) * 3 * M * F;
+        A.part[q + pi] = s1[k];
+        A.part[q + (size_t)M * F + pi] = s3[k];
+        A.part[q + 2 * (size_t)M * F + pi] = sd[k];
+    }
+}
+
+// out[q, m, f] = (sum over the slots, in double) / Lg: the three sums' spectra, scaled so
+// that the unnormalised inverse transform gives the time-domain sums.  Four threads per
+// output take the slots j = t mod 4 in order; the four partials are added in a fixed
+// order.
+__global__ void k_dspec_sum(const float2* __restrict__ part, float2* __restrict__ out, size_t qmf,
+                            int slots, double inv_lg) {
+    const size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t i = g >> 2;
+    const int t = (int)(g & 3);
+    double re = 0.0, im = 0.0;
+    if (i < qmf)
+        for (int j = t; j < slots; j += 4) {
+            const float2 v = part[(size_t)j * qmf + i];
+            re += v.x;
+            im += v.y;
+        }
+    // (p0 + p1) + (p2 + p3) within each group of four lanes
+    re += __shfl_down_sync(0xffffffffu, re, 1);
+    im += __shfl_down_sync(0xffffffffu, im, 1);
+    re += __shfl_down_sync(0xffffffffu, re, 2);
+    im += __shfl_down_sync(0xffffffffu, im, 2);
+    if (t == 0 && i < qmf) out[i] = make_float2((float)(re * inv_lg), (float)(im * inv_lg));
+}
+
+// broadcast of an (M, F) spectrum over n
+__global__ void k_bcast_spec(float2* __restrict__ dst, const float2* __restrict__ plane, size_t mf,
+                             size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = plane[i % mf];
+}
+
+__global__ void k_scale(float* __restrict__ x, size_t n, float s) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        x[i] *= s;
+}
+
+}  // namespace
+
+int dspec_max_m() { return kWarps * 8; }
+
+size_t dspec_part_bytes(int M, int F, int slots) { return (size_t)slots * 3 * M * F * sizeof(float2); }
+
+int dspec_slots(int N, int chunk) { return ((N + chunk - 1) / chunk) * kSub; }
+
+int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int c1, int slot0) {
+    SArgs a;
+    a.Yh = Yh; a.G1h = c->G1h; a.G3h = G3h; a.Dh = c->Dhs; a.g1h = c->g1h; a.g3h = c->g3h;
+    a.Zh = c->sUh; a.Th = c->sVh; a.part = c->spart;
+    a.N = c->N; a.M = c->M; a.F = c->F; a.c0 = c0; a.c1 = c1; a.slot0 = slot0;
+    a.kd = c->p.sherman_const_cdl; a.scale = 1.f / (float)c->Lg;
+    const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)kSub);
+    const size_t sm = (size_t)2 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * (4 + 8 + 8);
+    if (c->M <= 4 * kWarps) {
+        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k_dspec<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_dspec<4><<<g, kBins * kWarps, sm, c->stream>>>(a);
+    } else {
+        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k_dspec<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_dspec<8><<<g, kBins * kWarps, sm, c->stream>>>(a);
+    }
+    LAUNCH_CHECK(c, "k_dspec");
+    return CDLGB_OK;
+}
+
+int dspec_sums(cdlgb_ctx* c, float2* out) {
+    const size_t qmf = (size_t)3 * c->M * c->F;
+    k_dspec_sum<<<(unsigned)((4 * qmf + 255) / 256), 256, 0, c->stream>>>(
+        c->spart, out, qmf, dspec_slots(c->N, c->chunk), 1.0 / (double)c->Lg);
+    LAUNCH_CHECK(c, "k_dspec_sum");
+    return CDLGB_OK;
+}
+
+int dspec_bcast(cdlgb_ctx* c, float2* dst, const float2* plane) {
+    const size_t mf = (size_t)c->M * c->F;
+    k_bcast_spec<<<grid_for(mf * c->N, 256), 256, 0, c->stream>>>(dst, plane, mf, mf * c->N);
+    LAUNCH_CHECK(c, "k_bcast_spec");
+    return CDLGB_OK;
+}
+
+int dspec_scale(cdlgb_ctx* c, float* x, size_t n, float s) {
+    k_scale<<<grid_for(n, 256), 256, 0, c->stream>>>(x, n, s);
+    LAUNCH_CHECK(c, "k_scale");
+    return CDLGB_OK;
+}

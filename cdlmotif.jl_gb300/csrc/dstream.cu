@@ -119,8 +119,8 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
         const size_t pa = (size_t)ma * Lg + gl;
         const size_t oa = ((size_t)n * A.M + ma) * F;
         dfwd_one<N1, P, 0>(A, sb, gl, tw2, act, keep, ra, pa, oa);
-        dfwd_one<N1, P, 1>(A, sb, gl, tw2, act, keep, ra, pa, oa);
-        if (A.Dh) dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, ra, pa, oa);   // uniform
+        if (A.Hh) dfwd_one<N1, P, 1>(A, sb, gl, tw2, act, keep, ra, pa, oa);   // uniform
+        if (A.Dh) dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, ra, pa, oa);
     }
 }
 
@@ -265,8 +265,8 @@ void dfwd_plan_free(void* p) {
     delete P;
 }
 
-// Y3-hat, H-hat and d-hat of sequences [n0, n0 + cn) into Yh, Hh, Dh (chunk layout); with
-// Dh null, d-hat is not formed.
+// Y3-hat, H-hat and d-hat of sequences [n0, n0 + cn) into Yh, Hh, Dh (chunk layout); a
+// null Hh or Dh skips that transform.
 int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh) {
     FwdPlan* P = (FwdPlan*)p;
     const size_t off = (size_t)n0 * c->M * c->Lg;

@@ -13,6 +13,8 @@
 // transforms; results differ from the time-domain path by FP32 rounding.
 #include "cdlgb_internal.h"
 
+#include <cuda_pipeline_primitives.h>
+
 namespace {
 
 __device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -44,7 +46,9 @@ constexpr int kSub = 64;     // sub-ranges (CTAs along y) per launch
 // grid (ceil(F / 32), kSub): a CTA takes 32 bins and sub-range s of the sequences
 // [c0, c1), in order, and writes that sub-range's sums to slot slot0 + s; warp w owns
 // filters w, w + 16, ...
-template <int MW>
+// With PIPE, each thread's spectra of sequence n + 1 are copied to shared memory
+// (asynchronous copies, two buffers) while sequence n is computed.
+template <int MW, bool PIPE>
 __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     extern __shared__ float4 sm4[];
     const int M = A.M, F = A.F;
@@ -71,18 +75,54 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     __syncthreads();
     const bool live = on;                                  // lanes past F load bin 0
     const int fl = live ? f : 0;
+    // staging: [2][4][MW][threads], each thread's own slots
+    float2* stg = pT + kWarps * kBins;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    auto stage = [&](int n, int buf) {
+        const size_t base = (size_t)n * M * F + fl;
+        const size_t ybase = (size_t)(n - A.c0) * M * F + fl;
+#pragma unroll
+        for (int k = 0; k < MW; ++k) {
+            const int m = min(w + kWarps * k, M - 1);
+            float2* d0 = stg + ((size_t)(buf * 4 + 0) * MW + k) * nt + tid;
+            __pipeline_memcpy_async(d0, A.Yh + ybase + (size_t)m * F, sizeof(float2));
+            __pipeline_memcpy_async(d0 + (size_t)MW * nt, A.g1h + base + (size_t)m * F, sizeof(float2));
+            __pipeline_memcpy_async(d0 + (size_t)2 * MW * nt, A.g3h + base + (size_t)m * F, sizeof(float2));
+            __pipeline_memcpy_async(d0 + (size_t)3 * MW * nt, A.Dh + base + (size_t)m * F, sizeof(float2));
+        }
+        __pipeline_commit();
+    };
+    if (PIPE && n0 < n1) stage(n0, 0);
     for (int n = n0; n < n1; ++n) {
         const size_t base = (size_t)n * M * F + fl;
         const size_t ybase = (size_t)(n - A.c0) * M * F + fl;
         // every load of this sequence first (independent), then the arithmetic
         float2 yv[MW], g1v[MW], g3v[MW], dv[MW];
+        if (PIPE) {
+            if (n + 1 < n1) {
+                stage(n + 1, (n + 1 - n0) & 1);
+                __pipeline_wait_prior(1);
+            } else {
+                __pipeline_wait_prior(0);
+            }
+            const int buf = (n - n0) & 1;
 #pragma unroll
-        for (int k = 0; k < MW; ++k) {
-            const int m = min(w + kWarps * k, M - 1);      // in bounds; unused when m >= M
-            yv[k] = A.Yh[ybase + (size_t)m * F];
-            g1v[k] = A.g1h[base + (size_t)m * F];
-            g3v[k] = A.g3h[base + (size_t)m * F];
-            dv[k] = A.Dh[base + (size_t)m * F];
+            for (int k = 0; k < MW; ++k) {
+                const float2* s0 = stg + ((size_t)(buf * 4 + 0) * MW + k) * nt + tid;
+                yv[k] = s0[0];
+                g1v[k] = s0[(size_t)MW * nt];
+                g3v[k] = s0[(size_t)2 * MW * nt];
+                dv[k] = s0[(size_t)3 * MW * nt];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < MW; ++k) {
+                const int m = min(w + kWarps * k, M - 1);  // in bounds; unused when m >= M
+                yv[k] = A.Yh[ybase + (size_t)m * F];
+                g1v[k] = A.g1h[base + (size_t)m * F];
+                g3v[k] = A.g3h[base + (size_t)m * F];
+                dv[k] = A.Dh[base + (size_t)m * F];
+            }
         }
         float2 hv[MW];
         float B = 0.f;
@@ -209,11 +249,13 @@ int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int 
     const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)kSub);
     const size_t sm = (size_t)2 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * (4 + 8 + 8);
     if (c->M <= 4 * kWarps) {
-        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k_dspec<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_dspec<4><<<g, kBins * kWarps, sm, c->stream>>>(a);
+        // + the two staging buffers: 2 x 4 spectra x 4 filters x 512 threads
+        const size_t smp = sm + (size_t)2 * 4 * 4 * kBins * kWarps * sizeof(float2);
+        CU_TRY(c, cudaFuncSetAttribute(k_dspec<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smp));
+        k_dspec<4, true><<<g, kBins * kWarps, smp, c->stream>>>(a);
     } else {
-        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k_dspec<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_dspec<8><<<g, kBins * kWarps, sm, c->stream>>>(a);
+        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k_dspec<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k_dspec<8, false><<<g, kBins * kWarps, sm, c->stream>>>(a);
     }
     LAUNCH_CHECK(c, "k_dspec");
     return CDLGB_OK;

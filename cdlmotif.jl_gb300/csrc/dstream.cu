@@ -62,8 +62,10 @@ __device__ __forceinline__ void dfwd_one(const FArgs& A, float2* sb, int gl, con
             const int o = N1 * n2;
             float2 v;
             if (WHICH == 0) {
-                v = keep ? f2(__ldg(A.X + ra + o) + __ldg(A.y3 + ra + o),
-                              __ldg(A.X + ra + Lg + o) + __ldg(A.y3 + ra + Lg + o))
+                // Y3 = X + y3 on the kept rows.  Every X-step leaves y3 = +0 exactly there
+                // (projectionX! keeps X + y3, so y3' = (y3 + X) - Y3 is set to +0, as
+                // initialisation does), so X + 0 gives the same bits without reading y3.
+                v = keep ? f2(__ldg(A.X + ra + o) + 0.f, __ldg(A.X + ra + Lg + o) + 0.f)
                          : f2(0.f, 0.f);
             } else if (WHICH == 1) {
                 v = f2((__ldg(A.G1 + pa + o) - __ldg(A.g1 + ra + o)) + (__ldg(A.G3 + pa + o) - __ldg(A.g3 + ra + o)),

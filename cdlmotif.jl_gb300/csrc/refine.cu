@@ -133,12 +133,12 @@ __global__ void __launch_bounds__(512) k_extend(ExtArgs A) {
     // its own copy, so num_included stays len_pos.
     const int lowb = (int)floorf(__fmul_rn(A.perc, (float)nkeys));
     // A terminating loop takes at most L columns per side (past that no sequence has a
-    // column in range); beyond 2L + 4 rounds the reference would loop for ever.
-    const int max_rounds = 2 * A.L + 4;
+    // column in range); beyond 2L + 4 passes the reference would loop for ever.
+    const int max_passes = 2 * A.L + 4;
     int dec = 0, inc = 0, status = EXT_OK;
     bool el = true, er = true;
-    for (int round = 0;; ++round) {
-        if (round >= max_rounds) { status = EXT_ENDLESS; break; }
+    for (int pass = 0;; ++pass) {
+        if (pass >= max_passes) { status = EXT_ENDLESS; break; }
         for (int side = 0; side < 2; ++side) {
             const bool right = side == 1;
             if (!(right ? er : el)) continue;

@@ -304,7 +304,7 @@ def extension(data: np.ndarray, pos_col, mlen: int, comp_col, bg=(0.25,) * 4, ps
     key; comp_col (N,) use_comp flags or None.  Returns (new pos_col, new length,
     dec, inc).  The reference's num_included is decremented only inside
     explore_sides! (a local copy), so the usage bound of :74 / :165 compares the
-    unchanged entry count.  Raises RuntimeError after 2L + 4 rounds (the reference
+    unchanged entry count.  Raises RuntimeError after 2L + 4 passes (the reference
     does not return then) and KeyError where dummy_comp does."""
     N, L4 = data.shape
     L = L4 // 4
@@ -343,10 +343,10 @@ def extension(data: np.ndarray, pos_col, mlen: int, comp_col, bg=(0.25,) * 4, ps
         col = ((this_col + ps).astype(f32) / f32(tot + f32(f32(4) * ps))).astype(f32)
         return ic_col_single(col, bg), to_exclude
 
-    rounds = 0
+    passes = 0
     while True:
-        rounds += 1
-        if rounds > 2 * L + 4:
+        passes += 1
+        if passes > 2 * L + 4:
             raise RuntimeError("extension does not terminate")
         if explore_left:
             ic, ex = explore_sides(dec + 1, False)

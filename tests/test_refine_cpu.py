@@ -61,9 +61,9 @@ def test_ic_column_values():
 
 
 def test_extension_known_answer_with_exclusion():
-    """Round 1: left column 4 counts A x5 (sequence 0 has no column 0 and is dropped when
-    the column is accepted): IC 0.078 > 0.075, dec = 1.  Right column 8 over the five
-    remaining: (2,1,1,1), stop.  Round 2: left column 3 (2,1,1,1), stop."""
+    """Loop pass 1: left column 4 counts A x5 (sequence 0 has no column 0 and is dropped
+    when the column is accepted): IC 0.078 > 0.075, dec = 1.  Right column 8 over the
+    five remaining: (2,1,1,1), stop.  Pass 2: left column 3 (2,1,1,1), stop."""
     S = kat_data()
     pos = np.array([1, 5, 5, 5, 5, 5], np.int32)
     new, ln, dec, inc = SO.extension(S, pos, 3, None)
@@ -74,7 +74,7 @@ def test_extension_known_answer_with_exclusion():
 def test_extension_usage_bound_never_fires():
     """Reference quirk: num_included is decremented only in explore_sides!'s copy, so
     after sequence 0 is dropped (5 of 6 left, usage bound floor(0.95 * 6) = 5) the loop
-    still runs: column 3 = C x5 is accepted in round 2 (dec = 2); column 2 (all G) is
+    still runs: column 3 = C x5 is accepted in pass 2 (dec = 2); column 2 (all G) is
     then scored (0,0,5,0): IC 0.078, accepted too; column 1 (all G) likewise, and the
     next left column is out of range for every sequence: the empty column scores 0."""
     S = kat_data(col3="CCCCC")
@@ -86,8 +86,8 @@ def test_extension_usage_bound_never_fires():
 
 def test_extension_known_answer_reverse_complement():
     """Sequence 0 is a reverse-complemented entry at position 5: its left column is 8
-    (T, complemented A), so round 1 left counts A x6 (IC 0.103), dec = 1; its right
-    column is 4 (G -> C): (2,2,1,1), stop; round 2 left: its column 9 (A -> T) with
+    (T, complemented A), so pass 1 left counts A x6 (IC 0.103), dec = 1; its right
+    column is 4 (G -> C): (2,2,1,1), stop; pass 2 left: its column 9 (A -> T) with
     A C G T A: (2,1,1,2), stop.  New starts: p - dec forward, p - inc (= 5) complemented."""
     S = kat_data(comp_seq0=True)
     pos = np.array([5, 5, 5, 5, 5, 5], np.int32)

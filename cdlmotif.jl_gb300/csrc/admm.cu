@@ -592,7 +592,7 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     size_t b = 0;
     b += (size_t)N * L4 * 4;                    // data
     b += 7 * LMN * 4;                           // X x2, y2, y3, d, g1, g3
-    if (fused) b += (size_t)N * M * F * 8 * 3;  // d-hat, g1-hat, g3-hat (spectral D-step)
+    if (fused) b += (size_t)N * M * F * 8 * 2;  // d-hat, g1-hat (spectral D-step)
     if (fused) b += (size_t)dspec_slots(N, chunk_for(N, (int)M, (int)Lg)) * 3 * M * F * 8;
     b += 8 * LN * 4;                            // Y1 y1 DX Td G2 g2 + 2 scratch
     b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
@@ -626,7 +626,7 @@ int admm_alloc(cdlgb_ctx* c) {
         ST_TRY(A((void**)&c->Dhs, nmf * 8));
         if (c->M <= dspec_max_m()) {
             ST_TRY(A((void**)&c->g1h, nmf * 8));
-            ST_TRY(A((void**)&c->g3h, nmf * 8));
+            ST_TRY(A((void**)&c->Dg, (size_t)c->M * c->F * 8));
             ST_TRY(A((void**)&c->G3h, (size_t)c->M * c->F * 8));
             ST_TRY(A((void**)&c->sumspec, (size_t)3 * c->M * c->F * 8));
         }
@@ -675,7 +675,7 @@ void admm_free(cdlgb_ctx* c) {
                     &c->dsum, &c->Dbest, &c->vbar, &c->Ah, &c->sA, &c->sB, &c->part};
     for (auto p : fl) { if (*p) cudaFree(*p); *p = nullptr; }
     float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh, &c->Dhs,
-                     &c->g1h, &c->g3h, &c->G3h, &c->spart, &c->sumspec};
+                     &c->g1h, &c->Dg, &c->G3h, &c->spart, &c->sumspec};
     for (auto p : cl) { if (*p) cudaFree(*p); *p = nullptr; }
     if (c->dred) cudaFree(c->dred);
     if (c->dscalar) cudaFree(c->dscalar);
@@ -761,7 +761,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
         const size_t nmf = (size_t)N * M * c->F;
         ST_TRY(dspec_bcast(c, c->Dhs, c->G1h));
         CU_TRY(c, cudaMemsetAsync(c->g1h, 0, nmf * 8, s));
-        CU_TRY(c, cudaMemsetAsync(c->g3h, 0, nmf * 8, s));
+        CU_TRY(c, cudaMemsetAsync(c->Dg, 0, (size_t)M * c->F * 8, s));
     }
     // DX = real(ifft(sum_m D-hat .* X-hat)) (CDL_setup.jl:197-203); G2 = DX
     for (int n0 = 0; n0 < N; n0 += c->chunk) {
@@ -867,7 +867,7 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                                                          c->gamma, LN, c->p.sigma);
             LAUNCH_CHECK(c, "k_dg2");
             // the three sums over n, back in the time domain: part as one chunk
-            ST_TRY(dspec_sums(c, c->sumspec));
+            ST_TRY(dspec_sums(c, c->G3h, c->sumspec));
             ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part));
             c->time_stale = 1;
             int flen = 4 * c->p.filter_size;
@@ -1020,14 +1020,18 @@ int admm_code_threshold(cdlgb_ctx* c, double* thr) {
 int admm_sync_time_state(cdlgb_ctx* c) {
     if (!c->dspec || !c->time_stale) return CDLGB_OK;
     const int M = c->M, Lg = c->Lg, F = c->F;
-    const float2* src[3] = {c->Dhs, c->g1h, c->g3h};
+    const float2* src[3] = {c->Dhs, c->g1h, c->g1h};
     float* dst[3] = {c->d, c->g1, c->g3};
     for (int q = 0; q < 3; ++q)
         for (int n0 = 0; n0 < c->N; n0 += c->chunk) {
             const int cn = std::min(c->chunk, c->N - n0);
             const size_t sp = (size_t)cn * M * F, tp = (size_t)cn * M * Lg;
-            CU_TRY(c, cudaMemcpyAsync(c->sAh, src[q] + (size_t)n0 * M * F, sp * 8,
-                                      cudaMemcpyDeviceToDevice, c->stream));
+            const float2* sq = src[q] + (size_t)n0 * M * F;
+            if (q == 2) {
+                ST_TRY(dspec_g3(c, c->sAh, sq, (size_t)cn * M));       // g3 = g1 - Dg
+            } else {
+                CU_TRY(c, cudaMemcpyAsync(c->sAh, sq, sp * 8, cudaMemcpyDeviceToDevice, c->stream));
+            }
             ST_TRY(c2r(c, (long long)M * cn, c->sAh, dst[q] + (size_t)n0 * M * Lg));
             ST_TRY(dspec_scale(c, dst[q] + (size_t)n0 * M * Lg, tp, 1.f / (float)Lg));
         }

@@ -54,10 +54,11 @@ struct cdlgb_ctx {
     // initialisation and the other D-step paths clear it)
     float2* Dhs = nullptr;
     int dh_valid = 0;
-    // spectral D-step state (dspec.cu): with dspec set, d-hat (Dhs), g1-hat and g3-hat
-    // are the dictionary state and d, g1, g3 are refreshed from them on demand
-    // (time_stale); G3-hat, the per-chunk sums and their total are scratch
-    float2 *g1h = nullptr, *g3h = nullptr, *G3h = nullptr, *spart = nullptr, *sumspec = nullptr;
+    // spectral D-step state (dspec.cu): with dspec set, d-hat (Dhs), g1-hat (N, M, F) and
+    // Dg = g1-hat - g3-hat (M, F, the same for every sequence) are the dictionary state
+    // and d, g1, g3 are refreshed from them on demand (time_stale); G3-hat, the per-range
+    // sums and their total are scratch
+    float2 *g1h = nullptr, *Dg = nullptr, *G3h = nullptr, *spart = nullptr, *sumspec = nullptr;
     int dspec = 0, time_stale = 0;
     // LN state
     float *Y1 = nullptr, *y1 = nullptr, *DX = nullptr, *Td = nullptr, *G2 = nullptr, *g2 = nullptr;
@@ -216,7 +217,8 @@ int dspec_max_m();
 size_t dspec_part_bytes(int M, int F, int slots);
 int dspec_slots(int N, int chunk);
 int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int c1, int slot0);
-int dspec_sums(cdlgb_ctx* c, float2* out);
+int dspec_sums(cdlgb_ctx* c, const float2* G3h, float2* out);
+int dspec_g3(cdlgb_ctx* c, float2* dst, const float2* g1h, size_t rows);
 int dspec_bcast(cdlgb_ctx* c, float2* dst, const float2* plane);
 int dspec_scale(cdlgb_ctx* c, float* x, size_t n, float s);
 int admm_sync_time_state(cdlgb_ctx* c);

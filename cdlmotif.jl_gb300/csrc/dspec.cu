@@ -5,12 +5,16 @@
 // duals g1 += d - G1 and g3 += d - G3 (:70, :72) and averages d + g1, d + g3 and d over
 // the sequences (:76, :83; and D_best, :91-98).  Every one of those steps after the
 // solve is linear, and nothing outside the D-step reads d, g1 or g3.  So they are kept
-// as half-spectra d-hat, g1-hat, g3-hat (N, M, F): H-hat = (G1-hat - g1-hat) +
-// (G3-hat - g3-hat) is formed per element, the dual updates are g1-hat += d-hat - G1-hat
-// and g3-hat += d-hat - G3-hat, and only the three averages -- (M, F) spectra -- are
-// returned to the time domain for the projections.  A D-step then transforms only Y3.
-// The same operations in the same order as the time-domain statements, applied to the
-// transforms; results differ from the time-domain path by FP32 rounding.
+// as half-spectra, with one more reduction:
+//   * g1 and g3 start at zero and both receive the same d; their difference changes by
+//     G3 - G1, the same for every sequence.  So g1 - g3 is one (M, F) spectrum Dg shared
+//     by all sequences, and g3 = g1 - Dg: only d-hat and g1-hat are per sequence;
+//   * H-hat = (G1-hat - g1-hat) + (G3-hat - g3-hat) with g3-hat = g1-hat - Dg, the duals
+//     g1-hat += d-hat - G1-hat and Dg += G3-hat - G1-hat, and the averages of d + g1 and
+//     d (that of d + g3 is the first minus Dg) are (M, F) spectra, returned to the time
+//     domain once per D-step for the projections.  A D-step then transforms only Y3.
+// The reference's statements applied to the transforms, with g3 recovered from the
+// shared difference; results differ from the time-domain path by FP32 rounding.
 #include "cdlgb_internal.h"
 
 #include <cuda_pipeline_primitives.h>
@@ -30,24 +34,24 @@ struct SArgs {
     const float2* Yh;     // scratch (c1 - c0, M, F): Y3-hat of sequences [c0, c1)
     const float2* G1h;    // (M, F)
     const float2* G3h;    // (M, F)
+    const float2* Dg;     // (M, F): g1-hat - g3-hat, the same for every sequence
     float2* Dh;           // (N, M, F): rfft(d_old) in, the new d-hat out
     float2* g1h;          // (N, M, F)
-    float2* g3h;          // (N, M, F)
     const float2* Zh;     // (N, F): rfft(G2 - g2)
     float2* Th;           // (N, F): scale * sum_m Y3h rfft(d_old)
-    float2* part;         // (slots, 3, M, F): sums of d + g1, d + g3, d over a sub-range
+    float2* part;         // (slots, 2, M, F): sums of d + g1 and of d over a sub-range
     int N, M, F, c0, c1, slot0;
     float kd, scale;
 };
 
 constexpr int kBins = 32, kWarps = 16;
 constexpr int kSub = 64;     // sub-ranges (CTAs along y) per launch
+constexpr int kArr = 3;      // staged spectra: Y3-hat, g1-hat, d-hat
 
 // grid (ceil(F / 32), kSub): a CTA takes 32 bins and sub-range s of the sequences
 // [c0, c1), in order, and writes that sub-range's sums to slot slot0 + s; warp w owns
-// filters w, w + 16, ...
-// With PIPE, each thread's spectra of sequence n + 1 are copied to shared memory
-// (asynchronous copies, two buffers) while sequence n is computed.
+// filters w, w + 16, ...  With PIPE, each thread's spectra of sequence n + 1 are copied
+// to shared memory (asynchronous copies, two buffers) while sequence n is computed.
 template <int MW, bool PIPE>
 __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     extern __shared__ float4 sm4[];
@@ -61,21 +65,23 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     const bool edge = f == 0 || f == F - 1;
     float2* G1s = reinterpret_cast<float2*>(sm4);          // [M][32]
     float2* G3s = G1s + (size_t)M * kBins;                 // [M][32]
-    float* pB = reinterpret_cast<float*>(G3s + (size_t)M * kBins);   // [kWarps][32]
+    float2* Dgs = G3s + (size_t)M * kBins;                 // [M][32]
+    float* pB = reinterpret_cast<float*>(Dgs + (size_t)M * kBins);   // [kWarps][32]
     float2* pQ = reinterpret_cast<float2*>(pB + kWarps * kBins);     // [kWarps][32]
     float2* pT = pQ + kWarps * kBins;                                // [kWarps][32]
     for (int i = threadIdx.x; i < M * kBins; i += blockDim.x) {
         const int m = i / kBins, ff = blockIdx.x * kBins + i % kBins;
-        G1s[i] = ff < F ? A.G1h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
-        G3s[i] = ff < F ? A.G3h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        const bool in = ff < F;
+        G1s[i] = in ? A.G1h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        G3s[i] = in ? A.G3h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        Dgs[i] = in ? A.Dg[(size_t)m * F + ff] : make_float2(0.f, 0.f);
     }
-    float2 s1[MW], s3[MW], sd[MW];
+    float2 s1[MW], sd[MW];
 #pragma unroll
-    for (int k = 0; k < MW; ++k) s1[k] = s3[k] = sd[k] = make_float2(0.f, 0.f);
+    for (int k = 0; k < MW; ++k) s1[k] = sd[k] = make_float2(0.f, 0.f);
     __syncthreads();
-    const bool live = on;                                  // lanes past F load bin 0
-    const int fl = live ? f : 0;
-    // staging: [2][4][MW][threads], each thread's own slots
+    const int fl = on ? f : 0;                             // lanes past F load bin 0
+    // staging: [2][kArr][MW][threads], each thread's own slots
     float2* stg = pT + kWarps * kBins;
     const int nt = blockDim.x, tid = threadIdx.x;
     auto stage = [&](int n, int buf) {
@@ -84,20 +90,17 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
 #pragma unroll
         for (int k = 0; k < MW; ++k) {
             const int m = min(w + kWarps * k, M - 1);
-            float2* d0 = stg + ((size_t)(buf * 4 + 0) * MW + k) * nt + tid;
+            float2* d0 = stg + ((size_t)(buf * kArr + 0) * MW + k) * nt + tid;
             __pipeline_memcpy_async(d0, A.Yh + ybase + (size_t)m * F, sizeof(float2));
             __pipeline_memcpy_async(d0 + (size_t)MW * nt, A.g1h + base + (size_t)m * F, sizeof(float2));
-            __pipeline_memcpy_async(d0 + (size_t)2 * MW * nt, A.g3h + base + (size_t)m * F, sizeof(float2));
-            __pipeline_memcpy_async(d0 + (size_t)3 * MW * nt, A.Dh + base + (size_t)m * F, sizeof(float2));
+            __pipeline_memcpy_async(d0 + (size_t)2 * MW * nt, A.Dh + base + (size_t)m * F, sizeof(float2));
         }
         __pipeline_commit();
     };
     if (PIPE && n0 < n1) stage(n0, 0);
     for (int n = n0; n < n1; ++n) {
-        const size_t base = (size_t)n * M * F + fl;
-        const size_t ybase = (size_t)(n - A.c0) * M * F + fl;
         // every load of this sequence first (independent), then the arithmetic
-        float2 yv[MW], g1v[MW], g3v[MW], dv[MW];
+        float2 yv[MW], g1v[MW], dv[MW];
         if (PIPE) {
             if (n + 1 < n1) {
                 stage(n + 1, (n + 1 - n0) & 1);
@@ -108,19 +111,19 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             const int buf = (n - n0) & 1;
 #pragma unroll
             for (int k = 0; k < MW; ++k) {
-                const float2* s0 = stg + ((size_t)(buf * 4 + 0) * MW + k) * nt + tid;
+                const float2* s0 = stg + ((size_t)(buf * kArr + 0) * MW + k) * nt + tid;
                 yv[k] = s0[0];
                 g1v[k] = s0[(size_t)MW * nt];
-                g3v[k] = s0[(size_t)2 * MW * nt];
-                dv[k] = s0[(size_t)3 * MW * nt];
+                dv[k] = s0[(size_t)2 * MW * nt];
             }
         } else {
+            const size_t base = (size_t)n * M * F + fl;
+            const size_t ybase = (size_t)(n - A.c0) * M * F + fl;
 #pragma unroll
             for (int k = 0; k < MW; ++k) {
                 const int m = min(w + kWarps * k, M - 1);  // in bounds; unused when m >= M
                 yv[k] = A.Yh[ybase + (size_t)m * F];
                 g1v[k] = A.g1h[base + (size_t)m * F];
-                g3v[k] = A.g3h[base + (size_t)m * F];
                 dv[k] = A.Dh[base + (size_t)m * F];
             }
         }
@@ -130,13 +133,14 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
 #pragma unroll
         for (int k = 0; k < MW; ++k) {
             const int m = w + kWarps * k;
-            const bool use = live && m < M;
+            const bool use = on && m < M;
             const int ms = use ? m : 0;
             const float2 y = use ? yv[k] : make_float2(0.f, 0.f);
             float2 d = use ? dv[k] : make_float2(0.f, 0.f);
             if (edge) d.y = 0.f;
-            // H = (G1 - g1) + (G3 - g3)  (train.jl:52-54)
-            const float2 h = use ? cadd2(csub2(G1s[ms * kBins + lane], g1v[k]), csub2(G3s[ms * kBins + lane], g3v[k]))
+            // H = (G1 - g1) + (G3 - g3) with g3 = g1 - Dg  (train.jl:52-54)
+            const float2 g3 = csub2(g1v[k], Dgs[ms * kBins + lane]);
+            const float2 h = use ? cadd2(csub2(G1s[ms * kBins + lane], g1v[k]), csub2(G3s[ms * kBins + lane], g3))
                                  : make_float2(0.f, 0.f);
             hv[k] = h;
             B = fmaf(y.x, y.x, fmaf(y.y, y.y, B));
@@ -168,14 +172,11 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
                 float2 dh = cjfma2(yv[k], W, hv[k]);
                 if (edge) dh.y = 0.f;                      // the transform of a real d
                 const size_t i = (size_t)n * M * F + (size_t)m * F + f;
-                // g1 += d - G1, g3 += d - G3 with the G's before the update (train.jl:70, 72)
+                // g1 += d - G1 with G1 before the update (train.jl:70)
                 const float2 g1n = cadd2(g1v[k], csub2(dh, G1s[m * kBins + lane]));
-                const float2 g3n = cadd2(g3v[k], csub2(dh, G3s[m * kBins + lane]));
                 A.Dh[i] = dh;
                 A.g1h[i] = g1n;
-                A.g3h[i] = g3n;
                 s1[k] = cadd2(s1[k], cadd2(dh, g1n));
-                s3[k] = cadd2(s3[k], cadd2(dh, g3n));
                 sd[k] = cadd2(sd[k], dh);
             }
             if (w == 0) A.Th[(size_t)n * F + f] = make_float2(T.x * A.scale, T.y * A.scale);
@@ -187,35 +188,50 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
         const int m = w + kWarps * k;
         if (m >= M) continue;
         const size_t pi = (size_t)m * F + f;
-        const size_t q = (size_t)(A.slot0 + j) * 3 * M * F;
+        const size_t q = (size_t)(A.slot0 + j) * 2 * M * F;
         A.part[q + pi] = s1[k];
-        A.part[q + (size_t)M * F + pi] = s3[k];
-        A.part[q + 2 * (size_t)M * F + pi] = sd[k];
+        A.part[q + (size_t)M * F + pi] = sd[k];
     }
 }
 
-// out[q, m, f] = (sum over the slots, in double) / Lg: the three sums' spectra, scaled so
-// that the unnormalised inverse transform gives the time-domain sums.  Four threads per
-// output take the slots j = t mod 4 in order; the four partials are added in a fixed
-// order.
-__global__ void k_dspec_sum(const float2* __restrict__ part, float2* __restrict__ out, size_t qmf,
-                            int slots, double inv_lg) {
+// The three sums' spectra, scaled by 1/Lg so that the unnormalised inverse transform
+// gives the time-domain sums: out[0] = sum (d + g1), out[2] = sum d (over the slots, in
+// double), out[1] = sum (d + g3) = out[0] - N Dg (Dg after this D-step's update).  Four
+// threads per output take the slots j = t mod 4 in order; the four partials are added in
+// a fixed order.
+__global__ void k_dspec_sum(const float2* __restrict__ part, const float2* __restrict__ Dg,
+                            float2* __restrict__ out, size_t mf, int slots, int N, double inv_lg) {
     const size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const size_t i = g >> 2;
+    const size_t i = g >> 2;                                // 0 .. 2 mf - 1
     const int t = (int)(g & 3);
     double re = 0.0, im = 0.0;
-    if (i < qmf)
+    if (i < 2 * mf)
         for (int j = t; j < slots; j += 4) {
-            const float2 v = part[(size_t)j * qmf + i];
+            const float2 v = part[(size_t)j * 2 * mf + i];
             re += v.x;
             im += v.y;
         }
-    // (p0 + p1) + (p2 + p3) within each group of four lanes
     re += __shfl_down_sync(0xffffffffu, re, 1);
     im += __shfl_down_sync(0xffffffffu, im, 1);
     re += __shfl_down_sync(0xffffffffu, re, 2);
     im += __shfl_down_sync(0xffffffffu, im, 2);
-    if (t == 0 && i < qmf) out[i] = make_float2((float)(re * inv_lg), (float)(im * inv_lg));
+    if (t != 0 || i >= 2 * mf) return;
+    if (i < mf) {
+        out[i] = make_float2((float)(re * inv_lg), (float)(im * inv_lg));
+        const float2 dg = Dg[i];
+        out[mf + i] = make_float2((float)((re - (double)N * dg.x) * inv_lg),
+                                  (float)((im - (double)N * dg.y) * inv_lg));
+    } else {
+        out[mf + i] = make_float2((float)(re * inv_lg), (float)(im * inv_lg));
+    }
+}
+
+// Dg += G3-hat - G1-hat (the change of g1 - g3 in one D-step, train.jl:70, 72)
+__global__ void k_dg_update(float2* __restrict__ Dg, const float2* __restrict__ G1h,
+                            const float2* __restrict__ G3h, size_t mf) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= mf) return;
+    Dg[i] = cadd2(Dg[i], csub2(G3h[i], G1h[i]));
 }
 
 // broadcast of an (M, F) spectrum over n
@@ -224,6 +240,14 @@ __global__ void k_bcast_spec(float2* __restrict__ dst, const float2* __restrict_
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x)
         dst[i] = plane[i % mf];
+}
+
+// dst = a - plane, the plane broadcast over n (g3-hat = g1-hat - Dg)
+__global__ void k_sub_bcast(float2* __restrict__ dst, const float2* __restrict__ a,
+                            const float2* __restrict__ plane, size_t mf, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = csub2(a[i], plane[i % mf]);
 }
 
 __global__ void k_scale(float* __restrict__ x, size_t n, float s) {
@@ -236,21 +260,21 @@ __global__ void k_scale(float* __restrict__ x, size_t n, float s) {
 
 int dspec_max_m() { return kWarps * 8; }
 
-size_t dspec_part_bytes(int M, int F, int slots) { return (size_t)slots * 3 * M * F * sizeof(float2); }
+size_t dspec_part_bytes(int M, int F, int slots) { return (size_t)slots * 2 * M * F * sizeof(float2); }
 
 int dspec_slots(int N, int chunk) { return ((N + chunk - 1) / chunk) * kSub; }
 
 int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int c1, int slot0) {
     SArgs a;
-    a.Yh = Yh; a.G1h = c->G1h; a.G3h = G3h; a.Dh = c->Dhs; a.g1h = c->g1h; a.g3h = c->g3h;
+    a.Yh = Yh; a.G1h = c->G1h; a.G3h = G3h; a.Dg = c->Dg; a.Dh = c->Dhs; a.g1h = c->g1h;
     a.Zh = c->sUh; a.Th = c->sVh; a.part = c->spart;
     a.N = c->N; a.M = c->M; a.F = c->F; a.c0 = c0; a.c1 = c1; a.slot0 = slot0;
     a.kd = c->p.sherman_const_cdl; a.scale = 1.f / (float)c->Lg;
     const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)kSub);
-    const size_t sm = (size_t)2 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * (4 + 8 + 8);
+    const size_t sm = (size_t)3 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * (4 + 8 + 8);
     if (c->M <= 4 * kWarps) {
-        // + the two staging buffers: 2 x 4 spectra x 4 filters x 512 threads
-        const size_t smp = sm + (size_t)2 * 4 * 4 * kBins * kWarps * sizeof(float2);
+        // + the two staging buffers: 2 x 3 spectra x 4 filters x 512 threads
+        const size_t smp = sm + (size_t)2 * kArr * 4 * kBins * kWarps * sizeof(float2);
         CU_TRY(c, cudaFuncSetAttribute(k_dspec<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smp));
         k_dspec<4, true><<<g, kBins * kWarps, smp, c->stream>>>(a);
     } else {
@@ -261,10 +285,13 @@ int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int 
     return CDLGB_OK;
 }
 
-int dspec_sums(cdlgb_ctx* c, float2* out) {
-    const size_t qmf = (size_t)3 * c->M * c->F;
-    k_dspec_sum<<<(unsigned)((4 * qmf + 255) / 256), 256, 0, c->stream>>>(
-        c->spart, out, qmf, dspec_slots(c->N, c->chunk), 1.0 / (double)c->Lg);
+// the Dg update (after every chunk has used the old Dg) and the three sums: out (3, M, F)
+int dspec_sums(cdlgb_ctx* c, const float2* G3h, float2* out) {
+    const size_t mf = (size_t)c->M * c->F;
+    k_dg_update<<<(unsigned)((mf + 255) / 256), 256, 0, c->stream>>>(c->Dg, c->G1h, G3h, mf);
+    LAUNCH_CHECK(c, "k_dg_update");
+    k_dspec_sum<<<(unsigned)((4 * 2 * mf + 255) / 256), 256, 0, c->stream>>>(
+        c->spart, c->Dg, out, mf, dspec_slots(c->N, c->chunk), c->N, 1.0 / (double)c->Lg);
     LAUNCH_CHECK(c, "k_dspec_sum");
     return CDLGB_OK;
 }
@@ -273,6 +300,14 @@ int dspec_bcast(cdlgb_ctx* c, float2* dst, const float2* plane) {
     const size_t mf = (size_t)c->M * c->F;
     k_bcast_spec<<<grid_for(mf * c->N, 256), 256, 0, c->stream>>>(dst, plane, mf, mf * c->N);
     LAUNCH_CHECK(c, "k_bcast_spec");
+    return CDLGB_OK;
+}
+
+// g3-hat of rows (sequence x filter) [0, rows) of g1h into dst
+int dspec_g3(cdlgb_ctx* c, float2* dst, const float2* g1h, size_t rows) {
+    const size_t mf = (size_t)c->M * c->F;
+    k_sub_bcast<<<grid_for(rows * c->F, 256), 256, 0, c->stream>>>(dst, g1h, c->Dg, mf, rows * c->F);
+    LAUNCH_CHECK(c, "k_sub_bcast");
     return CDLGB_OK;
 }
 

@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
         // the HBM loads need no register array)
         if (pair) {
             const size_t ra = ((size_t)n * M + m0 + 2 * grp) * Lg + gl;
-#pragma unroll 4
+#pragma unroll 16
             for (int n2 = 0; n2 < P; ++n2) {
                 const int o = N1 * n2;
                 float2 a2 = f2(A.y2[ra + o], A.y2[ra + Lg + o]);
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
             for (int t = gl; t < A.L4; t += N1) Ss[t] = A.S[(size_t)n * A.L4 + t];
             __syncwarp(gmask);
             const size_t r = (size_t)n * Lg + gl;
-#pragma unroll 4
+#pragma unroll 16
             for (int n2 = 0; n2 < P; ++n2) {
                 const int o = N1 * n2;
                 const float Yv = A.Y1[r + o], yv = A.y1[r + o], dv = A.DX[r + o];

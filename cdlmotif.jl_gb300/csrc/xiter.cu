@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
             if (act) inv_step1<N1, P, true>(sb, gl, tw2);   // X (or DX) at T[n2][gl], l = gl + N1 n2
             if (pair) {
                 if (!last) {
-#pragma unroll 4
+#pragma unroll 8
                     for (int n2 = 0; n2 < P; ++n2) {
                         const int o = N1 * n2;
                         const int o3 = W3 * n2;
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                 // DX, then Y1 = (W'S + rho (DX + y1')) / (W'W + rho)  (update_Y1!,
                 // csc_kernels.jl:86-95), then the next iteration's y1' and U
                 const size_t r = (size_t)n * Lg + gl;
-#pragma unroll 4
+#pragma unroll 8
                 for (int n2 = 0; n2 < P; ++n2) {
                     const int o = N1 * n2;
                     const int l = gl + o;

@@ -57,7 +57,7 @@ __device__ __forceinline__ void dfwd_one(const FArgs& A, float2* sb, int gl, con
     constexpr int RS = N1 + 1;
     constexpr int F = Lg / 2 + 1;
     if (act) {
-#pragma unroll 8
+#pragma unroll 16
         for (int n2 = 0; n2 < P; ++n2) {
             const int o = N1 * n2;
             float2 v;

@@ -573,6 +573,27 @@ int chunk_for(int N, int M, int Lg) {
     return (int)ch;
 }
 
+// Sequences per chunk of the spectral D-step: its only scratch is the Y3 half-spectra
+// (M x F complex per sequence), so a chunk covers up to 6 GB of them (the whole dataset
+// at N = 20000, L = 200, K = 64), never fewer than the cuFFT passes' chunk.
+int spec_chunk_for(int N, int M, int Lg) {
+    size_t F = Lg / 2 + 1;
+    size_t ch = ((size_t)6 << 30) / ((size_t)M * F * 8);
+    ch = std::max(ch, (size_t)chunk_for(N, M, Lg));
+    if (ch > (size_t)N) ch = N;
+    return (int)ch;
+}
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+        cudaGetLastError();
+        return 152;
+    }
+    return sms;
+}
+
 // G1h = rfft(G1) and A = sum_m |G1h|^2
 int refresh_G1h(cdlgb_ctx* c) {
     ST_TRY(r2c(c, c->M, c->G1, c->G1h));
@@ -593,7 +614,12 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     b += (size_t)N * L4 * 4;                    // data
     b += 7 * LMN * 4;                           // X x2, y2, y3, d, g1, g3
     if (fused) b += (size_t)N * M * F * 8 * 2;  // d-hat, g1-hat (spectral D-step)
-    if (fused) b += (size_t)dspec_slots(N, chunk_for(N, (int)M, (int)Lg)) * 3 * M * F * 8;
+    if (fused) {
+        // spectral D-step: the sums' slots and the Y3 half-spectra beyond the cuFFT chunk
+        const size_t sch = spec_chunk_for(N, (int)M, (int)Lg), ch = chunk_for(N, (int)M, (int)Lg);
+        b += (size_t)dspec_slots(N, (int)sch, (int)F, device_sms()) * 2 * M * F * 8;
+        b += (sch - ch) * M * F * 8;
+    }
     b += 8 * LN * 4;                            // Y1 y1 DX Td G2 g2 + 2 scratch
     b += 8 * LM * 4 + M * F * 8 + F * 4;        // G1 G3 dmean Dbest v1 ... G1h A
     b += 2 * N * F * 8;                         // LN spectra
@@ -653,10 +679,17 @@ int admm_alloc(cdlgb_ctx* c) {
     // cuFFT-path scratch for one chunk of sequences (init's DX, the D-step, and the
     // X-step when no fused kernel covers Lg)
     c->chunk = chunk_for(c->N, c->M, c->Lg);
-    if (c->g1h) ST_TRY(A((void**)&c->spart, dspec_part_bytes(c->M, c->F, dspec_slots(c->N, c->chunk))));
+    c->schunk = c->chunk;
+    c->nsm = device_sms();
+    if (c->g1h) {
+        c->schunk = spec_chunk_for(c->N, c->M, c->Lg);
+        c->dslots = dspec_slots(c->N, c->schunk, c->F, c->nsm);
+        ST_TRY(A((void**)&c->spart, dspec_part_bytes(c->M, c->F, c->dslots)));
+    }
     const size_t cLMN = (size_t)c->chunk * c->M * c->Lg, cSp = (size_t)c->chunk * c->M * c->F;
     ST_TRY(A((void**)&c->sA, cLMN * 4));
-    ST_TRY(A((void**)&c->sAh, cSp * 8));
+    // the first Y3-hat scratch also holds a chunk of the spectral D-step
+    ST_TRY(A((void**)&c->sAh, (size_t)c->schunk * c->M * c->F * 8));
     ST_TRY(A((void**)&c->sB, cLMN * 4));
     ST_TRY(A((void**)&c->sBh, cSp * 8));
     ST_TRY(A((void**)&c->sCh, cSp * 8));
@@ -856,11 +889,11 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             ST_TRY(r2c(c, M, c->G3, c->G3h));
             void* fw = fused_dfwd(c);
             int slot0 = 0;
-            for (int n0 = 0; n0 < N; n0 += c->chunk) {
-                const int cn = std::min(c->chunk, N - n0);
+            for (int n0 = 0; n0 < N; n0 += c->schunk) {
+                const int cn = std::min(c->schunk, N - n0);
                 ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, nullptr, nullptr));
                 ST_TRY(dspec_launch(c, c->sAh, c->G3h, n0, n0 + cn, slot0));
-                slot0 += dspec_slots(cn, cn);
+                slot0 += dspec_nsub(cn, F, c->nsm);
             }
             ST_TRY(c2r(c, N, c->sVh, c->Td));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,

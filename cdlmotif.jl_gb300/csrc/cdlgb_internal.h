@@ -85,6 +85,9 @@ struct cdlgb_ctx {
 
     void* plans = nullptr;          // cuFFT plan cache keyed by (direction, batch)
     int chunk = 0;                  // sequences per chunk of the cuFFT-transform passes
+    int schunk = 0;                 // sequences per chunk of the spectral D-step
+    int dslots = 0;                 // its partial-sum slots over all chunks
+    int nsm = 0;                    // SMs of the device
 
     // scan scratch
     int32_t* scan_i = nullptr; size_t scan_i_cap = 0;
@@ -215,7 +218,8 @@ void scan_free(cdlgb_ctx* c);
 // ---- dspec.cu ----
 int dspec_max_m();
 size_t dspec_part_bytes(int M, int F, int slots);
-int dspec_slots(int N, int chunk);
+int dspec_nsub(int cn, int F, int nsm);
+int dspec_slots(int N, int chunk, int F, int nsm);
 int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int c1, int slot0);
 int dspec_sums(cdlgb_ctx* c, const float2* G3h, float2* out);
 int dspec_g3(cdlgb_ctx* c, float2* dst, const float2* g1h, size_t rows);

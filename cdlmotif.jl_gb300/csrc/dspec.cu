@@ -19,6 +19,8 @@
 
 #include <cuda_pipeline_primitives.h>
 
+#include <algorithm>
+
 namespace {
 
 __device__ __forceinline__ float2 cadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -45,10 +47,9 @@ struct SArgs {
 };
 
 constexpr int kBins = 32, kWarps = 16;
-constexpr int kSub = 64;     // sub-ranges (CTAs along y) per launch
 constexpr int kArr = 3;      // staged spectra: Y3-hat, g1-hat, d-hat
 
-// grid (ceil(F / 32), kSub): a CTA takes 32 bins and sub-range s of the sequences
+// grid (ceil(F / 32), nsub): a CTA takes 32 bins and sub-range s of the sequences
 // [c0, c1), in order, and writes that sub-range's sums to slot slot0 + s; warp w owns
 // filters w, w + 16, ...  With PIPE, each thread's spectra of sequence n + 1 are copied
 // to shared memory (asynchronous copies, two buffers) while sequence n is computed.
@@ -262,7 +263,30 @@ int dspec_max_m() { return kWarps * 8; }
 
 size_t dspec_part_bytes(int M, int F, int slots) { return (size_t)slots * 2 * M * F * sizeof(float2); }
 
-int dspec_slots(int N, int chunk) { return ((N + chunk - 1) / chunk) * kSub; }
+// Sub-ranges of one launch over cn sequences.  One CTA fits per SM, so a launch runs
+// ceil(nbb nsub / nsm) waves of CTAs that each take ceil(cn / nsub) sequences after a
+// start-up (the block's G1-hat, G3-hat, Dg and the first staged sequence) worth about
+// two sequences; the count minimising that estimate is taken (the smallest on ties).
+// It depends only on (cn, F, nsm), so the slot layout and the order of the sums are
+// fixed for a given device and size.
+int dspec_nsub(int cn, int F, int nsm) {
+    const int nbb = (F + kBins - 1) / kBins;
+    if (nsm < 1) nsm = 1;
+    int best = 1;
+    long long bt = -1;
+    for (int s = 1; s <= std::min(cn, 2048); ++s) {
+        const long long waves = ((long long)nbb * s + nsm - 1) / nsm;
+        const long long t = waves * ((cn + s - 1) / s + 2);
+        if (bt < 0 || t < bt) { bt = t; best = s; }
+    }
+    return best;
+}
+
+int dspec_slots(int N, int chunk, int F, int nsm) {
+    int slots = 0;
+    for (int n0 = 0; n0 < N; n0 += chunk) slots += dspec_nsub(std::min(chunk, N - n0), F, nsm);
+    return slots;
+}
 
 int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int c1, int slot0) {
     SArgs a;
@@ -270,7 +294,7 @@ int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int 
     a.Zh = c->sUh; a.Th = c->sVh; a.part = c->spart;
     a.N = c->N; a.M = c->M; a.F = c->F; a.c0 = c0; a.c1 = c1; a.slot0 = slot0;
     a.kd = c->p.sherman_const_cdl; a.scale = 1.f / (float)c->Lg;
-    const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)kSub);
+    const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)dspec_nsub(c1 - c0, c->F, c->nsm));
     const size_t sm = (size_t)3 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * (4 + 8 + 8);
     if (c->M <= 4 * kWarps) {
         // + the two staging buffers: 2 x 3 spectra x 4 filters x 512 threads
@@ -291,7 +315,7 @@ int dspec_sums(cdlgb_ctx* c, const float2* G3h, float2* out) {
     k_dg_update<<<(unsigned)((mf + 255) / 256), 256, 0, c->stream>>>(c->Dg, c->G1h, G3h, mf);
     LAUNCH_CHECK(c, "k_dg_update");
     k_dspec_sum<<<(unsigned)((4 * 2 * mf + 255) / 256), 256, 0, c->stream>>>(
-        c->spart, c->Dg, out, mf, dspec_slots(c->N, c->chunk), c->N, 1.0 / (double)c->Lg);
+        c->spart, c->Dg, out, mf, c->dslots, c->N, 1.0 / (double)c->Lg);
     LAUNCH_CHECK(c, "k_dspec_sum");
     return CDLGB_OK;
 }

@@ -68,8 +68,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     float2* G3s = G1s + (size_t)M * kBins;                 // [M][32]
     float2* Dgs = G3s + (size_t)M * kBins;                 // [M][32]
     float* pB = reinterpret_cast<float*>(Dgs + (size_t)M * kBins);   // [kWarps][32]
-    float2* pQ = reinterpret_cast<float2*>(pB + kWarps * kBins);     // [kWarps][32]
-    float2* pT = pQ + kWarps * kBins;                                // [kWarps][32]
+    float4* pQT = reinterpret_cast<float4*>(pB + kWarps * kBins);    // [kWarps][32]: Q, T
     for (int i = threadIdx.x; i < M * kBins; i += blockDim.x) {
         const int m = i / kBins, ff = blockIdx.x * kBins + i % kBins;
         const bool in = ff < F;
@@ -83,7 +82,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     __syncthreads();
     const int fl = on ? f : 0;                             // lanes past F load bin 0
     // staging: [2][kArr][MW][threads], each thread's own slots
-    float2* stg = pT + kWarps * kBins;
+    float2* stg = reinterpret_cast<float2*>(pQT + kWarps * kBins);
     const int nt = blockDim.x, tid = threadIdx.x;
     auto stage = [&](int n, int buf) {
         const size_t base = (size_t)n * M * F + fl;
@@ -99,7 +98,12 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
         __pipeline_commit();
     };
     if (PIPE && n0 < n1) stage(n0, 0);
+    // rfft(G2 - g2) of the bin, loaded one sequence ahead (it is needed after the
+    // cross-warp sums, where a load issued then would stall every warp)
+    float2 zn = (on && n0 < n1) ? A.Zh[(size_t)n0 * F + f] : make_float2(0.f, 0.f);
     for (int n = n0; n < n1; ++n) {
+        const float2 z = zn;
+        if (on && n + 1 < n1) zn = A.Zh[(size_t)(n + 1) * F + f];
         // every load of this sequence first (independent), then the arithmetic
         float2 yv[MW], g1v[MW], dv[MW];
         if (PIPE) {
@@ -149,20 +153,19 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             T = cfma2(y, d, T);
         }
         pB[w * kBins + lane] = B;
-        pQ[w * kBins + lane] = Q;
-        pT[w * kBins + lane] = T;
+        pQT[w * kBins + lane] = make_float4(Q.x, Q.y, T.x, T.y);
         __syncthreads();
         B = 0.f;
         Q = T = make_float2(0.f, 0.f);
 #pragma unroll
         for (int v = 0; v < kWarps; ++v) {
             B += pB[v * kBins + lane];
-            Q = cadd2(Q, pQ[v * kBins + lane]);
-            T = cadd2(T, pT[v * kBins + lane]);
+            const float4 qt = pQT[v * kBins + lane];
+            Q = cadd2(Q, make_float2(qt.x, qt.y));
+            T = cadd2(T, make_float2(qt.z, qt.w));
         }
         __syncthreads();                                   // partials read before reuse
         if (on) {
-            const float2 z = A.Zh[(size_t)n * F + f];
             const float inv = 1.f / (B + A.kd);
             const float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
             const float2 W = csub2(z, beta);

@@ -106,6 +106,32 @@ __device__ __forceinline__ void repack_X_r(float2* __restrict__ bufs, int BUF, i
     }
 }
 
+// L2 prefetch of the rows sequence n will read at its first iteration (this CTA's MC
+// filter rows of X, y2, y3; Y1, y1, DX and the W'S window), issued by the 32 lanes of
+// one warp while the current sequence is still iterating.  Bulk prefetches are hints:
+// nothing waits on them.  Every row is a multiple of 16 bytes long (Lg and L4 are
+// multiples of 4 floats); a base pointer that is not 16-byte aligned skips the hint.
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+    if (((uintptr_t)p & 15) == 0)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void prefetch_next(const IArgs& A, int n, int m0, int MC, int Lg, int lane) {
+    if (n >= A.N) return;
+    const unsigned rb = (unsigned)Lg * 4u;
+    const size_t r0 = ((size_t)n * A.M + m0) * Lg;
+    for (int q = lane; q < 3 * MC + 4; q += 32) {
+        if (q < 3 * MC) {
+            const float* base = q < MC ? A.Xin : q < 2 * MC ? A.y2 : A.y3;
+            l2_prefetch(base + r0 + (size_t)(q % MC) * Lg, rb);
+        } else if (q < 3 * MC + 3) {
+            const float* base = q == 3 * MC ? A.Y1 : q == 3 * MC + 1 ? A.y1 : A.DX;
+            l2_prefetch(base + (size_t)n * Lg, rb);
+        } else {
+            l2_prefetch(A.S + (size_t)n * A.L4, (unsigned)A.L4 * 4u);
+        }
+    }
+}
+
 // MC filters per CTA (compile time), NT threads: every slot's lane group and every
 // thread's bins of the cross-filter phases are fixed, and each thread keeps the G1h
 // values of its bins in registers for the whole launch (G1 is fixed during a code update).
@@ -207,6 +233,8 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
         }
 
         for (int t = 0; t < A.iters; ++t, ++it) {
+            if (t == A.iters / 2 && threadIdx.x >= 32 && threadIdx.x < 64)
+                prefetch_next(A, n + nclusters, m0, MC, Lg, lane);
             __syncwarp();
             fwd_step2<N1, P>(sb, gl, act);
             __syncthreads();

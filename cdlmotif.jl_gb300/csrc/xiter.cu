@@ -218,7 +218,21 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
         } else if (act) {
             // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
             __syncwarp(gmask);                  // the previous sequence's reads of Ss are done
-            for (int t = gl; t < A.L4; t += N1) Ss[t] = A.S[(size_t)n * A.L4 + t];
+            // the window in batches of 8 loads per lane, all issued before their stores
+            const float* Sn = A.S + (size_t)n * A.L4;
+            for (int t0 = gl; t0 < A.L4; t0 += 8 * N1) {
+                float sv[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int t = t0 + N1 * k;
+                    sv[k] = t < A.L4 ? Sn[t] : 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int t = t0 + N1 * k;
+                    if (t < A.L4) Ss[t] = sv[k];
+                }
+            }
             __syncwarp(gmask);
             const size_t r = (size_t)n * Lg + gl;
 #pragma unroll 16

@@ -429,6 +429,35 @@ __global__ void k_abssum(const float4* __restrict__ X, size_t n4, double* __rest
     if (threadIdx.x == 0) out[blockIdx.x] = acc;
 }
 
+// The initial X in one pass: drawn as k_randn_masked draws it, or the given X0 masked
+// as k_mask4 masks it; y2 = y3 = 0 (CDL_setup.jl:220-230); and the per-block sums of
+// |X| for the initial objective.  Launched on k_abssum's grid (304 blocks of kBlock), so
+// every thread visits k_abssum's indices in its order: the same sums, bit for bit.
+__global__ void k_init_x(float4* __restrict__ X, float4* __restrict__ y2, float4* __restrict__ y3,
+                         size_t n4, uint64_t seed, int draw, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n4;
+         j += (size_t)gridDim.x * blockDim.x) {
+        float4 v;
+        if (draw) {
+            const uint64_t h = splitmix64(seed * 0x2545F4914F6CDD1Dull ^ (uint64_t)(4 * j));
+            const float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
+            const float u2 = ((float)(h & 0xFFFFFFull) + 0.5f) * (1.0f / 16777216.0f);
+            v = make_float4(sqrtf(-2.f * logf(u1)) * cospif(2.f * u2), 0.f, 0.f, 0.f);
+        } else {
+            v = make_float4(X[j].x, 0.f, 0.f, 0.f);
+        }
+        X[j] = v;
+        y2[j] = z;
+        y3[j] = z;
+        acc += (double)((fabsf(v.x) + fabsf(v.y)) + (fabsf(v.z) + fabsf(v.w)));
+    }
+    acc = block_sum_d(acc, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = acc;
+}
+
 // sum over the data window of (DX - S)^2  (||W*DX - S||^2)
 __global__ void k_fit(const float* __restrict__ DX, const float* __restrict__ S, int Lg, int L4,
                       int gamma, size_t n, double* __restrict__ out) {
@@ -719,6 +748,18 @@ void admm_free(cdlgb_ctx* c) {
 
 int cdlgb_set_plan_streams(cdlgb_ctx* c) { return set_plan_streams(c); }
 
+// the initial time-domain dictionary state: d = G1 broadcast over n, g1 = g3 = 0
+static int write_time_init(cdlgb_ctx* c) {
+    const size_t LMN = c->LMN;
+    k_bcast_plane<<<grid_for(LMN / 4, kBlock), kBlock, 0, c->stream>>>(
+        (float4*)c->d, (const float4*)c->G1, c->LM / 4, LMN / 4);
+    LAUNCH_CHECK(c, "k_bcast_plane");
+    CU_TRY(c, cudaMemsetAsync(c->g1, 0, LMN * 4, c->stream));
+    CU_TRY(c, cudaMemsetAsync(c->g3, 0, LMN * 4, c->stream));
+    c->time_init = 0;
+    return CDLGB_OK;
+}
+
 int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     cudaStream_t s = c->stream;
     const int Lg = c->Lg, M = c->M, N = c->N, flen = 4 * c->p.filter_size;
@@ -728,16 +769,20 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     c->absx_fused = 0;
     c->dh_valid = 0;
     float* X = c->Xb[0];
-    // X0 (CDL_setup.jl:191-192): given, or standard normal; then masked to the 4-stride
-    if (X0) {
-        CU_TRY(c, cudaMemcpyAsync(X, X0, LMN * 4, cudaMemcpyHostToDevice, s));
-    } else {
-        k_randn_masked<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)X, LMN / 4, seed);
-        LAUNCH_CHECK(c, "k_randn_masked");
-    }
-    if (X0) {      // a given X0 is masked here; the drawn one already is
-        k_mask4<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)X, LMN / 4);
-        LAUNCH_CHECK(c, "k_mask4");
+    // X0 (CDL_setup.jl:191-192): given, or standard normal; masked to the 4-stride; with
+    // y2 = y3 = 0 and sum |X| for the initial objective in the same pass
+    if (X0) CU_TRY(c, cudaMemcpyAsync(X, X0, LMN * 4, cudaMemcpyHostToDevice, s));
+    k_init_x<<<152 * 2, kBlock, 0, s>>>((float4*)X, (float4*)c->y2, (float4*)c->y3, LMN / 4, seed,
+                                        X0 ? 0 : 1, c->dred);
+    LAUNCH_CHECK(c, "k_init_x");
+    c->absx_init = 1;
+    // the spectral D-step (dspec.cu) where its transforms cover Lg and M
+    c->dspec = 0;
+    c->time_stale = 0;
+    c->time_init = 0;
+    if (c->g1h && c->fused && fused_dfwd(c) && !fused_has_dstep(c)) {
+        const char* e = getenv("CDLGB_DSPEC");
+        if (!e || atoi(e) != 0) c->dspec = 1;
     }
     // D0 (CDL_setup.jl:182-183), masked by P_D
     std::vector<float> D(LM, 0.f);
@@ -769,27 +814,21 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     CU_TRY(c, cudaMemcpyAsync(c->G3, c->G1, LM * 4, cudaMemcpyDeviceToDevice, s));
     CU_TRY(c, cudaMemcpyAsync(c->Dbest, c->G1, LM * 4, cudaMemcpyDeviceToDevice, s));
     CU_TRY(c, cudaMemcpyAsync(c->dsum, c->G1, LM * 4, cudaMemcpyDeviceToDevice, s));
-    // d = real(ifft(d-hat)) with d-hat = D-hat broadcast (CDL_setup.jl:207-210)
-    k_bcast_plane<<<grid_for(LMN / 4, kBlock), kBlock, 0, s>>>((float4*)c->d, (const float4*)c->G1,
-                                                                 LM / 4, LMN / 4);
-    LAUNCH_CHECK(c, "k_bcast_plane");
-    // duals and Y1 start at zero (CDL_setup.jl:220-230)
-    CU_TRY(c, cudaMemsetAsync(c->y2, 0, LMN * 4, s));
-    CU_TRY(c, cudaMemsetAsync(c->y3, 0, LMN * 4, s));
-    CU_TRY(c, cudaMemsetAsync(c->g1, 0, LMN * 4, s));
-    CU_TRY(c, cudaMemsetAsync(c->g3, 0, LMN * 4, s));
+    // d = real(ifft(d-hat)) with d-hat = D-hat broadcast (CDL_setup.jl:207-210); the duals
+    // g1, g3 start at zero (CDL_setup.jl:220-230).  In the spectral form nothing reads
+    // these time-domain arrays before a D-step replaces them: written when first read.
+    if (c->dspec) {
+        c->time_init = 1;
+    } else {
+        ST_TRY(write_time_init(c));
+    }
+    // Y1 and the LN duals start at zero
     CU_TRY(c, cudaMemsetAsync(c->Y1, 0, LN * 4, s));
     CU_TRY(c, cudaMemsetAsync(c->y1, 0, LN * 4, s));
     CU_TRY(c, cudaMemsetAsync(c->g2, 0, LN * 4, s));
     CU_TRY(c, cudaMemsetAsync(c->Td, 0, LN * 4, s));
     ST_TRY(refresh_G1h(c));
     // spectral D-step: d-hat = D-hat broadcast, g1-hat = g3-hat = 0
-    c->dspec = 0;
-    c->time_stale = 0;
-    if (c->g1h && c->fused && fused_dfwd(c) && !fused_has_dstep(c)) {
-        const char* e = getenv("CDLGB_DSPEC");
-        if (!e || atoi(e) != 0) c->dspec = 1;
-    }
     if (c->dspec) {
         const size_t nmf = (size_t)N * M * c->F;
         ST_TRY(dspec_bcast(c, c->Dhs, c->G1h));
@@ -903,6 +942,7 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             ST_TRY(dspec_sums(c, c->G3h, c->sumspec));
             ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part));
             c->time_stale = 1;
+            c->time_init = 0;
             int flen = 4 * c->p.filter_size;
             k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
                                                                    LM, Lg, flen, N, 1);
@@ -985,7 +1025,10 @@ static int objective_async(cdlgb_ctx* c) {
     const double* pa = c->dred;
     const double* fp = nullptr;
     int nf = 0;
-    if (c->absx_fused && fused_absx(c, &fp, &nf)) {
+    if (c->absx_init) {
+        // sum |X| came with the initial X (k_init_x)
+        c->absx_init = 0;
+    } else if (c->absx_fused && fused_absx(c, &fp, &nf)) {
         // sum |X| came with the last fused X-step
         pa = fp;
         nb1 = nf;
@@ -1051,7 +1094,9 @@ int admm_code_threshold(cdlgb_ctx* c, double* thr) {
 // d, g1, g3 in the time domain from the spectral state (for readers of those fields);
 // the spectra are copied to scratch first (the inverse transform may overwrite its input)
 int admm_sync_time_state(cdlgb_ctx* c) {
-    if (!c->dspec || !c->time_stale) return CDLGB_OK;
+    if (!c->dspec) return CDLGB_OK;
+    if (c->time_init) return write_time_init(c);    // no D-step since the initialisation
+    if (!c->time_stale) return CDLGB_OK;
     const int M = c->M, Lg = c->Lg, F = c->F;
     const float2* src[3] = {c->Dhs, c->g1h, c->g1h};
     float* dst[3] = {c->d, c->g1, c->g3};

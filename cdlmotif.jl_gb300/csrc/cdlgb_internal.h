@@ -60,6 +60,10 @@ struct cdlgb_ctx {
     // sums and their total are scratch
     float2 *g1h = nullptr, *Dg = nullptr, *G3h = nullptr, *spart = nullptr, *sumspec = nullptr;
     int dspec = 0, time_stale = 0;
+    // with dspec: d, g1, g3 still to receive their initial values (d = G1 broadcast,
+    // g1 = g3 = 0), written when first read, unless a D-step comes first
+    int time_init = 0;
+    int absx_init = 0;              // dred[0, 304) holds sum |X| of the initial X
     // LN state
     float *Y1 = nullptr, *y1 = nullptr, *DX = nullptr, *Td = nullptr, *G2 = nullptr, *g2 = nullptr;
     // LM state

@@ -493,10 +493,11 @@ def extend(c: CDL, positions, lens, filter_size: int, use_comp=None, bg=_BG, pse
     "pfms" (list or None), "keep" (bool (K,))}."""
     pos, ln, _, _ = extension(c, positions, lens, use_comp, bg, pseudocount, perc_no_less_than,
                               ic_extension_thresh)
-    keep = ((pos > 0).sum(axis=0) > 0) & (ln > filter_size + 2)
-    pos = np.ascontiguousarray(pos[:, keep])
+    keep = (pos > 0).any(axis=0) & (ln > filter_size + 2)
+    kept = np.flatnonzero(keep)
+    pos = pos.take(kept, axis=1)          # (a C-order copy; faster than a boolean column index)
     ln = ln[keep]
-    uc = None if use_comp is None else np.ascontiguousarray(np.asarray(use_comp)[:, keep])
+    uc = None if use_comp is None else np.asarray(use_comp).take(kept, axis=1)
     pfms = None
     if re_evaluate_pfm:
         pfms = posdicts2pfms(c, pos, ln, uc, pseudocounts_r, pseudocount, smoothing) if len(ln) else []
@@ -546,20 +547,21 @@ def masked_trim(pfms, filter_size: int, positions=None, use_comp=None, bg=_BG,
            for p, f, b in zip(pfms, front, back)]
     pos = None
     if positions is not None:
+        # every entry (position > 0) moves by its motif's front trim, or by its back
+        # trim when reverse-complemented after merging (trim.jl:47-59)
         pos = np.array(positions, np.int32, copy=True)
-        for k in range(len(new)):
-            on = pos[:, k] > 0
-            shift = np.full(pos.shape[0], front[k], np.int32)
-            if after_merged and use_comp is not None:
-                shift = np.where(np.asarray(use_comp)[:, k] != 0, back[k], front[k]).astype(np.int32)
-            pos[on, k] += shift[on]
+        if after_merged and use_comp is not None:
+            shift = np.where(np.asarray(use_comp) != 0, back[None, :], front[None, :]).astype(np.int32)
+        else:
+            shift = front[None, :]
+        pos += (pos > 0).astype(np.int32) * shift
     keep = np.array([p.shape[1] > filter_size + 1 for p in new], bool)
     if pos is not None:
-        keep &= (pos > 0).sum(axis=0) > 0
+        keep &= (pos > 0).any(axis=0)
     new = [p for p, kk in zip(new, keep) if kk]
     lens = np.array([p.shape[1] for p in new], np.int32)
     out = {"pfms": new, "lens": lens, "keep": keep, "front": front, "back": back,
-           "positions": (np.ascontiguousarray(pos[:, keep]) if (pos is not None and update_positions)
+           "positions": (pos.take(np.flatnonzero(keep), axis=1) if (pos is not None and update_positions)
                          else None),
            "use_comp": use_comp, "pwms": None, "thresh": None}
     if c is not None and len(new):

@@ -123,6 +123,93 @@ __global__ void k_scan_both(const float* __restrict__ data, const float* __restr
     }
 }
 
+// k_scan_both with the block's inputs staged once: the sequence base-major (xt[j][p],
+// so consecutive positions are consecutive words), every PWM and its reverse complement
+// as (fwd, comp) pairs in the order the sums consume them (pw[k][j][kk]), one position
+// per thread, and the argmax of each motif reduced within each warp by shuffles (no
+// barrier) and across the warps once, after the last motif.  The products and sums are
+// k_scan_both's, in its order, and the (value, index) reduction is the same total order,
+// so positions, scores and strands are bit-identical to it.
+__global__ void k_scan_both_staged(const float* __restrict__ data, const float* __restrict__ pwms,
+                                   const int32_t* __restrict__ lens, const float* __restrict__ thresh,
+                                   int K, int maxlen, int L, int32_t* __restrict__ pos,
+                                   float* __restrict__ score, uint8_t* __restrict__ comp) {
+    extern __shared__ float4 sm4s[];
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float2* pw = reinterpret_cast<float2*>(sm4s);                  // [K][4][maxlen]
+    VI* wb = reinterpret_cast<VI*>(pw + (size_t)K * 4 * maxlen);     // [K][nw][2]
+    float* xt = reinterpret_cast<float*>(wb + (size_t)K * nw * 2);  // [4][L]
+    const int n = blockIdx.x;
+    const float* col = data + (size_t)n * 4 * L;
+    for (int i = threadIdx.x; i < 4 * L; i += blockDim.x) xt[(i & 3) * L + (i >> 2)] = col[i];
+    const int per = 4 * maxlen;
+    for (int i = threadIdx.x; i < K * per; i += blockDim.x) {
+        const int k = i / per, r = i - k * per, j = r / maxlen, kk = r - j * maxlen;
+        const int w = lens[k];
+        float f = 0.f, cc = 0.f;
+        if (kk < w) {
+            f = pwms[k + K * (j + 4 * kk)];
+            cc = pwms[k + K * ((3 - j) + 4 * (w - 1 - kk))];
+        }
+        pw[i] = make_float2(f, cc);
+    }
+    __syncthreads();
+    const int l = threadIdx.x;
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        VI bf{-INFINITY, 0x7fffffff}, bc{-INFINITY, 0x7fffffff};
+        if (l <= L - w) {
+            const float2* p = pw + (size_t)k * per;
+            float sf = 0.f, sc = 0.f;
+            for (int j = 0; j < 4; ++j) {
+                const float* xr = xt + j * L + l;
+                const float2* pj = p + j * maxlen;
+#pragma unroll 4
+                for (int kk = 0; kk < w; ++kk) {
+                    const float x = xr[kk];
+                    const float2 q = pj[kk];
+                    sf = __fadd_rn(sf, __fmul_rn(q.x, x));
+                    sc = __fadd_rn(sc, __fmul_rn(q.y, x));
+                }
+            }
+            if (sf > -INFINITY) bf = VI{sf, l};
+            if (sc > -INFINITY) bc = VI{sc, l};
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            VI y;
+            y.v = __shfl_xor_sync(0xffffffffu, bf.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, bf.i, o);
+            bf = vi_best(bf, y);
+            y.v = __shfl_xor_sync(0xffffffffu, bc.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, bc.i, o);
+            bc = vi_best(bc, y);
+        }
+        if (lane == 0) {
+            wb[((size_t)k * nw + wid) * 2] = bf;
+            wb[((size_t)k * nw + wid) * 2 + 1] = bc;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        VI rf{-INFINITY, 0x7fffffff}, rc{-INFINITY, 0x7fffffff};
+        for (int v = 0; v < nw; ++v) {
+            rf = vi_best(rf, wb[((size_t)k * nw + v) * 2]);
+            rc = vi_best(rc, wb[((size_t)k * nw + v) * 2 + 1]);
+        }
+        const float sF = rf.i == 0x7fffffff ? -INFINITY : rf.v;
+        const float sC = rc.i == 0x7fffffff ? -INFINITY : rc.v;
+        const int iF = rf.i == 0x7fffffff ? -1 : rf.i + 1;
+        const int iC = rc.i == 0x7fffffff ? -1 : rc.i + 1;
+        const bool fwd = sF >= sC;
+        const float sv = fwd ? sF : sC;
+        const bool keep = sv > thresh[k];
+        const size_t o = k + (size_t)K * n;
+        if (pos) pos[o] = keep ? (fwd ? iF : iC) : 0;
+        if (score) score[o] = keep ? sv : 0.f;
+        if (comp) comp[o] = (keep && !fwd) ? 1 : 0;
+    }
+}
+
 // integer count matrices: grid (K, chunks); counts (4, maxlen, K) col-major
 __global__ void k_count(const float* __restrict__ data, const int32_t* __restrict__ pos,
                         const uint8_t* __restrict__ comp, const int32_t* __restrict__ lens, int K,
@@ -214,12 +301,27 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
     float* dscore = c->scan_f + (size_t)K * 4 * maxlen + K;
     size_t shm = (size_t)4 * L * sizeof(float);
     if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
-    if (shm > 48 * 1024)
-        CU_TRY(c, cudaFuncSetAttribute(k_scan_both, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    k_scan_both<<<N, kScanThreads, shm, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
-                                                      c->scan_f + (size_t)K * 4 * maxlen, K,
-                                                      maxlen, L, dpos, dscore, c->scan_u);
-    LAUNCH_CHECK(c, "k_scan_both");
+    // one position per thread and the staged PWMs when they fit: at most 1024 positions
+    // and 64 KB of staged inputs (several blocks per SM)
+    const int nts = ((L + 31) / 32) * 32;
+    const size_t shs = (size_t)K * 4 * maxlen * sizeof(float2) + (size_t)K * (nts / 32) * 2 * sizeof(VI) +
+                       (size_t)4 * L * sizeof(float);
+    if (nts <= 1024 && shs <= 64 * 1024) {
+        if (shs > 48 * 1024)
+            CU_TRY(c, cudaFuncSetAttribute(k_scan_both_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           64 * 1024));
+        k_scan_both_staged<<<N, nts, shs, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                                        c->scan_f + (size_t)K * 4 * maxlen, K, maxlen, L,
+                                                        dpos, dscore, c->scan_u);
+        LAUNCH_CHECK(c, "k_scan_both_staged");
+    } else {
+        if (shm > 48 * 1024)
+            CU_TRY(c, cudaFuncSetAttribute(k_scan_both, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        k_scan_both<<<N, kScanThreads, shm, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                                          c->scan_f + (size_t)K * 4 * maxlen, K,
+                                                          maxlen, L, dpos, dscore, c->scan_u);
+        LAUNCH_CHECK(c, "k_scan_both");
+    }
     if (pos_out)
         CU_TRY(c, cudaMemcpyAsync(pos_out, dpos, (size_t)K * N * 4, cudaMemcpyDeviceToHost, c->stream));
     if (score_out)

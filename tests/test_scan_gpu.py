@@ -79,6 +79,21 @@ def test_scans_bit_exact_random(pkg, built_lib, N, L, K):
         np.testing.assert_array_equal(nseq, rn)
 
 
+@pytest.mark.parametrize("N,L,K,lo,hi", [(3, 1100, 3, 4, 21), (4, 40, 300, 20, 32)])
+def test_two_strand_scan_unstaged_sizes(pkg, built_lib, N, L, K, lo, hi):
+    """The sizes the staged two-strand kernel does not take (more than 1024 positions,
+    more than 64 KB of staged PWMs) run the unstaged kernel: bit-exact too."""
+    rng = np.random.default_rng(N * L + K)
+    S, _ = random_onehot(rng, N, L)
+    pwms, lens, thresh = _random_pwms(rng, K, lo, hi)
+    with _ctx(pkg, S) as c:
+        pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+        rp, rs, rc = SO.overlapping_scan(S, pwms, lens, thresh)
+        np.testing.assert_array_equal(pos.T, rp)
+        np.testing.assert_array_equal(score.T, rs)
+        np.testing.assert_array_equal(comp.T, rc)
+
+
 def test_scan_edge_cases(pkg, built_lib):
     rng = np.random.default_rng(3)
     N, L = 12, 9

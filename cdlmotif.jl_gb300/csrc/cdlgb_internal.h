@@ -207,6 +207,29 @@ inline int ensure_scratch(cdlgb_ctx* c, T** p, size_t* cap, size_t n) {
     *cap = n;
     return CDLGB_OK;
 }
+// The first entry i of pos (n-major, k fastest: K entries per sequence, 1-based, 0 =
+// none) that is negative or, with lens, whose window of lens[k] bases leaves a sequence
+// of L bases (without lens: that exceeds L); -1 when every entry is valid.  A
+// branch-free pass over all entries first (the compiler vectorises it), the search for
+// the index only when that pass finds one.
+inline long long first_bad_position(const int32_t* pos, const int32_t* lens, int K, size_t N, int L) {
+    int bad = 0;
+    for (size_t n = 0; n < N; ++n) {
+        const int32_t* pr = pos + n * (size_t)K;
+        for (int k = 0; k < K; ++k) {
+            const int p = pr[k];
+            const int lim = lens ? L + 1 - lens[k] : L;
+            bad |= (p < 0) | ((p > 0) & (p > lim));
+        }
+    }
+    if (!bad) return -1;
+    for (size_t i = 0; i < N * (size_t)K; ++i) {
+        const int p = pos[i];
+        const int lim = lens ? L + 1 - lens[i % K] : L;
+        if (p < 0 || (p > 0 && p > lim)) return (long long)i;
+    }
+    return -1;
+}
 // ---- scan.cu ----
 int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* thresh,
              int K, int maxlen, int32_t* pos_out);

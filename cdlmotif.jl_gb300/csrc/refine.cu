@@ -220,9 +220,8 @@ int extend_positions(cdlgb_ctx* c, int32_t* pos, const uint8_t* use_comp, int32_
         if (lens[k] < 1 || lens[k] > L)
             return cdlgb_seterr(c, CDLGB_EINVAL, "extend: lens[%d]=%d outside 1..L=%d", k, lens[k], L);
     const size_t KN = (size_t)K * N;
-    for (size_t i = 0; i < KN; ++i)
-        if (pos[i] < 0 || pos[i] > L)
-            return cdlgb_seterr(c, CDLGB_EINVAL, "extend: pos[%zu]=%d outside 0..L=%d", i, pos[i], L);
+    if (const long long i = first_bad_position(pos, nullptr, K, (size_t)N, L); i >= 0)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "extend: pos[%lld]=%d outside 0..L=%d", i, pos[i], L);
     // device scratch: lens (K) + out (4K) + pos (KN) ints, use_comp (KN) bytes, list (KN) int2
     ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)5 * K + KN));
     ST_TRY(ensure_scratch(c, &c->scan_u, &c->scan_u_cap, KN));
@@ -278,12 +277,9 @@ int rescore_positions(cdlgb_ctx* c, const float* pwms, const int32_t* pos, const
     for (int k = 0; k < K; ++k)
         if (lens[k] < 1 || lens[k] > maxlen)
             return cdlgb_seterr(c, CDLGB_EINVAL, "rescore: lens[%d]=%d outside 1..maxlen=%d", k, lens[k], maxlen);
-    for (size_t i = 0; i < KN; ++i) {
-        const int k = (int)(i % K);
-        if (pos[i] < 0 || (pos[i] > 0 && pos[i] - 1 + lens[k] > L))
-            return cdlgb_seterr(c, CDLGB_EINVAL, "rescore: window at pos[%zu]=%d (len %d) leaves the sequence (L=%d)",
-                                i, pos[i], lens[k], L);
-    }
+    if (const long long i = first_bad_position(pos, lens, K, (size_t)N, L); i >= 0)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "rescore: window at pos[%lld]=%d (len %d) leaves the sequence (L=%d)",
+                            i, pos[i], lens[i % K], L);
     const size_t npwm = (size_t)K * 4 * maxlen;
     ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)K + KN));
     ST_TRY(ensure_scratch(c, &c->scan_f, &c->scan_f_cap, npwm + KN));

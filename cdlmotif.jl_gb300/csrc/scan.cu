@@ -344,14 +344,12 @@ int count_pfms(cdlgb_ctx* c, const int32_t* pos, const uint8_t* use_comp, const 
     for (int k = 0; k < K; ++k)
         if (lens[k] < 1 || lens[k] > maxlen)
             return cdlgb_seterr(c, CDLGB_EINVAL, "count_pfms: lens[%d]=%d", k, lens[k]);
-    for (int n = 0; n < N; ++n)          // in memory order: k fastest
-        for (int k = 0; k < K; ++k) {
-            const int p = pos[k + (size_t)K * n];
-            if (p < 0 || (p > 0 && p - 1 + lens[k] > L))
-                return cdlgb_seterr(c, CDLGB_EINVAL,
-                                    "count_pfms: window at pos[%d,%d]=%d (len %d) leaves the sequence (L=%d)",
-                                    k, n, p, lens[k], L);
-        }
+    if (const long long i = first_bad_position(pos, lens, K, (size_t)N, L); i >= 0) {
+        const int k = (int)(i % K), n = (int)(i / K);
+        return cdlgb_seterr(c, CDLGB_EINVAL,
+                            "count_pfms: window at pos[%d,%d]=%d (len %d) leaves the sequence (L=%d)",
+                            k, n, pos[i], lens[k], L);
+    }
     size_t ncnt = (size_t)4 * maxlen * K;
     ST_TRY(ensure_scratch(c, &c->scan_i, &c->scan_i_cap, (size_t)K + (size_t)K * N + ncnt + K));
     ST_TRY(ensure_scratch(c, &c->scan_u, &c->scan_u_cap, (size_t)K * N));

@@ -61,7 +61,7 @@ def dataset(wl=WORKLOAD, N=None):
 
 # DRAM bytes (read + write) of one launch on 1000 sequences of the L=200, K=64 workload,
 # from the ncu captures summarised in profiles/
-XITER_DRAM_BYTES_N1000 = 1403218688      # k_xiter, one launch = 15 X-steps
+XITER_DRAM_BYTES_N1000 = 1405720320      # k_xiter, one launch = 15 X-steps
 XWARP_DRAM_BYTES_N1000 = 1391571456      # k_xstep_warp, one launch = 1 X-step
 
 

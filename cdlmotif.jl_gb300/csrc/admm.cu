@@ -41,27 +41,6 @@ __device__ __forceinline__ float2 cjfma(float2 a, float2 b, float2 c) {  // conj
 }
 
 // ---------------------------------------------------------------- init kernels
-// X0 = randn masked to the rows (l-1) % 4 == 0 (CDL_setup.jl:191-192).  Lg % 4 == 0, so
-// those rows are the .x components of the float4s; element 4 j draws from counter 4 j.
-__global__ void k_randn_masked(float4* __restrict__ X, size_t n4, uint64_t seed) {
-    for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n4;
-         j += (size_t)gridDim.x * blockDim.x) {
-        const uint64_t h = splitmix64(seed * 0x2545F4914F6CDD1Dull ^ (uint64_t)(4 * j));
-        const float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
-        const float u2 = ((float)(h & 0xFFFFFFull) + 0.5f) * (1.0f / 16777216.0f);
-        X[j] = make_float4(sqrtf(-2.f * logf(u1)) * cospif(2.f * u2), 0.f, 0.f, 0.f);
-    }
-}
-
-__global__ void k_mask4(float4* __restrict__ X, size_t n4) {
-    // Lg % 4 == 0, so component .x of every float4 sits on a row with (l-1) % 4 == 0
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
-         i += (size_t)gridDim.x * blockDim.x) {
-        float4 v = X[i];
-        X[i] = make_float4(v.x, 0.f, 0.f, 0.f);
-    }
-}
-
 __global__ void k_bcast_plane(float4* __restrict__ dst, const float4* __restrict__ plane,
                               size_t pl4, size_t n4) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
@@ -429,10 +408,13 @@ __global__ void k_abssum(const float4* __restrict__ X, size_t n4, double* __rest
     if (threadIdx.x == 0) out[blockIdx.x] = acc;
 }
 
-// The initial X in one pass: drawn as k_randn_masked draws it, or the given X0 masked
-// as k_mask4 masks it; y2 = y3 = 0 (CDL_setup.jl:220-230); and the per-block sums of
-// |X| for the initial objective.  Launched on k_abssum's grid (304 blocks of kBlock), so
-// every thread visits k_abssum's indices in its order: the same sums, bit for bit.
+// The initial X in one pass (CDL_setup.jl:191-192): standard normal on the rows
+// (l-1) % 4 == 0 and zero elsewhere.  Lg % 4 == 0, so those rows are the .x components
+// of the float4s; element 4 j draws from counter 4 j of the seed's splitmix64 stream
+// (Box-Muller on two 24-bit uniforms).  A given X0 is masked to the same rows instead.
+// Also y2 = y3 = 0 (CDL_setup.jl:220-230) and the per-block sums of |X| for the initial
+// objective.  Launched on k_abssum's grid (304 blocks of kBlock), so every thread visits
+// k_abssum's indices in its order: the same sums, bit for bit.
 __global__ void k_init_x(float4* __restrict__ X, float4* __restrict__ y2, float4* __restrict__ y3,
                          size_t n4, uint64_t seed, int draw, double* __restrict__ out) {
     __shared__ double sh[32];

@@ -757,7 +757,6 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     k_init_x<<<152 * 2, kBlock, 0, s>>>((float4*)X, (float4*)c->y2, (float4*)c->y3, LMN / 4, seed,
                                         X0 ? 0 : 1, c->dred);
     LAUNCH_CHECK(c, "k_init_x");
-    c->absx_init = 1;
     // the spectral D-step (dspec.cu) where its transforms cover Lg and M
     c->dspec = 0;
     c->time_stale = 0;
@@ -830,6 +829,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     CU_TRY(c, cudaMemcpyAsync(c->G2, c->DX, LN * 4, cudaMemcpyDeviceToDevice, s));
     c->initialized = true;
     double obj = 0;
+    c->absx_init = 1;           // dred[0, 304) = k_init_x's sums of |X|, consumed here
     ST_TRY(admm_objective(c, &obj));
     c->obj_best = obj;
     return CDLGB_OK;

@@ -837,7 +837,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
 
 int admm_code_update(cdlgb_ctx* c, int iters) {
     cudaStream_t s = c->stream;
-    const size_t LMN = c->LMN, LN = c->LN;
+    const size_t LN = c->LN;
     const int F = c->F, M = c->M, N = c->N;
     if (iters > 0 && c->fused && fused_has_multi(c)) {
         // all iterations in one launch, the state on chip in between
@@ -898,7 +898,7 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
 
 int admm_dict_update(cdlgb_ctx* c, int iters) {
     cudaStream_t s = c->stream;
-    const size_t LMN = c->LMN, LN = c->LN, LM = c->LM;
+    const size_t LN = c->LN, LM = c->LM;
     const int F = c->F, M = c->M, N = c->N, Lg = c->Lg;
     for (int it = 0; it < iters; ++it) {
         cdlgb_phase_begin(c, PH_DSTEP);

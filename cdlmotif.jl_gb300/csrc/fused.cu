@@ -33,7 +33,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kMaxFactors = 12;
-constexpr int kMaxPrime = 31;
 
 // cos/sin(2 pi m / p) for the odd primes 3..31, concatenated
 __constant__ float2 c_trig[3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31];
@@ -305,7 +304,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_xstep_fused(XArgs A) {
         for (int idx = threadIdx.x; idx < B * Lg4; idx += blockDim.x) {
             int j = idx / Lg4;
             int l4 = idx - j * Lg4;
-            int ma = m0 + 2 * j, mb = ma + 1;
+            const int ma = m0 + 2 * j;
             bool hasb = (2 * j + 1) < Mc;
             size_t ba = ((size_t)n * M + ma) * Lg + 4 * (size_t)l4;
             size_t bb = ba + Lg;

@@ -52,7 +52,6 @@ def _pkg():
 
 
 def dataset(wl=WORKLOAD, N=None):
-    from importlib import import_module  # noqa: F401
     pkg = _pkg()
     n = wl["N"] if N is None else N
     bases, _, _ = pkg.synth.plant_dataset(wl["seed"], n, wl["L"], wl["widths"], wl["occ"])
@@ -162,7 +161,6 @@ def cpu_reference(steps: int, warmup: int, procs: int, per_proc: int):
     if procs == 1:
         from oracle import cdl_oracle  # noqa: F401
         times = []
-        import threading  # noqa: F401
 
         class _B:
             def wait(self):

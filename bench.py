@@ -573,12 +573,16 @@ def search_cpu_baseline(S, pwms, thresh, n_sample):
 
 
 def run_precision(args):
-    """The float32 path (fused X-step, float64 objective) against the all-FP64 GPU
-    reference from the same initial state, outer iteration by outer iteration: relative
-    L2 error of X, X_best, d, D_best, G1 and the objective gap."""
+    """Precision study on the N = 20000, L = 200, K = 64 workload: from one initial state,
+    the float32 CUDA path, the reference's statement order evaluated in float32 (torch,
+    full complex FFTs: the drift FP32 rounding alone causes in the reference) and an
+    all-FP64 reference (torch, half-spectrum form) are run outer iteration by outer
+    iteration; at each checkpoint the relative L2 distance of X, X_best, d, D_best, G1 and
+    the objective from FP64 is reported for both float32 runs, with the float32 path's
+    residual norms beside the FP64 ones."""
     import torch
     pkg = _pkg()
-    from cdlmotif_gb300.fp64ref import FP64Reference
+    from oracle.torch_admm import FP64Reference, LiteralADMM, relative_residuals
     wl = WORKLOAD
     bases = dataset(wl)
     S = pkg.synth.onehot(bases)
@@ -586,34 +590,66 @@ def run_precision(args):
                          sigma=wl["sigma"], csc_iter_num=wl["csc_iter"], cdl_iter_num=wl["cdl_iter"])
     c = pkg.init_cdl(setup, S, seed=wl["seed"])
     dev = "cuda:0"
+    chunk = 512
 
-    def rel(a32, b64):
-        a = torch.from_numpy(a32).to(dev, torch.float64)
-        return float((a - b64).norm() / b64.norm())
+    def rel(a, b64):
+        """relative L2 distance of a (numpy float32 or torch) from the float64 tensor b64,
+        summed in float64 over chunks of the first axis"""
+        num = den = 0.0
+        for i0 in range(0, b64.shape[0], chunk):
+            i1 = min(b64.shape[0], i0 + chunk)
+            x = a[i0:i1]
+            x = (torch.from_numpy(np.ascontiguousarray(x)) if isinstance(x, np.ndarray) else x)
+            x = x.to(dev, torch.float64)
+            num += float(((x - b64[i0:i1]) ** 2).sum())
+            den += float((b64[i0:i1] ** 2).sum())
+        return (num / den) ** 0.5
 
-    ref = FP64Reference(S, c.X, c.G1, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"],
-                        device=dev)
+    X0, D0 = c.X, c.G1
+    ref = FP64Reference(S, X0, D0, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"],
+                        device=dev, chunk=chunk)
+    lit = LiteralADMM(S, X0, D0, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"],
+                      device=dev, chunk=chunk, dtype=torch.float32)
+    del X0
+    at = sorted({int(v) for v in args.precision_at.split(",") if v})
     rows = []
-    t32 = t64 = 0.0
-    for it in range(1, args.precision_iters + 1):
+    secs = {"f32_cuda": 0.0, "f32_reference_order": 0.0, "f64": 0.0}
+    for it in range(1, at[-1] + 1):
         t0 = time.perf_counter()
         o32 = float(pkg.run_outer(c, 1)[0])
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        o64 = ref.run_outer(1)[0]
+        ol = lit.run_outer(1)[0]
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        t32 += t1 - t0
-        t64 += t2 - t1
-        rows.append({"outer_iteration": it, "objective_f32": o32, "objective_f64": o64,
-                     "objective_rel_gap": abs(o32 - o64) / abs(o64),
-                     "X_rel_l2": rel(c.X, ref.X), "d_rel_l2": rel(c.d, ref.d),
-                     "X_best_rel_l2": rel(c.X_best, ref.X_best),
-                     "D_best_rel_l2": rel(c.D_best, ref.D_best), "G1_rel_l2": rel(c.G1, ref.G1)})
+        o64 = ref.run_outer(1)[0]
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        secs["f32_cuda"] += t1 - t0
+        secs["f32_reference_order"] += t2 - t1
+        secs["f64"] += t3 - t2
+        if it not in at:
+            continue
+        row = {"outer_iteration": it, "objective_f64": o64,
+               "cuda_f32": {"objective_rel_gap": abs(o32 - o64) / abs(o64),
+                            "X": rel(c.X, ref.X), "X_best": rel(c.X_best, ref.X_best),
+                            "d": rel(c.d, ref.d), "D_best": rel(c.D_best, ref.D_best),
+                            "G1": rel(c.G1, ref.G1)},
+               "reference_order_f32": {"objective_rel_gap": abs(ol - o64) / abs(o64),
+                                       "X": rel(lit.X, ref.X), "X_best": rel(lit.X_best, ref.X_best),
+                                       "d": rel(lit.d, ref.d), "D_best": rel(lit.D_best, ref.D_best),
+                                       "G1": rel(lit.G1, ref.G1)},
+               "relative_residuals_f64": relative_residuals(ref.resid)}
+        if hasattr(c, "residuals"):
+            row["relative_residuals_cuda_f32"] = relative_residuals(c.residuals())
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
     c.close()
-    return {"metric": "precision: float32 path vs all-FP64 GPU reference", "workload": wl["name"],
-            "N": wl["N"], "rows": rows, "seconds_f32": t32, "seconds_f64": t64,
-            "note": "float64 objective / reductions in both; FP64 reference = torch float64 cuFFT"}
+    return {"metric": "precision: float32 CUDA path and float32 reference order vs all-FP64",
+            "workload": wl["name"], "N": wl["N"], "rows": rows, "seconds": secs,
+            "note": "same initial state for all three; float64 objective and residual sums; "
+                    "FP64 = torch float64 cuFFT (half-spectrum form); reference order = "
+                    "src/CDL/train.jl statement by statement in torch float32, c2c FFTs"}
 
 
 def main():
@@ -638,7 +674,8 @@ def main():
     ap.add_argument("--batched-n", type=int, default=64)
     ap.add_argument("--precision", action="store_true",
                     help="precision study: float32 GPU path vs an all-FP64 GPU reference")
-    ap.add_argument("--precision-iters", type=int, default=3)
+    ap.add_argument("--precision-at", default="1,3,10,100",
+                    help="outer iterations at which the precision study reports")
     ap.add_argument("--search", action="store_true",
                     help="motif-search stage: scans, non-overlap selection, extension, trim")
     ap.add_argument("--search-k", type=int, default=32)

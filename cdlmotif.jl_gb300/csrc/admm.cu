@@ -323,27 +323,6 @@ __global__ void k_dcons(const float4* __restrict__ d, float4* __restrict__ g1,
 
 // v1 = sum(d+g1)/N, v2 = sum(d+g3)/N, dmean = sum(d)/N;  G3 = projection2box!(v2)
 // (cdl_kernels.jl:37-51); P_D = 1 on rows l < filter_len.
-// the partial sums of k_dcons over already-updated duals: s1 = sum (d + g1),
-// s3 = sum (d + g3), sd = sum d per chunk of sequences (read only)
-__global__ void k_dsum(const float4* __restrict__ d, const float4* __restrict__ g1,
-                       const float4* __restrict__ g3, float4* __restrict__ part, size_t pl4,
-                       int N, int nchunk) {
-    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (j >= pl4) return;
-    int ch = blockIdx.y;
-    int n0 = (int)((int64_t)N * ch / nchunk), n1 = (int)((int64_t)N * (ch + 1) / nchunk);
-    float4 s1 = make_float4(0, 0, 0, 0), s3 = s1, sd = s1;
-    for (int n = n0; n < n1; ++n) {
-        size_t i = (size_t)n * pl4 + j;
-        float4 dv = d[i], a = g1[i], b = g3[i];
-        s1.x += dv.x + a.x; s1.y += dv.y + a.y; s1.z += dv.z + a.z; s1.w += dv.w + a.w;
-        s3.x += dv.x + b.x; s3.y += dv.y + b.y; s3.z += dv.z + b.z; s3.w += dv.w + b.w;
-        sd.x += dv.x; sd.y += dv.y; sd.z += dv.z; sd.w += dv.w;
-    }
-    part[((size_t)ch * 3 + 0) * pl4 + j] = s1;
-    part[((size_t)ch * 3 + 1) * pl4 + j] = s3;
-    part[((size_t)ch * 3 + 2) * pl4 + j] = sd;
-}
 __global__ void k_dfinish(const float* __restrict__ part, float* __restrict__ v1,
                           float* __restrict__ G3, float* __restrict__ dmean, size_t pl,
                           int Lg, int flen, int N, int nchunk) {
@@ -761,7 +740,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     c->dspec = 0;
     c->time_stale = 0;
     c->time_init = 0;
-    if (c->g1h && c->fused && fused_dfwd(c) && !fused_has_dstep(c)) {
+    if (c->g1h && c->fused && fused_dfwd(c)) {
         const char* e = getenv("CDLGB_DSPEC");
         if (!e || atoi(e) != 0) c->dspec = 1;
     }
@@ -935,16 +914,7 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             cdlgb_phase_end(c, PH_DSTEP);
             continue;
         }
-        if (c->fused && fused_has_dstep(c)) {
-            // transforms, solve, d, duals and G2 in one launch; then the means over n
-            c->dh_valid = 0;
-            ST_TRY(fused_dstep(c));
-            size_t pl4 = LM / 4;
-            dim3 g((unsigned)((pl4 + 255) / 256), (unsigned)c->nchunk);
-            k_dsum<<<g, 256, 0, s>>>((const float4*)c->d, (const float4*)c->g1,
-                                     (const float4*)c->g3, (float4*)c->part, pl4, N, c->nchunk);
-            LAUNCH_CHECK(c, "k_dsum");
-        } else {
+        {
             k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
             LAUNCH_CHECK(c, "k_sub");
             ST_TRY(r2c(c, N, c->sU, c->sUh));

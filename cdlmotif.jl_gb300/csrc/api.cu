@@ -154,6 +154,11 @@ int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out) {
         return CDLGB_ECUDA;
     }
     c->own_stream = true;
+    // load the allocation-free objective's module and look up its scratch on this
+    // device now, while the caller's memory is still free (lazy module loading would
+    // otherwise do it at the first cdlgb_objective_noalloc call); a failure here only
+    // leaves that lookup to the first call
+    (void)noalloc_warm_current_device();
     Ring* r = new (std::nothrow) Ring();
     if (r) {
         bool ok = true;

@@ -17,8 +17,8 @@ enum cdlgb_phase {
     PH_DSTEP,         // one whole D-step iteration
     PH_OBJ,           // objective / update_best
     PH_XFUSED,        // the fused X-step kernel alone
-    PH_DFUSED_A,      // fused D-step kernel, pass A
-    PH_DFUSED_B,      // fused D-step kernel, pass B
+    PH_SPARE_A,       // unused (keeps the reported slot order)
+    PH_SPARE_B,       // unused
     PH_SCAN,
     PH_COUNT
 };
@@ -157,7 +157,6 @@ int fused_supported(int Lg, int M);
 int fused_setup(cdlgb_ctx* c);
 void fused_free(cdlgb_ctx* c);
 int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs);
-int fused_dstep(cdlgb_ctx* c);
 int fused_absx(cdlgb_ctx* c, const double** part, int* n);
 size_t fused_scratch_bytes(int Lg, int M, int N);
 
@@ -183,11 +182,8 @@ int warp_plan_filters(void* p);
 int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* cs, int32_t* mc,
                    int32_t* n_out, int32_t* chosen);
 int fused_has_multi(cdlgb_ctx* c);
-// fused D-step (dfused.cu)
-void* dfused_plan_create(cdlgb_ctx* c, int* status);
-void dfused_plan_free(void* p);
-int dfused_step(cdlgb_ctx* c, void* p, const float* X);
-int fused_has_dstep(cdlgb_ctx* c);
+// noalloc.cu: scratch lookup of the allocation-free objective on the current device
+int noalloc_warm_current_device();
 // streaming forward transforms of the D-step (dstream.cu)
 void* dfwd_plan_create(cdlgb_ctx* c, int* status);
 void dfwd_plan_free(void* p);

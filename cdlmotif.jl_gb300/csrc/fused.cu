@@ -54,7 +54,6 @@ struct FusedPlan {
     double* absx_part;      // one partial sum of |X| per CTA
     void* warp;             // register-FFT variant (xwarp.cu) when Lg has one
     void* iter;             // multi-iteration register-FFT variant (xiter.cu)
-    void* dplan;            // fused D-step (dfused.cu)
     void* dfwd;             // streaming forward transforms of the D-step (dstream.cu)
 };
 
@@ -557,8 +556,6 @@ int fused_setup(cdlgb_ctx* c) {
     P->F = c->F;
     if (!getenv("CDLGB_GENERIC_FFT")) {
         int st = CDLGB_OK;
-        P->dplan = dfused_plan_create(c, &st);
-        if (st != CDLGB_OK) return st;
         P->dfwd = dfwd_plan_create(c, &st);
         if (st != CDLGB_OK) return st;
         P->iter = iter_plan_create(c, &st);
@@ -618,7 +615,6 @@ void fused_free(cdlgb_ctx* c) {
     if (P->absx_part) cudaFree(P->absx_part);
     warp_plan_free(P->warp);
     iter_plan_free(P->iter);
-    dfused_plan_free(P->dplan);
     dfwd_plan_free(P->dfwd);
     delete P;
     c->fplan = nullptr;
@@ -669,11 +665,6 @@ int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs) {
 void* fused_dfwd(cdlgb_ctx* c) {
     FusedPlan* P = (FusedPlan*)c->fplan;
     return P ? P->dfwd : nullptr;
-}
-
-int fused_has_dstep(cdlgb_ctx* c) {
-    FusedPlan* P = (FusedPlan*)c->fplan;
-    return P && P->dplan;
 }
 
 // The X-step autotuner: every register-FFT X-step variant that fits (multi-iteration
@@ -791,12 +782,6 @@ int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* c
     *n_out = (int32_t)cands.size();
     *chosen = best;
     return CDLGB_OK;
-}
-
-int fused_dstep(cdlgb_ctx* c) {
-    FusedPlan* P = (FusedPlan*)c->fplan;
-    if (!P || !P->dplan) return cdlgb_seterr(c, CDLGB_ENOTSUP, "no fused D-step for this size");
-    return dfused_step(c, P->dplan, c->Xb[c->xcur]);   // the current X
 }
 
 // partial sums of |X| written by the last fused X-step (one per CTA)

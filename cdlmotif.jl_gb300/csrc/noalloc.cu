@@ -19,7 +19,14 @@
 //     it and must be serialised by the caller.
 //   * The first call on a device looks up the scratch's device address
 //     (cudaGetSymbolAddress) with that device current and caches it; that first
-//     call should come before any stream capture.
+//     call should come before any stream capture.  cdlgb_create does the same
+//     lookup for its device, as a warm-up.
+//   * With CUDA's lazy module loading (the default since CUDA 12.2) the driver
+//     loads this module, and backs the 1 MiB array, only at that lookup.  A caller
+//     whose pool later takes (almost) all free memory must therefore make the
+//     first call, or create a context, on each device before the pool grows, or
+//     set CUDA_MODULE_LOADING=EAGER; otherwise that first lookup can fail for lack
+//     of memory (reported as CDLGB_ECUDA, nothing else is affected).
 #include "cdlgb_internal.h"
 
 #include <mutex>
@@ -61,13 +68,7 @@ __global__ void k_obj_per_seq(const float* __restrict__ X, const float* __restri
     const size_t cols = (size_t)M * Lg;
     const float* x = X + n * cols;
     double a = 0.0;
-    float fa = 0.f;
-    int cnt = 0;
-    for (size_t i = threadIdx.x; i < cols; i += blockDim.x) {
-        fa += fabsf(x[i]);
-        if (++cnt == 64) { a += (double)fa; fa = 0.f; cnt = 0; }
-    }
-    a += (double)fa;
+    for (size_t i = threadIdx.x; i < cols; i += blockDim.x) a += (double)fabsf(x[i]);
     double r = 0.0;
     for (int j = threadIdx.x; j < L4; j += blockDim.x) {
         const double d = (double)DX[n * Lg + gamma + j] - (double)S[n * L4 + j];
@@ -115,6 +116,13 @@ int scratch_for_current_device(double** out) {
 }
 
 }  // namespace
+
+// Warm-up for cdlgb_create: the scratch address of the current device, looked up
+// (and the module loaded) while the caller's memory is still free.
+int noalloc_warm_current_device() {
+    double* p = nullptr;
+    return scratch_for_current_device(&p);
+}
 
 extern "C" int cdlgb_objective_noalloc(const float* X, const float* DX, const float* S,
                                        int32_t L4, int32_t N, int32_t M, int32_t gamma,

@@ -336,7 +336,7 @@ int cdlgb_set_stream(cdlgb_ctx* ctx, void* cuda_stream);
 int cdlgb_profile(cdlgb_ctx* ctx, int32_t enable);
 
 /* Read the accumulated phase times: ms[8], counts[8] (order: X-step, D-step,
- * objective, fused X kernel, fused D kernel pass A, pass B, scan, reserved),
+ * objective, fused X kernel, two unused slots, scan, reserved),
  * the number of this library's kernel launches and of cuFFT executions. */
 int cdlgb_profile_read(cdlgb_ctx* ctx, double* ms, int64_t* counts, int64_t* launches,
                        int64_t* fft_calls, int32_t reset);
@@ -350,8 +350,12 @@ int cdlgb_profile_read(cdlgb_ctx* ctx, double* ms, int64_t* counts, int64_t* lau
  * with a fixed budget).  Its scratch is a static 1 MiB device array: at most 65536
  * sequences (larger N returns CDLGB_EINVAL before any GPU work); every call shares it,
  * so calls that overlap on the GPU race; the first call on a device looks up the
- * array's address and should come before any stream capture.  stream: cudaStream_t or
- * NULL (legacy default stream). */
+ * array's address and should come before any stream capture.  CUDA loads modules
+ * lazily by default, so the array is only backed by device memory at that lookup:
+ * make the first call (or a cdlgb_create on that device, which does the lookup as a
+ * warm-up) before a memory pool takes the free memory, or set
+ * CUDA_MODULE_LOADING=EAGER.  sum |X| is widened to float64 per element.
+ * stream: cudaStream_t or NULL (legacy default stream). */
 int cdlgb_objective_noalloc(const float* X, const float* DX, const float* S, int32_t L4,
                             int32_t N, int32_t M, int32_t gamma, float lambda, double* obj,
                             void* stream);

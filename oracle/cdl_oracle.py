@@ -197,6 +197,7 @@ def init_cdl(S: np.ndarray, M: int, filter_size: int, rho: float, sigma: float, 
     c.X_best = c.Y3.copy()
     c.obj_best = objective(c)
     c.D0, c.X0 = D, X
+    c.resid = np.zeros(13)
     return c
 
 
@@ -257,6 +258,32 @@ def code_update(c: CDLState, num_iter: int, sherman_const_csc: float = 2.0) -> N
         c.Y1h = _fft(c.Y1.astype(c.cdtype))                                  # :36
         c.Y3 = projectionX(c.X, c.y3).astype(c.dtype)                        # :40
         c.Y3h = _fft(c.Y3.astype(c.cdtype))                                  # :41
+    c.resid[0:5] = x_residuals(c)
+
+
+def x_residuals(c: CDLState) -> np.ndarray:
+    """Primal residuals of the final iterate of a code update, in float64: what the next
+    dual updates (src/CDL/train.jl:12-14) would add -- sum (X - shrink(X + y2))^2,
+    sum (X - projectionX(X + y3))^2, sum (DX - Y1)^2 -- and sum X^2, sum DX^2."""
+    X = c.X.astype(np.float64)
+    r2 = X - shrink(c.X + c.y2, c.lam).astype(np.float64)
+    r3 = X - projectionX(c.X, c.y3).astype(np.float64)
+    r1 = c.DX.astype(np.float64) - c.Y1.astype(np.float64)
+    return np.array([np.sum(r2 * r2), np.sum(r3 * r3), np.sum(r1 * r1), np.sum(X * X),
+                     np.sum(c.DX.astype(np.float64) ** 2)])
+
+
+def relative_residuals(r) -> dict:
+    """The stopping test's five relative residuals from a 13-value residual record:
+    primal of the code update (X - Y2, X - Y3 against |X|; DX - Y1 against |DX|), primal
+    of the D-step (the g1, g3 increments against |d|; the g2 increment against |Td|) and
+    the D-step's consensus dual residual (the change of G1, G3 against |G|)."""
+    tiny = 1e-300
+    return {"primal_x": np.sqrt((r[0] + r[1]) / max(r[3], tiny)),
+            "primal_dx": np.sqrt(r[2] / max(r[4], tiny)),
+            "primal_d": np.sqrt((r[5] + r[6]) / max(2.0 * r[8], tiny)),
+            "primal_td": np.sqrt(r[7] / max(r[9], tiny)),
+            "dual_d": np.sqrt((r[10] + r[11]) / max(r[12], tiny))}
 
 
 def dict_update(c: CDLState, num_iter: int, sherman_const_cdl: float = 2.0) -> None:
@@ -273,12 +300,20 @@ def dict_update(c: CDLState, num_iter: int, sherman_const_cdl: float = 2.0) -> N
         c.g1 = c.g1 + c.d - c.G1[None]; c.g1h = _fft(c.g1.astype(c.cdtype))  # :70
         c.g2 = c.g2 + c.Td - c.G2; c.g2h = _fft(c.g2.astype(c.cdtype))       # :71
         c.g3 = c.g3 + c.d - c.G3[None]; c.g3h = _fft(c.g3.astype(c.cdtype))  # :72
+        d64, Td64 = c.d.astype(np.float64), c.Td.astype(np.float64)
+        G1o, G3o = c.G1.astype(np.float64), c.G3.astype(np.float64)
+        c.resid[5:10] = [np.sum((d64 - G1o[None]) ** 2), np.sum((d64 - G3o[None]) ** 2),
+                         np.sum((Td64 - c.G2.astype(np.float64)) ** 2), np.sum(d64 * d64),
+                         np.sum(Td64 * Td64)]
         v2 = (np.sum(c.d + c.g3, axis=0) / c.N).astype(c.dtype)              # :76
         c.G3 = projection2box(v2, c.P_D)                                     # :77
         c.G3h = _fft(c.G3.astype(c.cdtype))                                  # :78
         v1 = (np.sum(c.d + c.g1, axis=0) / c.N).astype(c.dtype)              # :83
         c.G1 = prox_simplex_zeros(v1, c.P_D).astype(c.dtype)                 # :84
         c.G1h = _fft(c.G1.astype(c.cdtype))                                  # :85
+        G1n, G3n = c.G1.astype(np.float64), c.G3.astype(np.float64)
+        c.resid[10:13] = [c.N * np.sum((G1n - G1o) ** 2), c.N * np.sum((G3n - G3o) ** 2),
+                          c.N * (np.sum(G1n * G1n) + np.sum(G3n * G3n))]
 
 
 def update_best(c: CDLState) -> tuple[float, bool]:

@@ -38,17 +38,29 @@ def test_objective_noalloc_matches_context(pkg, built_lib):
     Sd = torch.from_numpy(np.ascontiguousarray(S)).to(dev)
     torch.cuda.synchronize()
     lib = built_lib
-    vals = []
-    for _ in range(2):
+
+    def call():
         out = C.c_double(0.0)
         st = lib.cdlgb_objective_noalloc(C.c_void_p(Xd.data_ptr()), C.c_void_p(DXd.data_ptr()),
                                          C.c_void_p(Sd.data_ptr()), 4 * L, N, M, gamma, 0.1,
                                          C.byref(out), None)
         assert st == 0
-        vals.append(out.value)
+        return out.value
+
+    # after a first call (which may load the module on a lazy-loading driver), further
+    # calls must leave the device's free memory unchanged: the entry point allocates
+    # nothing
+    vals = [call()]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    vals.append(call())
+    vals.append(call())
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
     for v in vals:
         assert v == pytest.approx(ref, rel=TOL_OBJ)
-    assert vals[0] == vals[1]
+    assert vals[0] == vals[1] == vals[2]
 
 
 def test_objective_noalloc_rejects_oversized(pkg, built_lib):

@@ -13,10 +13,11 @@ iteration of cdl_optimize (src/WRAPPER/wrap.jl:6-11): 15 X-steps, update_best!,
          (cdlgb_init_state), runs E outer iterations (cdlgb_run_outer) and reads the
          objectives and D_best back; the unit is the same (outer iterations/s).
 
-``--impl reference`` times the CPU restatement of the reference (the oracle: an
-FP64 NumPy port of src/CDL/train.jl, the reference having no host path of its own
-and Julia being absent) with a process per host core, each on its own slice of
-the sequences, and reports the same metric scaled to the full N.
+``--impl reference`` times the CPU restatement of the reference (oracle/cdl_cpu.cpp:
+src/CDL/train.jl's statements in float32 on host arrays with full complex FFTs,
+OpenMP over the sequences on every host core; the reference has no host path of its
+own and Julia is absent) on the first 2000 sequences, one outer iteration per step,
+and reports the same metric scaled to the full N (the factor is in the line).
 
 ``--impl refstruct`` times the reference-structured CUDA baseline (baseline/refstruct.cu:
 the reference's CUDA.jl statements restated one for one, full-spectrum cuFFT C2C,
@@ -27,7 +28,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import multiprocessing as mp
 import os
 import subprocess
 import sys
@@ -128,66 +128,37 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------ CPU leg
-def _cpu_worker(args):
-    """Run the oracle on a slice of sequences: W + K outer iterations, each between
-    two barrier waits so the parent can time the step across all workers."""
-    bases, wl, barrier, steps, warmup = args
-    from oracle import cdl_oracle as O
-    N, L = bases.shape
-    S = np.zeros((N, L, 4), np.float32)
-    S[np.arange(N)[:, None], np.arange(L)[None], bases] = 1
-    S = S.reshape(N, 4 * L)
-    Lg = 4 * L + 8 * wl["filter_size"]
-    rng = np.random.default_rng(1)
-    X0 = rng.standard_normal((N, wl["M"], Lg)).astype(np.float32)
-    D0 = rng.standard_normal((wl["M"], Lg)).astype(np.float32)
-    c = O.init_cdl(S, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"], X0=X0, D0=D0)
-    for _ in range(warmup + steps):
-        if barrier is not None:
-            barrier.wait()
-        O.code_update(c, wl["csc_iter"])
-        O.update_best(c)
-        O.dict_update(c, wl["cdl_iter"])
-        if barrier is not None:
-            barrier.wait()
-    return True
-
-
-def cpu_reference(steps: int, warmup: int, procs: int, per_proc: int):
-    """Times the oracle with `procs` processes of `per_proc` sequences each; returns
-    (outer iterations/s scaled to the full N, ms per sample step, sample text)."""
+def cpu_reference(steps: int, warmup: int, n_sample: int, threads: int = 0):
+    """Times the float32 C++/OpenMP CPU restatement of the reference (oracle/cdl_cpu.cpp:
+    src/CDL/train.jl's statements on host arrays, full complex FFTs) with `threads`
+    OpenMP threads (0 = every host core) on the first n_sample sequences of the
+    workload: W untimed and K timed outer iterations.  Returns (outer iterations/s
+    scaled to the full N, mean ms per sample step, threads, sample text)."""
+    from oracle.cdl_cpu import CPUADMM, threads as omp_threads
+    pkg = _pkg()
     wl = WORKLOAD
-    bases = dataset(wl, N=procs * per_proc)
-    if procs == 1:
-        from oracle import cdl_oracle  # noqa: F401
-        times = []
-
-        class _B:
-            def wait(self):
-                times.append(time.perf_counter())
-        _cpu_worker((bases, wl, _B(), steps, warmup))
-        t = np.diff(np.array(times))[0::2][warmup:]
-    else:
-        ctx = mp.get_context("spawn")
-        barrier = ctx.Manager().Barrier(procs + 1)
-        with ctx.Pool(procs) as pool:
-            res = pool.map_async(_cpu_worker, [(bases[i * per_proc:(i + 1) * per_proc], wl, barrier,
-                                                steps, warmup) for i in range(procs)])
-            t = []
-            for s in range(warmup + steps):
-                barrier.wait()
-                t0 = time.perf_counter()
-                barrier.wait()
-                if s >= warmup:
-                    t.append(time.perf_counter() - t0)
-            res.get()
-        t = np.array(t)
+    bases = dataset(wl, N=n_sample)
+    S = pkg.synth.onehot(bases)
+    Lg = 4 * wl["L"] + 8 * wl["filter_size"]
+    X0 = pkg.synth.init_X0(1, n_sample, wl["M"], Lg)
+    D0 = pkg.synth.init_D0_unit_norm(1, wl["M"], Lg, 4 * wl["filter_size"])
+    c = CPUADMM(S, X0, D0, wl["M"], wl["filter_size"], wl["rho"], wl["sigma"], wl["lam"],
+                threads=threads)
+    nt = threads or omp_threads()
+    t = []
+    for s in range(warmup + steps):
+        t0 = time.perf_counter()
+        c.run_outer(1, wl["csc_iter"], wl["cdl_iter"])
+        if s >= warmup:
+            t.append(time.perf_counter() - t0)
+    c.close()
     sec = float(np.mean(t))
-    seqs = procs * per_proc
-    rate = 1.0 / (sec * wl["N"] / seqs)
-    sample = (f"{seqs} of {wl['N']} sequences ({procs} process(es) x {per_proc}), one outer "
-              f"iteration per step, FP64 NumPy oracle; rate scaled by N/{seqs}")
-    return rate, sec * 1e3, sample
+    factor = wl["N"] / n_sample
+    rate = 1.0 / (sec * factor)
+    sample = (f"{n_sample} of {wl['N']} sequences, one outer iteration per step, float32 C++/OpenMP "
+              f"restatement of the reference (full complex FFTs) on {nt} threads; rate = "
+              f"1 / (seconds per step x {factor:g}) (extrapolation factor {factor:g})")
+    return rate, sec * 1e3, nt, sample
 
 
 # ------------------------------------------------------------------------ GPU leg
@@ -660,7 +631,10 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference", "refstruct"])
     ap.add_argument("--fft-mode", type=int, default=0, help="0 auto, 1 cuFFT, 2 fused")
     ap.add_argument("--e2e-outer", type=int, default=3)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-sample", type=int, default=1000,
+                    help="sequences of the CPU baseline leg (one outer iteration)")
+    ap.add_argument("--ref-sample", type=int, default=2000,
+                    help="sequences per step of --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=0, help="override N (small cases for profiling)")
     ap.add_argument("--skip-e2e", action="store_true")
@@ -714,13 +688,14 @@ def main():
     if args.impl == "reference":
         if world > 1 and rank != 0:
             return
-        procs = os.cpu_count() or 1
-        rate, ms, sample = cpu_reference(args.steps, args.warmup, procs, per_proc=2)
+        rate, ms, nt, sample = cpu_reference(args.steps, args.warmup, args.ref_sample)
         line = {"metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / rate,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded planted motifs)", "config": config, "impl": "reference",
-                "cpu_baseline": {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
+                "note": "ms_per_step is the measured time of one step on the sample; value is "
+                        "scaled to the full N by the extrapolation factor in cpu_baseline.sample",
+                "cpu_baseline": {"value": rate, "unit": UNIT, "cores": nt, "kind": "port",
                                  "sample": sample, "sample_ms_per_step": ms},
                 "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -738,11 +713,8 @@ def main():
     # the CPU baseline runs before any GPU call, single process, bounded sample
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        per = 2
-        r1, ms1, _ = cpu_reference(1, 0, 1, per)
-        k = max(1, int(args.cpu_seconds / max(ms1 / 1e3, 1e-3)))
-        rate, ms, sample = cpu_reference(min(k, 20), 0, 1, per)
-        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+        rate, ms, nt, sample = cpu_reference(1, 0, args.cpu_sample)
+        cpu = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample}
     r = run_gpu(args, rank, world)
     if rank != 0:
         return

@@ -81,6 +81,7 @@ class CDLSetup:
     iter_num: int = 10
     std_threshold_multiplier: float = 1.0
     num_train: int = 2
+    stop_tol: float = 0.0     # stopping test of run_outer; 0 = the reference's fixed count
 
     def params(self, device: int = 0, fft_mode: int = 0, init_mode: int = 0,
                hbm_budget_bytes: int = 0) -> CdlgbParams:
@@ -93,6 +94,7 @@ class CDLSetup:
         p.std_threshold_multiplier = float(self.std_threshold_multiplier)
         p.device, p.fft_mode, p.init_mode = int(device), int(fft_mode), int(init_mode)
         p.hbm_budget_bytes = int(hbm_budget_bytes)
+        p.stop_tol = float(self.stop_tol)
         return p
 
 
@@ -242,6 +244,27 @@ class CDL:
                                              out.nbytes))
         return out
 
+    RESIDUALS = ("x_y2", "x_y3", "x_y1", "x_norm", "dx_norm", "d_g1", "d_g3", "d_g2", "d_norm",
+                 "td_norm", "dual_G1", "dual_G3", "G_norm", "rel_primal_x", "rel_primal_dx",
+                 "rel_primal_d", "rel_primal_td", "rel_dual_d", "rel_max")
+
+    def residuals(self) -> np.ndarray:
+        """The residual record (19 float64, include/cdlgb.h: primal residuals of the last
+        code update's final iterate, the last D-step's dual increments and consensus
+        change, the relative residuals of the stopping test)."""
+        out = np.zeros(19, np.float64)
+        _check(self._h, _lib.lib().cdlgb_get(self._h, 19, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def relative_residuals(self) -> dict:
+        return dict(zip(self.RESIDUALS[13:], (float(v) for v in self.residuals()[13:])))
+
+    @property
+    def outer_done(self) -> int:
+        v = C.c_int32()
+        _check(self._h, _lib.lib().cdlgb_get(self._h, 20, C.cast(C.byref(v), C.c_void_p), 4))
+        return v.value
+
     @property
     def obj_best(self) -> float:
         v = C.c_double()
@@ -313,10 +336,12 @@ def update_best(c: CDL) -> tuple[float, bool]:
 
 
 def run_outer(c: CDL, iter_num: int) -> np.ndarray:
-    """iter_num passes of cdl_optimize's loop body (src/WRAPPER/wrap.jl:6-11)."""
+    """iter_num passes of cdl_optimize's loop body (src/WRAPPER/wrap.jl:6-11); fewer
+    when the setup's stop_tol > 0 and the stopping test passes (one objective per pass
+    run)."""
     objs = np.zeros(max(iter_num, 1), np.float64)
     _check(c._h, _lib.lib().cdlgb_run_outer(c._h, int(iter_num), ptr(objs, C.c_double)))
-    return objs[:iter_num]
+    return objs[:c.outer_done]
 
 
 def code_threshold(c: CDL) -> float:

@@ -618,6 +618,7 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     b += ch * M * (2 * Lg * 4 + 3 * F * 8);             // cuFFT-path scratch, one chunk
     b += ch * M * Lg * 4;                               // cuFFT work area (estimate)
     b += 64ull * 3 * LM * 4;                    // D-step partials
+    b += resid_part_doubles(N, (int)F, 1 << 16) * 8 + 2 * LM * 4;   // residual partials, G_old
     b += (64u << 20);                           // reductions, scan scratch, slack
     return b;
 }
@@ -689,6 +690,9 @@ int admm_alloc(cdlgb_ctx* c) {
     ST_TRY(A((void**)&c->dred, (size_t)c->nred * 4 * sizeof(double)));
     ST_TRY(A((void**)&c->dscalar, 8 * sizeof(double)));
     CU_TRY(c, cudaMallocHost((void**)&c->hscalar, 8 * sizeof(double)));
+    ST_TRY(A((void**)&c->dres, RESIDUAL_COUNT * sizeof(double)));
+    ST_TRY(A((void**)&c->rpart, resid_part_doubles(c->N, c->F, c->dslots) * sizeof(double)));
+    ST_TRY(A((void**)&c->Gprev, 2 * LM * 4));
     return CDLGB_OK;
 }
 
@@ -703,7 +707,11 @@ void admm_free(cdlgb_ctx* c) {
     if (c->dred) cudaFree(c->dred);
     if (c->dscalar) cudaFree(c->dscalar);
     if (c->hscalar) cudaFreeHost(c->hscalar);
+    if (c->dres) cudaFree(c->dres);
+    if (c->rpart) cudaFree(c->rpart);
+    if (c->Gprev) cudaFree(c->Gprev);
     c->dred = nullptr; c->dscalar = nullptr; c->hscalar = nullptr;
+    c->dres = nullptr; c->rpart = nullptr; c->Gprev = nullptr;
     free_plans(c);
 }
 
@@ -729,6 +737,8 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     c->best_is_cur = 1;
     c->absx_fused = 0;
     c->dh_valid = 0;
+    c->outer_done = 0;
+    CU_TRY(c, cudaMemsetAsync(c->dres, 0, RESIDUAL_COUNT * sizeof(double), c->stream));
     float* X = c->Xb[0];
     // X0 (CDL_setup.jl:191-192): given, or standard normal; masked to the 4-stride; with
     // y2 = y3 = 0 and sum |X| for the initial objective in the same pass
@@ -829,6 +839,11 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
             c->xcur = 1 - c->xcur;
             c->best_is_cur = 0;
         }
+        // the residuals of the final iterate, from the kernel's store pass
+        const double* rp = nullptr;
+        int nr = 0;
+        if (fused_resid(c, &rp, &nr)) ST_TRY(resid_x_from_parts(c, rp, nr));
+        else ST_TRY(resid_x_from_arrays(c, cur_X(c)));
         cdlgb_phase_end_n(c, PH_XSTEP, iters);
         return CDLGB_OK;
     }
@@ -870,6 +885,7 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
             c->xcur = 1 - c->xcur;
             c->best_is_cur = 0;
         }
+        if (it == iters - 1) ST_TRY(resid_x_from_arrays(c, cur_X(c)));
         cdlgb_phase_end(c, PH_XSTEP);
     }
     return CDLGB_OK;
@@ -895,21 +911,25 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                 ST_TRY(dspec_launch(c, c->sAh, c->G3h, n0, n0 + cn, slot0));
                 slot0 += dspec_nsub(cn, F, c->nsm);
             }
+            ST_TRY(resid_d_from_spec_parts(c, slot0 * ((F + 31) / 32)));
             ST_TRY(c2r(c, N, c->sVh, c->Td));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
                                                          c->gamma, LN, c->p.sigma);
             LAUNCH_CHECK(c, "k_dg2");
+            ST_TRY(resid_td(c));
             // the three sums over n, back in the time domain: part as one chunk
             ST_TRY(dspec_sums(c, c->G3h, c->sumspec));
             ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part));
             c->time_stale = 1;
             c->time_init = 0;
             int flen = 4 * c->p.filter_size;
+            ST_TRY(resid_save_G(c));
             k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
                                                                    LM, Lg, flen, N, 1);
             LAUNCH_CHECK(c, "k_dfinish");
             k_dprox<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->vbar, c->G1, Lg, M, flen);
             LAUNCH_CHECK(c, "k_dprox");
+            ST_TRY(resid_dual_and_finish(c));
             ST_TRY(refresh_G1h(c));
             cdlgb_phase_end(c, PH_DSTEP);
             continue;
@@ -957,13 +977,17 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                                       (const float4*)c->G1, (const float4*)c->G3,
                                       (float4*)c->part, pl4, N, c->nchunk);
             LAUNCH_CHECK(c, "k_dcons");
+            ST_TRY(resid_td(c));
+            ST_TRY(resid_d_from_arrays(c));
         }
         int flen = 4 * c->p.filter_size;
+        ST_TRY(resid_save_G(c));
         k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
                                                                LM, Lg, flen, N, c->nchunk);
         LAUNCH_CHECK(c, "k_dfinish");
         k_dprox<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->vbar, c->G1, Lg, M, flen);
         LAUNCH_CHECK(c, "k_dprox");
+        ST_TRY(resid_dual_and_finish(c));
         ST_TRY(refresh_G1h(c));
         cdlgb_phase_end(c, PH_DSTEP);
     }

@@ -120,6 +120,7 @@ int cdlgb_params_default(cdlgb_params* p) {
     p->init_mode = 0;
     p->fft_mode = 0;
     p->hbm_budget_bytes = 0;
+    p->stop_tol = 0.f;
     return CDLGB_OK;
 }
 
@@ -133,6 +134,8 @@ static int check_params(cdlgb_ctx* c, const cdlgb_params* p) {
         return cdlgb_seterr(c, CDLGB_EINVAL, "sherman constants must be > 0");
     if (p->fft_mode < 0 || p->fft_mode > 2)
         return cdlgb_seterr(c, CDLGB_EINVAL, "fft_mode=%d (0 auto, 1 cuFFT, 2 fused)", p->fft_mode);
+    if (!(p->stop_tol >= 0.f))
+        return cdlgb_seterr(c, CDLGB_EINVAL, "stop_tol must be >= 0 (0 = fixed iteration count)");
     return CDLGB_OK;
 }
 
@@ -424,6 +427,7 @@ int cdlgb_update_best(cdlgb_ctx* c, double* obj, int32_t* improved) {
 int cdlgb_run_outer(cdlgb_ctx* c, int32_t iter_num, double* objs) {
     NEED_INIT(c);
     if (iter_num < 0) return cdlgb_seterr(c, CDLGB_EINVAL, "iter_num < 0");
+    c->outer_done = 0;
     for (int it = 0; it < iter_num; ++it) {
         ST_TRY(admm_code_update(c, c->p.csc_iter_num));
         double o = 0;
@@ -431,6 +435,14 @@ int cdlgb_run_outer(cdlgb_ctx* c, int32_t iter_num, double* objs) {
         ST_TRY(admm_update_best(c, &o, &imp));
         ST_TRY(admm_dict_update(c, c->p.cdl_iter_num));
         if (objs) objs[it] = o;
+        c->outer_done = it + 1;
+        if (c->p.stop_tol > 0.f) {
+            // the stopping test: the largest relative residual (float64, on the device)
+            CU_TRY(c, cudaMemcpyAsync(c->hscalar + 7, c->dres + RESIDUAL_REL_MAX, sizeof(double),
+                                      cudaMemcpyDeviceToHost, c->stream));
+            CU_TRY(c, cudaStreamSynchronize(c->stream));
+            if (c->hscalar[7] <= (double)c->p.stop_tol) break;
+        }
     }
     return CDLGB_OK;
 }
@@ -480,6 +492,11 @@ int cdlgb_get(cdlgb_ctx* c, int32_t field, void* dst, size_t bytes) {
         case CDLGB_FIELD_OBJ_BEST:
             if (bytes != sizeof(double)) return cdlgb_seterr(c, CDLGB_EINVAL, "obj_best is one float64");
             *(double*)dst = c->obj_best;
+            return CDLGB_OK;
+        case CDLGB_FIELD_RESIDUALS: src = c->dres; want = RESIDUAL_COUNT * sizeof(double); break;
+        case CDLGB_FIELD_OUTER_DONE:
+            if (bytes != sizeof(int32_t)) return cdlgb_seterr(c, CDLGB_EINVAL, "outer_done is one int32");
+            *(int32_t*)dst = c->outer_done;
             return CDLGB_OK;
         default: return cdlgb_seterr(c, CDLGB_EINVAL, "unknown field %d", field);
     }

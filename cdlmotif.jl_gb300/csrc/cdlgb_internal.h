@@ -23,6 +23,31 @@ enum cdlgb_phase {
     PH_COUNT
 };
 
+// The residual record (float64 on the device, resid.cu), in order; read with
+// cdlgb_get(CDLGB_FIELD_RESIDUALS).
+enum cdlgb_residual {
+    RESIDUAL_X_Y2 = 0,        // sum (X - shrink(X + y2))^2        after a code update
+    RESIDUAL_X_Y3,            // sum (X - projectionX(X + y3))^2
+    RESIDUAL_X_Y1,            // sum (DX - Y1)^2
+    RESIDUAL_X_NORM,          // sum X^2
+    RESIDUAL_DX_NORM,         // sum DX^2
+    RESIDUAL_D_G1,            // sum (d - G1_old)^2               after a D-step
+    RESIDUAL_D_G3,            // sum (d - G3_old)^2
+    RESIDUAL_D_G2,            // sum (Td - G2)^2
+    RESIDUAL_D_NORM,          // sum d^2
+    RESIDUAL_TD_NORM,         // sum Td^2
+    RESIDUAL_DUAL_G1,         // N sum (G1 - G1_old)^2
+    RESIDUAL_DUAL_G3,         // N sum (G3 - G3_old)^2
+    RESIDUAL_G_NORM,          // N (sum G1^2 + sum G3^2)
+    RESIDUAL_REL_PRIMAL_X,    // sqrt((X_Y2 + X_Y3) / X_NORM)
+    RESIDUAL_REL_PRIMAL_DX,   // sqrt(X_Y1 / DX_NORM)
+    RESIDUAL_REL_PRIMAL_D,    // sqrt((D_G1 + D_G3) / (2 D_NORM))
+    RESIDUAL_REL_PRIMAL_TD,   // sqrt(D_G2 / TD_NORM)
+    RESIDUAL_REL_DUAL_D,      // sqrt((DUAL_G1 + DUAL_G3) / G_NORM)
+    RESIDUAL_REL_MAX,         // the largest of the five: the stopping test's value
+    RESIDUAL_COUNT
+};
+
 struct cdlgb_ctx {
     cdlgb_params p;
     int dev = 0;
@@ -83,6 +108,12 @@ struct cdlgb_ctx {
     double* dscalar = nullptr;                        // device scalars
     double* hscalar = nullptr;                        // pinned host mirror
     double obj_best = 0.0;
+    // residual record (RESIDUAL_COUNT float64), its per-block partials, G1 and G3 of
+    // the D-step before their update (2 LM), outer iterations of the last run_outer
+    double* dres = nullptr;
+    double* rpart = nullptr;
+    float* Gprev = nullptr;
+    int outer_done = 0;
 
     // fused path twiddles / plan
     void* fplan = nullptr;
@@ -182,6 +213,18 @@ int warp_plan_filters(void* p);
 int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* cs, int32_t* mc,
                    int32_t* n_out, int32_t* chosen);
 int fused_has_multi(cdlgb_ctx* c);
+// resid.cu: residual norms and the stopping test
+size_t resid_part_doubles(int N, int F, int slots);
+int resid_finish(cdlgb_ctx* c);
+int resid_x_from_parts(cdlgb_ctx* c, const double* part, int nb);
+int resid_x_from_arrays(cdlgb_ctx* c, const float* X);
+int resid_d_from_spec_parts(cdlgb_ctx* c, int nb);
+int resid_d_from_arrays(cdlgb_ctx* c);
+int resid_td(cdlgb_ctx* c);
+int resid_save_G(cdlgb_ctx* c);
+int resid_dual_and_finish(cdlgb_ctx* c);
+int iter_resid(void* p, const double** part, int* n);
+int fused_resid(cdlgb_ctx* c, const double** part, int* n);
 // noalloc.cu: scratch lookup of the allocation-free objective on the current device
 int noalloc_warm_current_device();
 // streaming forward transforms of the D-step (dstream.cu)

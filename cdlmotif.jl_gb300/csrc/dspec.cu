@@ -42,6 +42,8 @@ struct SArgs {
     const float2* Zh;     // (N, F): rfft(G2 - g2)
     float2* Th;           // (N, F): scale * sum_m Y3h rfft(d_old)
     float2* part;         // (slots, 2, M, F): sums of d + g1 and of d over a sub-range
+    double* rpart;        // (slots, nbb, 3): Parseval sums of |d-hat - G1-hat|^2,
+                          // |d-hat - G3-hat|^2, |d-hat|^2 of a CTA (the residual record)
     int N, M, F, c0, c1, slot0;
     float kd, scale;
 };
@@ -79,6 +81,10 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     float2 s1[MW], sd[MW];
 #pragma unroll
     for (int k = 0; k < MW; ++k) s1[k] = sd[k] = make_float2(0.f, 0.f);
+    // compensated (Kahan) float32 sums over this thread's sequences of the g1 and g3
+    // increments' and d's squared magnitudes (Parseval weights: 1 at the edge bins, 2
+    // elsewhere), combined in float64 at the end
+    float rs[3] = {0.f, 0.f, 0.f}, rc[3] = {0.f, 0.f, 0.f};
     __syncthreads();
     const int fl = on ? f : 0;                             // lanes past F load bin 0
     // staging: [2][kArr][MW][threads], each thread's own slots
@@ -169,6 +175,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             const float inv = 1.f / (B + A.kd);
             const float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
             const float2 W = csub2(z, beta);
+            float q[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int k = 0; k < MW; ++k) {
                 const int m = w + kWarps * k;
@@ -177,13 +184,42 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
                 if (edge) dh.y = 0.f;                      // the transform of a real d
                 const size_t i = (size_t)n * M * F + (size_t)m * F + f;
                 // g1 += d - G1 with G1 before the update (train.jl:70)
-                const float2 g1n = cadd2(g1v[k], csub2(dh, G1s[m * kBins + lane]));
+                const float2 e1 = csub2(dh, G1s[m * kBins + lane]);
+                const float2 g1n = cadd2(g1v[k], e1);
                 A.Dh[i] = dh;
                 A.g1h[i] = g1n;
                 s1[k] = cadd2(s1[k], cadd2(dh, g1n));
                 sd[k] = cadd2(sd[k], dh);
+                const float2 e3 = csub2(dh, G3s[m * kBins + lane]);   // g3 += d - G3 (:72)
+                q[0] = fmaf(e1.x, e1.x, fmaf(e1.y, e1.y, q[0]));
+                q[1] = fmaf(e3.x, e3.x, fmaf(e3.y, e3.y, q[1]));
+                q[2] = fmaf(dh.x, dh.x, fmaf(dh.y, dh.y, q[2]));
+            }
+            const float wt = edge ? 1.f : 2.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float y = __fsub_rn(__fmul_rn(wt, q[k]), rc[k]);
+                const float t = __fadd_rn(rs[k], y);
+                rc[k] = __fsub_rn(__fsub_rn(t, rs[k]), y);
+                rs[k] = t;
             }
             if (w == 0) A.Th[(size_t)n * F + f] = make_float2(T.x * A.scale, T.y * A.scale);
+        }
+    }
+    {
+        // the CTA's residual partials, in float64, added in warp order
+        __shared__ double rsh[3][kWarps];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double v = (double)rs[k] - (double)rc[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) rsh[k][w] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            double t = 0.0;
+            for (int v = 0; v < kWarps; ++v) t += rsh[threadIdx.x][v];
+            A.rpart[((size_t)(A.slot0 + j) * gridDim.x + blockIdx.x) * 3 + threadIdx.x] = t;
         }
     }
     if (!on) return;
@@ -294,7 +330,7 @@ int dspec_slots(int N, int chunk, int F, int nsm) {
 int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int c1, int slot0) {
     SArgs a;
     a.Yh = Yh; a.G1h = c->G1h; a.G3h = G3h; a.Dg = c->Dg; a.Dh = c->Dhs; a.g1h = c->g1h;
-    a.Zh = c->sUh; a.Th = c->sVh; a.part = c->spart;
+    a.Zh = c->sUh; a.Th = c->sVh; a.part = c->spart; a.rpart = c->rpart;
     a.N = c->N; a.M = c->M; a.F = c->F; a.c0 = c0; a.c1 = c1; a.slot0 = slot0;
     a.kd = c->p.sherman_const_cdl; a.scale = 1.f / (float)c->Lg;
     const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)dspec_nsub(c1 - c0, c->F, c->nsm));

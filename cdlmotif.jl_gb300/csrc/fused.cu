@@ -784,6 +784,13 @@ int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* c
     return CDLGB_OK;
 }
 
+// the X-step residual partials of the last multi-iteration launch (five per CTA)
+int fused_resid(cdlgb_ctx* c, const double** part, int* n) {
+    FusedPlan* P = (FusedPlan*)c->fplan;
+    if (!P || !P->iter) return 0;
+    return iter_resid(P->iter, part, n);
+}
+
 // partial sums of |X| written by the last fused X-step (one per CTA)
 int fused_absx(cdlgb_ctx* c, const double** part, int* n) {
     FusedPlan* P = (FusedPlan*)c->fplan;

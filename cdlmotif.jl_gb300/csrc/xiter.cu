@@ -42,6 +42,7 @@ struct IArgs {
     const float* Ah;
     const float2* tw2;      // [P][N1] exp(-2 pi i n1 k2 / Lg)
     double* absx_part;
+    double* res_part;       // per CTA: the five X-step residual sums of the final iterate
     int N, M, L4, gamma, iters;
     float lam, rho, kc;
     int ld, ld3;            // row strides (pairs) of the y2 and compacted y3 rows in shared memory
@@ -169,7 +170,10 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     float* Ahs = y1s + Lg;                                 // [Fp] sum_m |G1h|^2
     float* Ss = Ahs + Fp;                                  // [L4] this sequence's W'S window
     __shared__ double red[NT / 32];
+    // per warp: sums of (X - Y2)^2, (X - Y3)^2, X^2, (DX - Y1)^2, DX^2 of the final iterates
+    __shared__ double rsum[NT / 32][5];
 
+    for (int t = threadIdx.x; t < 5 * (NT / 32); t += blockDim.x) (&rsum[0][0])[t] = 0.0;
     for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
     for (int t = threadIdx.x; t < F; t += blockDim.x) Ahs[t] = A.Ah[t];
     __syncthreads();
@@ -294,6 +298,10 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
             inv_step2<N1, P, false>(sb, gl, act, tw2);
             const bool last = t == A.iters - 1;
             if (act) inv_step1<N1, P, true>(sb, gl, tw2);   // X (or DX) at T[n2][gl], l = gl + N1 n2
+            // residuals of the final iterate: what the next dual updates would add
+            // (train.jl:12-14): X - shrink(X + y2), X - projectionX(X + y3) (X off the
+            // kept rows; +0 on them, where y3 = +0), DX - Y1
+            float q2 = 0.f, q3 = 0.f, qx = 0.f, q1 = 0.f, qd = 0.f;
             if (pair) {
                 if (!last) {
 #pragma unroll 8
@@ -325,6 +333,13 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                         A.y3[ra + Lg + o] = a3.y;
                         s += fabsf(xv.x);
                         s += fabsf(xv.y);
+                        const float2 t2 = cadd(xv, a2);
+                        const float2 r2 = csub(xv, csub(t2, f2(fminf(fmaxf(t2.x, -lam), lam),
+                                                               fminf(fmaxf(t2.y, -lam), lam))));
+                        const float sx = fmaf(xv.x, xv.x, xv.y * xv.y);
+                        q2 = fmaf(r2.x, r2.x, fmaf(r2.y, r2.y, q2));
+                        if (!keep) q3 += sx;
+                        qx += sx;
                     }
                     absacc += (double)s;
                 }
@@ -349,9 +364,21 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                         A.DX[r + o] = dx;
                         A.Y1[r + o] = Y1n;
                         A.y1[r + o] = yp;
+                        const float e = dx - Y1n;
+                        q1 = fmaf(e, e, q1);
+                        qd = fmaf(dx, dx, qd);
                     }
                 }
                 if (!last) fwd_step1<N1, P>(sb, gl, tw2);
+            }
+            if (last) {
+                // one float64 partial per warp and sequence, added in warp order
+                double v[5] = {(double)q2, (double)q3, (double)qx, (double)q1, (double)qd};
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+                    if (lane == 0) rsum[threadIdx.x >> 5][k] += v[k];
+                }
             }
         }
     }
@@ -364,6 +391,11 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
         A.absx_part[blockIdx.x] = t;
+    }
+    if (threadIdx.x < 5) {
+        double t = 0.0;
+        for (int w = 0; w < NT / 32; ++w) t += rsum[w][threadIdx.x];
+        A.res_part[(size_t)blockIdx.x * 5 + threadIdx.x] = t;
     }
 }
 
@@ -402,6 +434,7 @@ struct IterPlan {
     size_t smem;
     float2* tw2;
     double* absx_part;
+    double* res_part;
 };
 
 }  // namespace
@@ -469,11 +502,13 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
         if (nclusters > c->N) nclusters = c->N;
         P->grid = nclusters * P->CS;
         e = cudaMalloc((void**)&P->absx_part, (size_t)P->grid * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&P->res_part, (size_t)P->grid * 5 * sizeof(double));
     }
     if (e != cudaSuccess || nclusters < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "multi-iteration X-step setup failed: %s",
                                e != cudaSuccess ? cudaGetErrorString(e) : "no cluster fits");
         if (P->tw2) cudaFree(P->tw2);
+        if (P->absx_part) cudaFree(P->absx_part);
         delete P;
         return nullptr;
     }
@@ -485,6 +520,7 @@ void iter_plan_free(void* p) {
     if (!P) return;
     if (P->tw2) cudaFree(P->tw2);
     if (P->absx_part) cudaFree(P->absx_part);
+    if (P->res_part) cudaFree(P->res_part);
     delete P;
 }
 
@@ -503,6 +539,7 @@ int iter_xsteps_n(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iter
     a.Xin = Xin; a.Xout = Xout; a.y2 = c->y2; a.y3 = c->y3;
     a.Y1 = c->Y1; a.y1 = c->y1; a.DX = c->DX; a.S = c->S;
     a.G1h = c->G1h; a.Ah = c->Ah; a.tw2 = P->tw2; a.absx_part = P->absx_part;
+    a.res_part = P->res_part;
     a.N = Nlim; a.M = c->M; a.L4 = c->L4; a.gamma = c->gamma; a.iters = iters;
     a.lam = c->p.lambda; a.rho = c->p.rho; a.kc = c->p.sherman_const_csc;
     a.ld = P->ld; a.ld3 = P->ld3;
@@ -529,6 +566,14 @@ int iter_absx(void* p, const double** part, int* n) {
     IterPlan* P = (IterPlan*)p;
     if (!P) return 0;
     *part = P->absx_part;
+    *n = P->grid;
+    return 1;
+}
+
+int iter_resid(void* p, const double** part, int* n) {
+    IterPlan* P = (IterPlan*)p;
+    if (!P) return 0;
+    *part = P->res_part;
     *n = P->grid;
     return 1;
 }

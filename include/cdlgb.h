@@ -71,6 +71,12 @@ typedef struct {
     int32_t fft_mode;           /* 0 = auto (fused in-kernel FFT path where the size is
                                    supported, else cuFFT transforms), 1 = cuFFT, 2 = fused */
     uint64_t hbm_budget_bytes;  /* 0 = free device memory minus a 1 GiB margin */
+    float stop_tol;             /* stopping test of cdlgb_run_outer (no counterpart in the
+                                   reference, whose loop count is fixed, wrap.jl:6-11):
+                                   0 = off (default: iter_num iterations, as the
+                                   reference); > 0 = stop after the first outer iteration
+                                   whose largest relative residual (CDLGB_FIELD_RESIDUALS
+                                   entry 18) is <= stop_tol */
 } cdlgb_params;
 
 /* Fields readable with cdlgb_get (sizes in elements; all float32 unless noted). */
@@ -93,8 +99,27 @@ typedef enum {
     CDLGB_FIELD_Y1_DUAL = 15,   /* y1, (Lg, N) */
     CDLGB_FIELD_OBJ_BEST = 16,  /* one float64 */
     CDLGB_FIELD_DATA = 17,      /* the loaded one-hot data, (4L, N) float32 */
-    CDLGB_FIELD_BACKGROUND = 18 /* the shuffled background (cdlgb_make_background), (4L, N) float32 */
+    CDLGB_FIELD_BACKGROUND = 18, /* the shuffled background (cdlgb_make_background), (4L, N) float32 */
+    CDLGB_FIELD_RESIDUALS = 19, /* the residual record, 19 float64 (below) */
+    CDLGB_FIELD_OUTER_DONE = 20 /* one int32: outer iterations run by the last cdlgb_run_outer */
 } cdlgb_field;
+
+/* The residual record (CDLGB_FIELD_RESIDUALS), float64 sums accumulated on the GPU.
+ * The reference computes no residual; these follow its dual updates.  After every code
+ * update, the primal residuals of its final iterate -- the vectors the next dual
+ * updates of code_update! (src/CDL/train.jl:12-14) would add:
+ *   [0] sum (X - shrink(X + y2))^2   [1] sum (X - projectionX(X + y3))^2
+ *   [2] sum (DX - Y1)^2              [3] sum X^2            [4] sum DX^2
+ * after every D-step, the increments its dual updates (train.jl:70-72) added and the
+ * change of the consensus dictionary (the D-step's dual residual over sigma):
+ *   [5] sum (d - G1_old)^2   [6] sum (d - G3_old)^2   [7] sum (Td - G2)^2
+ *   [8] sum d^2              [9] sum Td^2
+ *   [10] N sum (G1 - G1_old)^2   [11] N sum (G3 - G3_old)^2   [12] N (sum G1^2 + sum G3^2)
+ * and the relative residuals of the stopping test:
+ *   [13] sqrt(([0] + [1]) / [3])   [14] sqrt([2] / [4])   [15] sqrt(([5] + [6]) / (2 [8]))
+ *   [16] sqrt([7] / [9])           [17] sqrt(([10] + [11]) / [12])   [18] max of [13..17]
+ * Sums over d use the spectral state through Parseval's relation where the D-step keeps
+ * it.  All zero after cdlgb_init_state. */
 
 /* Fill *p with the CDL_setup defaults. */
 int cdlgb_params_default(cdlgb_params* p);
@@ -150,7 +175,9 @@ int cdlgb_update_best(cdlgb_ctx* ctx, double* obj, int32_t* improved);
 
 /* iter_num passes of cdl_optimize's loop body (src/WRAPPER/wrap.jl:6-11):
  * code_update!(csc_iter_num); update_best!; dict_update!(cdl_iter_num).
- * objs (may be NULL) receives the iter_num objective values. */
+ * objs (may be NULL) receives the objective values, one per pass run.  With
+ * params.stop_tol > 0 the loop ends early after the first pass whose largest relative
+ * residual is <= stop_tol; CDLGB_FIELD_OUTER_DONE then tells how many passes ran. */
 int cdlgb_run_outer(cdlgb_ctx* ctx, int32_t iter_num, double* objs);
 
 /* std(X_best[X_best .> 0]) * multiplier -- src/WRAPPER/wrap.jl:12 (float64 on the GPU). */

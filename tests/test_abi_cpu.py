@@ -83,3 +83,26 @@ def test_counts_to_pfms_c_matches_oracle(pkg, built_lib):
 def test_golden_scan_pfms_from_counts(pkg, built_lib):
     g = np.load(os.path.join(ROOT, "tests", "golden", "scan_small.npz"))
     assert SO.transfac_text(g["pfms"][0, :, : g["lens"][0]]) == str(g["transfac"])
+
+
+def test_params_struct_layout_matches_header(pkg, built_lib, tmp_path):
+    """The ctypes mirror of cdlgb_params has the C struct's size and field offsets."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    from cdlmotif_gb300._lib import CdlgbParams
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in CdlgbParams._fields_]
+    cnames = ["lambda" if n == "lambda_" else n for n in names]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "cdlgb.h"\nint main(void){\n'
+                   'printf("%zu\\n", sizeof(cdlgb_params));\n' +
+                   "".join(f'printf("%zu\\n", offsetof(cdlgb_params, {n}));\n' for n in cnames) +
+                   "return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == C.sizeof(CdlgbParams)
+    assert vals[1:] == [getattr(CdlgbParams, n).offset for n in names]

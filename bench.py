@@ -342,10 +342,10 @@ def roofline(prof, steps, fused):
 
 def serve_requests(n_req: int, seed: int = 77, rate: float = 20.0):
     """The serving workload's request stream: Poisson arrivals (mean `rate`/s),
-    N log-uniform in [200, 50000], L uniform in [50, 1000] padded to the next FFT-friendly
-    length, 1-6 planted Dirichlet(0.1) motifs of width 8-20 at 10-40 % occupancy."""
+    N log-uniform in [200, 50000], L uniform in [50, 1000], 1-6 planted Dirichlet(0.1)
+    motifs of width 8-20 at 10-40 % occupancy; each request is FASTA text (the server
+    pads L to the next FFT-friendly length).  Returns (arrival s, FASTA bytes, N, L)."""
     pkg = _pkg()
-    from cdlmotif_gb300 import serve
     rng = np.random.Generator(np.random.PCG64(seed))
     t = 0.0
     out = []
@@ -357,8 +357,7 @@ def serve_requests(n_req: int, seed: int = 77, rate: float = 20.0):
         widths = [int(w) for w in rng.integers(8, 21, k)]
         occ = [float(o) for o in rng.uniform(0.1, 0.4, k)]
         bases, _, _ = pkg.synth.plant_dataset(seed * 1000 + i, N, L, widths, occ)
-        Lp = serve.friendly_length(L, 16)
-        out.append((t, serve.pad_onehot(pkg.synth.onehot(bases), L, Lp), N, L, Lp))
+        out.append((t, pkg.synth.to_fasta(bases).encode(), N, L))
     return out
 
 
@@ -370,7 +369,8 @@ def run_serve(args):
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
     res = serve.serve_stream(setup, [(t, d) for t, d, *_ in reqs], slots=args.serve_slots,
-                             iter_num=args.serve_iters, seed=1)
+                             iter_num=args.serve_iters, seed=1, keep_results=False,
+                             pad_friendly=True)
     clocks = sampler.stop()
     res.pop("results", None)
     return {"metric": "served datasets/hr (Poisson 20/s, N log-uniform 200-50000, L 50-1000, K=32, W=16)",
@@ -380,9 +380,10 @@ def run_serve(args):
             "requests": res["requests"], "completed": res["completed"],
             "rejected": res["rejected"], "slots": args.serve_slots,
             "outer_iterations_per_dataset": args.serve_iters, "dtype": "f32",
-            "data": "synthetic (seeded planted motifs)", "clocks": clocks,
+            "data": "synthetic (seeded planted motifs), FASTA text through cdlgb_server_submit_fasta",
+            "clocks": clocks,
             "config": {"workload": "serving", "requests": args.serve_requests,
-                       "L_padded": [int(r[4]) for r in reqs], "N": [int(r[2]) for r in reqs]}}
+                       "N": [int(r[2]) for r in reqs], "L": [int(r[3]) for r in reqs]}}
 
 
 def batched_requests(n: int = 64, seed: int = 91):
@@ -554,7 +555,10 @@ def run_precision(args):
     import torch
     pkg = _pkg()
     from oracle.torch_admm import FP64Reference, LiteralADMM, relative_residuals
-    wl = WORKLOAD
+    wl = dict(WORKLOAD)
+    if args.precision_reference_defaults:
+        # the reference's own CDL_setup defaults (src/SETUP/WRAPPER_setup.jl:3-5)
+        wl.update(lam=0.01, rho=100.0, sigma=100.0)
     bases = dataset(wl)
     S = pkg.synth.onehot(bases)
     setup = pkg.CDLSetup(M=wl["M"], filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
@@ -585,6 +589,8 @@ def run_precision(args):
     at = sorted({int(v) for v in args.precision_at.split(",") if v})
     rows = []
     secs = {"f32_cuda": 0.0, "f32_reference_order": 0.0, "f64": 0.0}
+    first_nonfinite = {"f32_cuda": None, "f32_reference_order": None, "f64": None}
+    objectives = {"f32_cuda": [], "f32_reference_order": [], "f64": []}
     for it in range(1, at[-1] + 1):
         t0 = time.perf_counter()
         o32 = float(pkg.run_outer(c, 1)[0])
@@ -599,6 +605,10 @@ def run_precision(args):
         secs["f32_cuda"] += t1 - t0
         secs["f32_reference_order"] += t2 - t1
         secs["f64"] += t3 - t2
+        for k, o in (("f32_cuda", o32), ("f32_reference_order", ol), ("f64", o64)):
+            objectives[k].append(o)
+            if first_nonfinite[k] is None and not np.isfinite(o):
+                first_nonfinite[k] = it
         if it not in at:
             continue
         row = {"outer_iteration": it, "objective_f64": o64,
@@ -617,7 +627,9 @@ def run_precision(args):
         print(json.dumps(row), file=sys.stderr, flush=True)
     c.close()
     return {"metric": "precision: float32 CUDA path and float32 reference order vs all-FP64",
-            "workload": wl["name"], "N": wl["N"], "rows": rows, "seconds": secs,
+            "workload": wl["name"], "N": wl["N"], "lambda": wl["lam"], "rho": wl["rho"],
+            "sigma": wl["sigma"], "rows": rows, "seconds": secs,
+            "first_nonfinite_objective": first_nonfinite, "objectives": objectives,
             "note": "same initial state for all three; float64 objective and residual sums; "
                     "FP64 = torch float64 cuFFT (half-spectrum form); reference order = "
                     "src/CDL/train.jl statement by statement in torch float32, c2c FFTs"}
@@ -640,7 +652,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--serve", action="store_true",
                     help="serving workload: Poisson request stream, datasets/hr and p50/p99")
-    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-iters", type=int, default=3)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--batched", action="store_true",
@@ -648,6 +660,8 @@ def main():
     ap.add_argument("--batched-n", type=int, default=64)
     ap.add_argument("--precision", action="store_true",
                     help="precision study: float32 GPU path vs an all-FP64 GPU reference")
+    ap.add_argument("--precision-reference-defaults", action="store_true",
+                    help="precision study with the reference's CDL_setup defaults (lambda 0.01, rho 100)")
     ap.add_argument("--precision-at", default="1,3,10,100",
                     help="outer iterations at which the precision study reports")
     ap.add_argument("--search", action="store_true",

@@ -83,6 +83,33 @@ SIGNATURES = {
                                           C.c_int32, C.c_float, _f64p, _vp]),
 }
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("device", C.c_int32), ("iter_num", C.c_int32),
+                ("keep_codes", C.c_int32), ("pad_friendly", C.c_int32),
+                ("hbm_budget_bytes", C.c_uint64), ("seed", C.c_uint64)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("N", C.c_int32), ("L4", C.c_int32),
+                ("M", C.c_int32), ("Lg", C.c_int32), ("outer_done", C.c_int32),
+                ("footprint_bytes", C.c_uint64), ("obj_best", C.c_double),
+                ("code_thresh", C.c_double), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("t_now", C.c_double), ("error", C.c_char * 256)]
+
+
+SIGNATURES.update({
+    "cdlgb_server_create": (C.c_int, [C.POINTER(CdlgbParams), C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "cdlgb_server_submit": (C.c_int, [_vp, _f32p, C.c_int32, C.c_int32, _i64p]),
+    "cdlgb_server_submit_fasta": (C.c_int, [_vp, C.c_char_p, C.c_size_t, C.c_int32, _i64p]),
+    "cdlgb_server_poll": (C.c_int, [_vp, C.c_int64, C.c_int32, C.POINTER(RequestInfo)]),
+    "cdlgb_server_fetch": (C.c_int, [_vp, C.c_int64, _f32p, C.c_size_t, _f64p, C.c_int32, _f32p,
+                                     C.c_size_t]),
+    "cdlgb_server_release": (C.c_int, [_vp, C.c_int64]),
+    "cdlgb_server_stats": (C.c_int, [_vp, _i32p, _i32p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "cdlgb_server_last_error": (C.c_char_p, [_vp]),
+    "cdlgb_server_destroy": (C.c_int, [_vp]),
+})
+
 _lib = None
 
 

@@ -100,6 +100,77 @@ static int check_onehot(cdlgb_ctx* c) {
     return CDLGB_OK;
 }
 
+// read_fasta + data_2_dummy's rules (src/LOAD/read.jl:2-28, src/LOAD/to_dummy.jl:27-38)
+// on the host: '>'-records, header line dropped, lines joined, records with 'N'/'n'
+// dropped, the first max_entries kept, upper-cased; one byte per base (A C G T = 0..3;
+// 4 for every base of a record whose length differs from the first one's).
+int fasta_codes(const char* text, size_t nbytes, int32_t max_entries, std::vector<uint8_t>& codes,
+                int32_t* N_out, int32_t* L_out, int32_t* wrong_out, char* err, size_t errlen) {
+    if (!text || max_entries <= 0) {
+        snprintf(err, errlen, "load_fasta: null text or max_entries <= 0");
+        return CDLGB_EINVAL;
+    }
+    std::vector<std::string> reads;
+    size_t i = 0;
+    while (i < nbytes && (int)reads.size() < max_entries) {
+        size_t j = i;
+        while (j < nbytes && text[j] != '>') ++j;            // chunk [i, j)
+        if (j > i) {
+            size_t k = i;
+            while (k < j && text[k] != '\n') ++k;           // header line
+            std::string r;
+            bool has_n = false;
+            for (size_t t = k; t < j; ++t) {
+                const char ch = text[t];
+                if (ch == '\n') continue;
+                if (ch == 'N' || ch == 'n') has_n = true;
+                r.push_back(ch);
+            }
+            if (!has_n) reads.push_back(std::move(r));
+        }
+        i = j + 1;
+    }
+    if (reads.empty()) { snprintf(err, errlen, "load_fasta: no sequences"); return CDLGB_EINVAL; }
+    const size_t L = reads[0].size();
+    if (L == 0) { snprintf(err, errlen, "load_fasta: the first sequence is empty"); return CDLGB_EINVAL; }
+    if (L > (size_t)(1 << 28) / 4) { snprintf(err, errlen, "load_fasta: sequences too long"); return CDLGB_EINVAL; }
+    const int32_t N = (int32_t)reads.size();
+    codes.assign((size_t)N * L, 0);
+    int32_t wrong = 0;
+    for (int32_t n = 0; n < N; ++n) {
+        const std::string& r = reads[n];
+        uint8_t* o = codes.data() + (size_t)n * L;
+        if (r.size() != L) {           // left uninitialised by the reference; zeros here
+            ++wrong;
+            memset(o, 4, L);
+            continue;
+        }
+        for (size_t l = 0; l < L; ++l) {
+            const char u = (char)toupper((unsigned char)r[l]);
+            const uint8_t b = u == 'A' ? 0 : u == 'C' ? 1 : u == 'G' ? 2 : u == 'T' ? 3 : 255;
+            if (b == 255) {   // dummy[uppercase(c)] raises a KeyError in the reference
+                snprintf(err, errlen, "load_fasta: record %d has character 0x%02x at %zu", n,
+                         (unsigned)(unsigned char)r[l], l);
+                return CDLGB_EINVAL;
+            }
+            o[l] = b;
+        }
+    }
+    *N_out = N;
+    *L_out = (int32_t)L;
+    *wrong_out = wrong;
+    return CDLGB_OK;
+}
+
+extern "C" {
+static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, int32_t L4, int32_t N);
+}
+
+// the context loaded from one byte per base (fasta_codes' output)
+int load_codes(cdlgb_ctx* c, const uint8_t* codes, int32_t L, int32_t N) {
+    return load_impl(c, nullptr, codes, 4 * L, N);
+}
+
 extern "C" {
 
 int cdlgb_params_default(cdlgb_params* p) {
@@ -239,7 +310,6 @@ static int upload_data(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, 
     return CDLGB_OK;
 }
 
-static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, int32_t L4, int32_t N);
 
 int cdlgb_load_data(cdlgb_ctx* c, const float* onehot, int32_t L4, int32_t N) {
     if (!c) return CDLGB_EINVAL;
@@ -316,56 +386,15 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
 int cdlgb_load_fasta(cdlgb_ctx* c, const char* text, size_t nbytes, int32_t max_entries,
                      int32_t* N_out, int32_t* L_out, int32_t* n_wrong_len) {
     if (!c) return CDLGB_EINVAL;
-    if (!text || max_entries <= 0)
-        return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: null text or max_entries <= 0");
-    std::vector<std::string> reads;
-    size_t i = 0;
-    while (i < nbytes && (int)reads.size() < max_entries) {
-        size_t j = i;
-        while (j < nbytes && text[j] != '>') ++j;            // chunk [i, j)
-        if (j > i) {
-            size_t k = i;
-            while (k < j && text[k] != '\n') ++k;           // header line
-            std::string r;
-            bool has_n = false;
-            for (size_t t = k; t < j; ++t) {
-                const char ch = text[t];
-                if (ch == '\n') continue;
-                if (ch == 'N' || ch == 'n') has_n = true;
-                r.push_back(ch);
-            }
-            if (!has_n) reads.push_back(std::move(r));
-        }
-        i = j + 1;
-    }
-    if (reads.empty()) return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: no sequences");
-    const size_t L = reads[0].size();
-    if (L == 0) return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: the first sequence is empty");
-    if (L > (size_t)(1 << 28) / 4) return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: sequences too long");
-    const int32_t N = (int32_t)reads.size();
-    std::vector<uint8_t> codes((size_t)N * L);
-    int32_t wrong = 0;
-    for (int32_t n = 0; n < N; ++n) {
-        const std::string& r = reads[n];
-        uint8_t* o = codes.data() + (size_t)n * L;
-        if (r.size() != L) {           // left uninitialised by the reference; zeros here
-            ++wrong;
-            memset(o, 4, L);
-            continue;
-        }
-        for (size_t l = 0; l < L; ++l) {
-            const char u = (char)toupper((unsigned char)r[l]);
-            const uint8_t b = u == 'A' ? 0 : u == 'C' ? 1 : u == 'G' ? 2 : u == 'T' ? 3 : 255;
-            if (b == 255)     // dummy[uppercase(c)] raises a KeyError in the reference
-                return cdlgb_seterr(c, CDLGB_EINVAL, "load_fasta: record %d has character 0x%02x at %zu",
-                                    n, (unsigned)(unsigned char)r[l], l);
-            o[l] = b;
-        }
-    }
-    int st = load_impl(c, nullptr, codes.data(), (int32_t)(4 * L), N);
+    std::vector<uint8_t> codes;
+    int32_t N = 0, L = 0, wrong = 0;
+    char err[256];
+    int st = fasta_codes(text, nbytes, max_entries, codes, &N, &L, &wrong, err, sizeof(err));
+    if (st != CDLGB_OK) return cdlgb_seterr(c, st, "%s", err);
+    st = load_impl(c, nullptr, codes.data(), 4 * L, N);
     if (st != CDLGB_OK) return st;
     if (N_out) *N_out = N;
-    if (L_out) *L_out = (int32_t)L;
+    if (L_out) *L_out = L;
     if (n_wrong_len) *n_wrong_len = wrong;
     return CDLGB_OK;
 }

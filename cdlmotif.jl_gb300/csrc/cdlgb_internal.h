@@ -213,6 +213,12 @@ int warp_plan_filters(void* p);
 int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* cs, int32_t* mc,
                    int32_t* n_out, int32_t* chosen);
 int fused_has_multi(cdlgb_ctx* c);
+// api.cu: FASTA text -> one byte per base (the reference's parsing rules), and a load
+// from those bytes
+#include <vector>
+int fasta_codes(const char* text, size_t nbytes, int32_t max_entries, std::vector<uint8_t>& codes,
+                int32_t* N, int32_t* L, int32_t* wrong, char* err, size_t errlen);
+int load_codes(cdlgb_ctx* c, const uint8_t* codes, int32_t L, int32_t N);
 // resid.cu: residual norms and the stopping test
 size_t resid_part_doubles(int N, int F, int slots);
 int resid_finish(cdlgb_ctx* c);

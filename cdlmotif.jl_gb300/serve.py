@@ -1,14 +1,13 @@
-"""Continuous-batching request loop for many CDL trainings on one GPU.
+"""Continuous-batching training server: a thin wrapper of the C ABI's cdlgb_server_*.
 
 The reference processes FASTA files one after another (find_motifs_fasta_folder,
-src/CDLmotif.jl:84-93), each through cdl_optimize (src/WRAPPER/wrap.jl:1-32).  Here
-requests (one dataset each) arrive at any time and are admitted while others are on
-the GPU: a request takes a slot when one is free and its device footprint
+src/CDLmotif.jl:84-93), each through cdl_optimize (src/WRAPPER/wrap.jl:1-32).  The
+library's server (csrc/server.cpp) admits requests (one dataset each) while others are
+on the GPU: a request takes a slot when one is free and its device footprint
 (cdlgb_footprint: ADMM state + scratch for its N and L) fits the HBM budget left by
-the requests in flight; otherwise it waits in arrival order.  Every admitted request
-runs on its own context (own CUDA stream, state resident until it finishes), so the
-kernels of different datasets overlap on the device; the ctypes calls release the
-GIL, so one host thread per slot is enough to keep them fed.
+the requests in flight, in arrival order.  Every admitted request runs on its own
+context (own CUDA stream, state resident until it finishes) on one of the server's
+worker threads, so the kernels of different datasets overlap on the device.
 
 Because every kernel is deterministic and a context shares no device memory with
 another, a dataset's result does not depend on what else is in flight.
@@ -16,16 +15,16 @@ another, a dataset's result does not depend on what else is in flight.
 from __future__ import annotations
 
 import ctypes as C
-import queue
-import threading
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import _lib
-from . import (CDLSetup, CDLGBError, init_cdl, code_update, dict_update, update_best,
-               code_threshold)
+from ._lib import RequestInfo, ServerConfig, ptr
+from . import CDLSetup, CDLGBError, init_cdl, code_update, dict_update, update_best, code_threshold
+
+STATES = {0: "pending", 1: "running", 2: "done", 3: "failed"}
 
 
 def footprint_bytes(setup: CDLSetup, L: int, N: int, fft_mode: int = 0) -> int:
@@ -71,111 +70,100 @@ def pad_onehot(S: np.ndarray, L: int, Lp: int) -> np.ndarray:
     return out
 
 
-@dataclass
-class Request:
-    rid: int
-    data: np.ndarray                   # (N, 4L) one-hot
-    arrival: float = 0.0               # seconds on the server clock
-    admitted: float = 0.0
-    done: float = 0.0
-    footprint: int = 0
-    result: dict = field(default_factory=dict)
-    error: str | None = None
-
-
 class Server:
-    """Admits requests by HBM footprint into at most `slots` concurrent trainings."""
+    """The library's training server (cdlgb_server_create): `slots` trainings in flight
+    at most, admitted by footprint within `hbm_budget` bytes (0 = 85 % of free device
+    memory), each `iter_num` outer iterations from `seed`."""
 
     def __init__(self, setup: CDLSetup, slots: int = 8, hbm_budget: int = 0, device: int = 0,
-                 iter_num: int | None = None, seed: int = 0):
+                 iter_num: int | None = None, seed: int = 0, keep_codes: bool = False,
+                 pad_friendly: bool = False):
+        L = _lib.lib()
         self.setup = setup
-        self.slots = slots
-        self.device = device
-        self.iter_num = setup.iter_num if iter_num is None else iter_num
-        self.seed = seed
-        if hbm_budget <= 0:
-            import torch  # noqa: F401  (only for the free-memory query)
-            free, _total = torch.cuda.mem_get_info(device)
-            hbm_budget = int(free * 0.85)
-        self.budget = hbm_budget
-        self.in_use = 0
-        self.cv = threading.Condition()
-        self.pending: list[Request] = []
-        self.running = 0
-        self.work: queue.Queue = queue.Queue()
-        self.finished: list[Request] = []
-        self.t0 = time.perf_counter()
-        self.stop = False
-        self.threads = [threading.Thread(target=self._worker, daemon=True) for _ in range(slots)]
-        for t in self.threads:
-            t.start()
-        self.admitter = threading.Thread(target=self._admit_loop, daemon=True)
-        self.admitter.start()
+        self._p = setup.params(device=device)
+        cfg = ServerConfig(slots=int(slots), device=int(device),
+                           iter_num=int(setup.iter_num if iter_num is None else iter_num),
+                           keep_codes=int(bool(keep_codes)), pad_friendly=int(bool(pad_friendly)),
+                           hbm_budget_bytes=int(hbm_budget),
+                           seed=int(seed) & (2**64 - 1))
+        h = C.c_void_p()
+        st = L.cdlgb_server_create(C.byref(self._p), C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise CDLGBError(st, "cdlgb_server_create failed")
+        self._h = h
+        self.iter_num = cfg.iter_num
 
-    def now(self) -> float:
-        return time.perf_counter() - self.t0
+    def _check(self, st):
+        if st != 0:
+            msg = _lib.lib().cdlgb_server_last_error(self._h)
+            raise CDLGBError(st, msg.decode() if msg else "")
 
-    def submit(self, req: Request):
-        req.arrival = self.now()
-        req.footprint = footprint_bytes(self.setup, req.data.shape[1] // 4, req.data.shape[0])
-        with self.cv:
-            if req.footprint > self.budget:
-                req.error = f"needs {req.footprint / 1e9:.1f} GB > budget {self.budget / 1e9:.1f} GB"
-                req.done = self.now()
-                self.finished.append(req)
-            else:
-                self.pending.append(req)
-            self.cv.notify_all()
+    def submit(self, data: np.ndarray) -> int:
+        """Queue one dataset, (N, 4L) one-hot; returns its request id.  Raises
+        CDLGBError(ENOMEM_BUDGET) when it can never fit."""
+        S = np.ascontiguousarray(data, np.float32)
+        rid = C.c_int64()
+        self._check(_lib.lib().cdlgb_server_submit(self._h, ptr(S, C.c_float), S.shape[1],
+                                                   S.shape[0], C.byref(rid)))
+        return rid.value
 
-    def _admit_loop(self):
-        while True:
-            with self.cv:
-                while not self.stop and not (self.pending and self.running < self.slots and
-                                             self.in_use + self.pending[0].footprint <= self.budget):
-                    self.cv.wait(0.05)
-                if self.stop and not self.pending:
-                    return
-                if not self.pending:
-                    continue
-                req = self.pending.pop(0)
-                self.in_use += req.footprint
-                self.running += 1
-                req.admitted = self.now()
-            self.work.put(req)
+    def submit_fasta(self, fasta, max_entries: int = 10000) -> int:
+        """Queue one dataset given as FASTA text (str or bytes), parsed by the rules of
+        read_fasta / data_2_dummy (src/LOAD/read.jl:2-28, src/LOAD/to_dummy.jl:27-38)."""
+        text = fasta.encode() if isinstance(fasta, str) else bytes(fasta)
+        rid = C.c_int64()
+        self._check(_lib.lib().cdlgb_server_submit_fasta(self._h, text, len(text), int(max_entries),
+                                                         C.byref(rid)))
+        return rid.value
 
-    def _worker(self):
-        while True:
-            req = self.work.get()
-            if req is None:
-                return
-            try:
-                req.result = run_training(self.setup, req.data, self.iter_num, self.seed,
-                                          self.device)
-            except CDLGBError as e:
-                req.error = str(e)
-            req.done = self.now()
-            with self.cv:
-                self.in_use -= req.footprint
-                self.running -= 1
-                self.finished.append(req)
-                self.cv.notify_all()
+    def poll(self, rid: int, wait_ms: int = 0) -> dict:
+        info = RequestInfo()
+        self._check(_lib.lib().cdlgb_server_poll(self._h, int(rid), int(wait_ms), C.byref(info)))
+        out = {k: getattr(info, k) for k, _ in RequestInfo._fields_ if k != "error"}
+        out["state"] = STATES[info.state]
+        out["error"] = info.error.decode() or None
+        return out
 
-    def drain(self, n_expected: int, timeout: float = 3600.0) -> list[Request]:
-        t_end = time.perf_counter() + timeout
-        with self.cv:
-            while len(self.finished) < n_expected and time.perf_counter() < t_end:
-                self.cv.wait(0.1)
-        return list(self.finished)
+    def fetch(self, rid: int, codes: bool = False) -> dict:
+        info = self.poll(rid)
+        M, Lg, N = info["M"], info["Lg"], info["N"]
+        D = np.empty((M, Lg), np.float32)
+        objs = np.zeros(max(info["outer_done"], 1), np.float64)
+        X = np.empty((N, M, Lg), np.float32) if codes else None
+        self._check(_lib.lib().cdlgb_server_fetch(
+            self._h, int(rid), ptr(D, C.c_float), D.nbytes, ptr(objs, C.c_double), objs.size,
+            ptr(X, C.c_float) if codes else None, X.nbytes if codes else 0))
+        res = {"D_best": D, "objs": objs[:info["outer_done"]], "code_thresh": info["code_thresh"],
+               "obj_best": info["obj_best"], "N": N, "L4": info["L4"]}
+        if codes:
+            res["X_best"] = X
+        return res
+
+    def release(self, rid: int):
+        self._check(_lib.lib().cdlgb_server_release(self._h, int(rid)))
+
+    def stats(self) -> dict:
+        p, r = C.c_int32(), C.c_int32()
+        u, b = C.c_uint64(), C.c_uint64()
+        self._check(_lib.lib().cdlgb_server_stats(self._h, C.byref(p), C.byref(r), C.byref(u), C.byref(b)))
+        return {"pending": p.value, "running": r.value, "in_use": u.value, "budget": b.value}
 
     def close(self):
-        with self.cv:
-            self.stop = True
-            self.cv.notify_all()
-        self.admitter.join()
-        for _ in self.threads:
-            self.work.put(None)
-        for t in self.threads:
-            t.join()
+        if getattr(self, "_h", None):
+            _lib.lib().cdlgb_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_training(setup: CDLSetup, data: np.ndarray, iter_num: int, seed: int, device: int) -> dict:
@@ -200,25 +188,37 @@ def percentile(v, q):
 
 
 def serve_stream(setup: CDLSetup, requests: list[tuple[float, np.ndarray]], slots: int = 8,
-                 iter_num: int = 3, seed: int = 0, device: int = 0, hbm_budget: int = 0) -> dict:
-    """Replays (arrival offset s, one-hot data) requests against a Server, sleeping until
-    each arrival; returns latency percentiles and throughput."""
-    srv = Server(setup, slots=slots, iter_num=iter_num, seed=seed, device=device,
-                 hbm_budget=hbm_budget)
-    t0 = srv.now()
-    for i, (t_arr, data) in enumerate(requests):
-        delay = t_arr - (srv.now() - t0)
-        if delay > 0:
-            time.sleep(delay)
-        srv.submit(Request(rid=i, data=data))
-    done = srv.drain(len(requests))
-    srv.close()
-    ok = [r for r in done if r.error is None]
-    lat = [r.done - r.arrival for r in ok]
-    span = max(r.done for r in done) - t0 if done else float("nan")
-    return {"requests": len(requests), "completed": len(ok),
-            "rejected": [r.error for r in done if r.error],
+                 iter_num: int = 3, seed: int = 0, device: int = 0, hbm_budget: int = 0,
+                 keep_results: bool = True, pad_friendly: bool = False) -> dict:
+    """Replays (arrival offset s, one-hot data (N, 4L) or FASTA text) requests against the
+    library's server,
+    sleeping until each arrival; returns latency percentiles and throughput (latency =
+    finish - arrival on the server's clock)."""
+    with Server(setup, slots=slots, iter_num=iter_num, seed=seed, device=device,
+                hbm_budget=hbm_budget, pad_friendly=pad_friendly) as srv:
+        t0 = time.perf_counter()
+        ids, rejected = {}, []
+        for i, (t_arr, data) in enumerate(requests):
+            delay = t_arr - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            try:
+                ids[i] = srv.submit_fasta(data) if isinstance(data, (bytes, str)) else srv.submit(data)
+            except CDLGBError as e:
+                rejected.append(str(e))
+        infos, results = {}, {}
+        for i, rid in ids.items():
+            infos[i] = srv.poll(rid, wait_ms=-1)
+            if infos[i]["state"] == "done" and keep_results:
+                results[i] = srv.fetch(rid)
+            srv.release(rid)
+    ok = [v for v in infos.values() if v["state"] == "done"]
+    failed = [v["error"] for v in infos.values() if v["state"] != "done"]
+    lat = [v["t_done"] - v["t_submit"] for v in ok]
+    t_first = min((v["t_submit"] for v in infos.values()), default=0.0)
+    span = max((v["t_done"] for v in ok), default=float("nan")) - t_first
+    return {"requests": len(requests), "completed": len(ok), "rejected": rejected + failed,
             "p50_s": percentile(lat, 50), "p99_s": percentile(lat, 99),
-            "mean_queue_s": float(np.mean([r.admitted - r.arrival for r in ok])) if ok else None,
+            "mean_queue_s": float(np.mean([v["t_admit"] - v["t_submit"] for v in ok])) if ok else None,
             "makespan_s": span, "datasets_per_hr": 3600.0 * len(ok) / span if span > 0 else None,
-            "results": {r.rid: r.result for r in ok}}
+            "results": results}

@@ -387,6 +387,70 @@ int cdlgb_objective_noalloc(const float* X, const float* DX, const float* S, int
                             int32_t N, int32_t M, int32_t gamma, float lambda, double* obj,
                             void* stream);
 
+/* ---- Training server: continuous batching of many datasets on one GPU. ----
+ * Replaces the reference's sequential loop over datasets, find_motifs_fasta_folder
+ * (src/CDLmotif.jl:84-93), each trained by cdl_optimize (src/WRAPPER/wrap.jl:1-32).
+ * Requests are submitted from any host thread at any time and admitted in arrival order
+ * as soon as a slot is free and their device footprint (cdlgb_footprint) fits in what
+ * the requests in flight leave of the HBM budget; each runs one training (init from
+ * `seed`, iter_num outer iterations with the params' stopping test, the code threshold)
+ * on its own context and stream, so kernels of different datasets overlap on the
+ * device, and its ADMM state stays resident until the training ends.  Results do not
+ * depend on what else is in flight.  All server calls are thread-safe. */
+typedef struct cdlgb_server cdlgb_server;
+
+typedef struct {
+    int32_t slots;              /* trainings in flight at most (1..64) */
+    int32_t device;             /* CUDA device ordinal */
+    int32_t iter_num;           /* outer iterations per request; 0 = params.iter_num */
+    int32_t keep_codes;         /* 1 = keep X_best of every finished request for fetch */
+    int32_t pad_friendly;       /* 1 = pad each dataset's sequences with empty (all-zero)
+                                   columns to the next length the register-FFT kernels
+                                   cover (within 8 % more transform columns; else the next
+                                   length whose transform factors into primes <= 31) */
+    uint64_t hbm_budget_bytes;  /* 0 = 85 % of the device's free memory at creation */
+    uint64_t seed;              /* initialisation seed of every request */
+} cdlgb_server_config;
+
+enum { CDLGB_REQ_PENDING = 0, CDLGB_REQ_RUNNING = 1, CDLGB_REQ_DONE = 2, CDLGB_REQ_FAILED = 3 };
+
+typedef struct {
+    int32_t state;              /* CDLGB_REQ_* */
+    int32_t status;             /* the training's cdlgb_status when FAILED */
+    int32_t N, L4, M, Lg;       /* dataset and transform sizes (M, Lg once done) */
+    int32_t outer_done;         /* outer iterations run */
+    uint64_t footprint_bytes;   /* device memory admitted for it */
+    double obj_best;            /* best objective (float64) */
+    double code_thresh;         /* std(X_best[X_best .> 0]) * multiplier (wrap.jl:12) */
+    double t_submit, t_admit, t_done, t_now;   /* seconds on the server's clock; -1 = not yet */
+    char error[256];            /* message when FAILED */
+} cdlgb_request_info;
+
+int cdlgb_server_create(const cdlgb_params* p, const cdlgb_server_config* cfg, cdlgb_server** out);
+/* Copy a (4L, N) col-major one-hot dataset into the queue; *request_id identifies it.
+ * CDLGB_ENOMEM_BUDGET when its footprint exceeds the whole budget (it can never run). */
+int cdlgb_server_submit(cdlgb_server* s, const float* onehot, int32_t L4, int32_t N,
+                        int64_t* request_id);
+/* The same from FASTA text, parsed by cdlgb_load_fasta's rules (one byte per base is
+ * kept until the request runs): the drop-in for one file of find_motifs_fasta_folder. */
+int cdlgb_server_submit_fasta(cdlgb_server* s, const char* text, size_t nbytes,
+                              int32_t max_entries, int64_t* request_id);
+/* State of a request; wait_ms > 0 waits up to that long for it to finish, < 0 waits
+ * until it does, 0 returns at once. */
+int cdlgb_server_poll(cdlgb_server* s, int64_t request_id, int32_t wait_ms, cdlgb_request_info* info);
+/* Copy a finished request's results: D_best (Lg, M) float32 (D_bytes = 4 Lg M), up to
+ * objs_cap objectives, X_best (Lg, M, N) float32 when keep_codes; NULL skips one. */
+int cdlgb_server_fetch(cdlgb_server* s, int64_t request_id, float* D_best, size_t D_bytes,
+                       double* objs, int32_t objs_cap, float* X_best, size_t X_bytes);
+/* Forget a finished request (its results are freed). */
+int cdlgb_server_release(cdlgb_server* s, int64_t request_id);
+/* Queue depth, trainings in flight, admitted bytes and the budget. */
+int cdlgb_server_stats(cdlgb_server* s, int32_t* pending, int32_t* running, uint64_t* in_use,
+                       uint64_t* budget);
+const char* cdlgb_server_last_error(const cdlgb_server* s);
+/* Wait for the trainings in flight, drop the requests not yet admitted, free everything. */
+int cdlgb_server_destroy(cdlgb_server* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,4 +1,6 @@
-"""Serving: datasets admitted while others run give the same result as alone."""
+"""Serving through the library's training server (cdlgb_server_*): datasets admitted
+while others run give the same result as alone; admission by footprint; the request
+calls from several host threads."""
 import numpy as np
 import pytest
 
@@ -50,3 +52,56 @@ def test_friendly_length(pkg, L):
         while n % p == 0:
             n //= p
     assert n == 1
+
+
+@pytest.mark.gpu
+def test_server_calls_from_threads(pkg, built_lib):
+    """submit from four host threads at once, poll until done, fetch D_best, objectives
+    and the codes (X_best), release; the results equal the single-context training."""
+    import threading
+    from cdlmotif_gb300 import serve
+    setup = pkg.CDLSetup(M=6, filter_size=3, lambda_=0.1, rho=1.0, sigma=100.0)
+    data = _datasets(pkg)
+    ids = [None] * len(data)
+    with serve.Server(setup, slots=3, iter_num=2, seed=5, hbm_budget=8 << 30, keep_codes=True) as srv:
+        def sub(i):
+            ids[i] = srv.submit(data[i])
+        th = [threading.Thread(target=sub, args=(i,)) for i in range(len(data))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        assert len(set(ids)) == len(data)
+        for i, rid in enumerate(ids):
+            info = srv.poll(rid, wait_ms=-1)
+            assert info["state"] == "done", info
+            assert info["N"] == data[i].shape[0] and info["outer_done"] == 2
+            assert 0 <= info["t_submit"] <= info["t_admit"] <= info["t_done"]
+            res = srv.fetch(rid, codes=True)
+            c = pkg.init_cdl(setup, data[i], seed=5)
+            with c:
+                objs = pkg.run_outer(c, 2)
+                np.testing.assert_array_equal(res["objs"], objs)
+                np.testing.assert_array_equal(res["D_best"], c.D_best)
+                np.testing.assert_array_equal(res["X_best"], c.X_best)
+                assert res["code_thresh"] == pkg.code_threshold(c)
+            srv.release(rid)
+        st = srv.stats()
+        assert st["pending"] == 0 and st["running"] == 0 and st["in_use"] == 0
+        with pytest.raises(pkg.CDLGBError):
+            srv.poll(ids[0])            # released
+
+
+@pytest.mark.gpu
+def test_server_refuses_what_never_fits(pkg, built_lib):
+    from cdlmotif_gb300 import serve
+    setup = pkg.CDLSetup(M=4, filter_size=2)
+    d = _datasets(pkg)[0]
+    fp = serve.footprint_bytes(setup, d.shape[1] // 4, d.shape[0])
+    with serve.Server(setup, slots=1, iter_num=1, hbm_budget=fp - 1) as srv:
+        with pytest.raises(pkg.CDLGBError) as e:
+            srv.submit(d)
+        assert e.value.status == -2
+    with serve.Server(setup, slots=1, iter_num=1, hbm_budget=fp) as srv:
+        rid = srv.submit(d)
+        assert srv.poll(rid, wait_ms=-1)["state"] == "done"

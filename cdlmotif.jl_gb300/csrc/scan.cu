@@ -210,6 +210,200 @@ __global__ void k_scan_both_staged(const float* __restrict__ data, const float* 
     }
 }
 
+// ---------------------------------------------------------------- sparse scans
+// On 0/1 data every term whose one-hot entry is 0 is pwm * 0 = +-0 for a finite pwm,
+// and adding +-0 to a partial sum that starts at +0 leaves it unchanged (s + -0 = s for
+// s != 0, +0 + -0 = +0, and the sum is never -0); a term whose entry is 1 is pwm * 1 =
+// pwm.  So the sum of the nonzero terms alone, added in the reference's order, has the
+// same bits: about w terms per window instead of 4 w products and sums.  Taken only
+// when the data is exact 0/1 and every PWM entry finite (an infinite entry times 0 is
+// NaN, which the dense kernels keep).
+
+// the base bits of position p of the staged sequence: bit j set when entry j is 1
+__device__ __forceinline__ uint32_t base_bits(const float* col, int p) {
+    const float4 v = reinterpret_cast<const float4*>(col)[p];
+    return (v.x != 0.f ? 1u : 0u) | (v.y != 0.f ? 2u : 0u) | (v.z != 0.f ? 4u : 0u) | (v.w != 0.f ? 8u : 0u);
+}
+
+// greedy_search! (scan.jl:223-239: position-major, nucleotide inner) on 0/1 data, one
+// position per thread: for ind = 0 .. w-1 the entries of base(l + ind) in nucleotide
+// order.  Same candidates and (value, index) order as k_scan_fwd.
+__global__ void k_scan_fwd_sparse(const float* __restrict__ data, const float* __restrict__ pwms,
+                                  const int32_t* __restrict__ lens, const float* __restrict__ thresh,
+                                  int K, int maxlen, int L, int32_t* __restrict__ pos) {
+    extern __shared__ float4 sm4f[];
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float* pw = reinterpret_cast<float*>(sm4f);                    // [K][maxlen][4]
+    VI* wb = reinterpret_cast<VI*>(pw + (size_t)K * 4 * maxlen);     // [K][nw]
+    uint8_t* bb = reinterpret_cast<uint8_t*>(wb + (size_t)K * nw);  // [L] base bits
+    const int n = blockIdx.x;
+    const float* col = data + (size_t)n * 4 * L;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) bb[i] = (uint8_t)base_bits(col, i);
+    for (int i = threadIdx.x; i < K * 4 * maxlen; i += blockDim.x) {
+        const int k = i / (4 * maxlen), r = i - k * 4 * maxlen, ind = r >> 2, a = r & 3;
+        pw[i] = pwms[k + K * (a + 4 * ind)];
+    }
+    __syncthreads();
+    const int l = threadIdx.x;
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        VI best{-INFINITY, 0x7fffffff};
+        if (l < L) {
+            float v = 0.f;
+            if (l <= L - w) {
+                const float* p = pw + (size_t)k * 4 * maxlen;
+                float s = 0.f;
+                for (int ind = 0; ind < w; ++ind) {
+                    uint32_t b = bb[l + ind];
+                    while (b) {
+                        const int a = __ffs(b) - 1;
+                        b &= b - 1;
+                        s = __fadd_rn(s, p[4 * ind + a]);
+                    }
+                }
+                v = s > thresh[k] ? s : 0.f;
+            }
+            best = VI{v, l};
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            VI y;
+            y.v = __shfl_xor_sync(0xffffffffu, best.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, best.i, o);
+            best = vi_best(best, y);
+        }
+        if (lane == 0) wb[(size_t)k * nw + wid] = best;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        VI r{-INFINITY, 0x7fffffff};
+        for (int v = 0; v < nw; ++v) r = vi_best(r, wb[(size_t)k * nw + v]);
+        pos[k + (size_t)K * n] = (r.i == 0) ? 0 : r.i + 1;
+    }
+}
+
+// scan_n on both strands (scan.jl:10-21: nucleotide-major) on 0/1 data, one position
+// per thread, w <= 64: the window's positions of base j are the set bits of a 64-bit
+// mask cut from the sequence's bit plane of j, so the nonzero terms are visited j by j,
+// ind ascending -- the dense order -- in one loop of exactly that many steps.  The
+// (forward, complement) coefficient pairs, the per-warp argmax and the final reduction
+// are k_scan_both_staged's.
+__global__ void k_scan_both_sparse(const float* __restrict__ data, const float* __restrict__ pwms,
+                                   const int32_t* __restrict__ lens, const float* __restrict__ thresh,
+                                   int K, int maxlen, int L, int32_t* __restrict__ pos,
+                                   float* __restrict__ score, uint8_t* __restrict__ comp) {
+    extern __shared__ float4 sm4p[];
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nwords = (L + 31) / 32 + 2;                           // two zero words of padding
+    float2* pw = reinterpret_cast<float2*>(sm4p);                   // [K][4][maxlen]
+    VI* wb = reinterpret_cast<VI*>(pw + (size_t)K * 4 * maxlen);     // [K][nw][2]
+    uint32_t* planes = reinterpret_cast<uint32_t*>(wb + (size_t)K * nw * 2);   // [4][nwords]
+    const int n = blockIdx.x;
+    const float* col = data + (size_t)n * 4 * L;
+    for (int i = threadIdx.x; i < 4 * nwords; i += blockDim.x) {
+        const int j = i / nwords, wd = i - j * nwords;
+        uint32_t m = 0;
+        for (int b = 0; b < 32; ++b) {
+            const int p = 32 * wd + b;
+            if (p < L && col[4 * p + j] != 0.f) m |= 1u << b;
+        }
+        planes[i] = m;
+    }
+    const int per = 4 * maxlen;
+    for (int i = threadIdx.x; i < K * per; i += blockDim.x) {
+        const int k = i / per, r = i - k * per, j = r / maxlen, kk = r - j * maxlen;
+        const int w = lens[k];
+        float f = 0.f, cc = 0.f;
+        if (kk < w) {
+            f = pwms[k + K * (j + 4 * kk)];
+            cc = pwms[k + K * ((3 - j) + 4 * (w - 1 - kk))];
+        }
+        pw[i] = make_float2(f, cc);
+    }
+    __syncthreads();
+    const int l = threadIdx.x;
+    const int wi = l >> 5, sh = l & 31;
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        VI bf{-INFINITY, 0x7fffffff}, bc{-INFINITY, 0x7fffffff};
+        if (l <= L - w) {
+            const uint64_t keep = w >= 64 ? ~0ull : ((1ull << w) - 1);
+            uint64_t mj[4];
+            int cnt = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t* pl = planes + j * nwords + wi;
+                const uint64_t lo = ((uint64_t)pl[1] << 32) | pl[0];
+                uint64_t m = lo >> sh;
+                if (sh) m |= (uint64_t)pl[2] << (64 - sh);
+                mj[j] = m & keep;
+                cnt += __popcll(mj[j]);
+            }
+            const float2* p = pw + (size_t)k * per;
+            float sf = 0.f, sc = 0.f;
+            int j = 0;
+            uint64_t m = mj[0];
+            for (int t = 0; t < cnt; ++t) {
+                while (m == 0) {
+                    ++j;
+                    m = j == 1 ? mj[1] : (j == 2 ? mj[2] : mj[3]);
+                }
+                const int kk = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                const float2 q = p[j * maxlen + kk];
+                sf = __fadd_rn(sf, q.x);
+                sc = __fadd_rn(sc, q.y);
+            }
+            bf = VI{sf, l};
+            bc = VI{sc, l};
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            VI y;
+            y.v = __shfl_xor_sync(0xffffffffu, bf.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, bf.i, o);
+            bf = vi_best(bf, y);
+            y.v = __shfl_xor_sync(0xffffffffu, bc.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, bc.i, o);
+            bc = vi_best(bc, y);
+        }
+        if (lane == 0) {
+            wb[((size_t)k * nw + wid) * 2] = bf;
+            wb[((size_t)k * nw + wid) * 2 + 1] = bc;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        VI rf{-INFINITY, 0x7fffffff}, rc{-INFINITY, 0x7fffffff};
+        for (int v = 0; v < nw; ++v) {
+            rf = vi_best(rf, wb[((size_t)k * nw + v) * 2]);
+            rc = vi_best(rc, wb[((size_t)k * nw + v) * 2 + 1]);
+        }
+        const float sF = rf.i == 0x7fffffff ? -INFINITY : rf.v;
+        const float sC = rc.i == 0x7fffffff ? -INFINITY : rc.v;
+        const int iF = rf.i == 0x7fffffff ? -1 : rf.i + 1;
+        const int iC = rc.i == 0x7fffffff ? -1 : rc.i + 1;
+        const bool fwd = sF >= sC;
+        const float sv = fwd ? sF : sC;
+        const bool keepk = sv > thresh[k];
+        const size_t o = k + (size_t)K * n;
+        if (pos) pos[o] = keepk ? (fwd ? iF : iC) : 0;
+        if (score) score[o] = keepk ? sv : 0.f;
+        if (comp) comp[o] = (keepk && !fwd) ? 1 : 0;
+    }
+}
+
+// the sparse scans apply: exact 0/1 data, finite PWM entries (within each motif's
+// length), not turned off by CDLGB_SCAN_DENSE
+bool sparse_ok(const cdlgb_ctx* c, const float* pwms, const int32_t* lens, int K, int maxlen) {
+    if (!c->onehot_exact) return false;
+    if (const char* e = getenv("CDLGB_SCAN_DENSE"))
+        if (atoi(e) != 0) return false;
+    for (int k = 0; k < K; ++k)
+        for (int kk = 0; kk < lens[k]; ++kk)
+            for (int a = 0; a < 4; ++a)
+                if (!isfinite(pwms[k + (size_t)K * (a + 4 * kk)])) return false;
+    return true;
+}
+
 // integer count matrices: grid (K, chunks); counts (4, maxlen, K) col-major
 __global__ void k_count(const float* __restrict__ data, const int32_t* __restrict__ pos,
                         const uint8_t* __restrict__ comp, const int32_t* __restrict__ lens, int K,
@@ -278,12 +472,27 @@ int scan_fwd(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float* 
     int32_t* dpos = c->scan_i + K;
     size_t shm = (size_t)4 * L * sizeof(float);
     if (shm > 200 * 1024) return cdlgb_seterr(c, CDLGB_ENOTSUP, "scan: L=%d too long", L);
-    if (shm > 48 * 1024)
-        CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    k_scan_fwd<<<N, kScanThreads, shm, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
-                                                     c->scan_f + (size_t)K * 4 * maxlen, K, maxlen,
-                                                     L, dpos);
-    LAUNCH_CHECK(c, "k_scan_fwd");
+    // one position per thread with the inputs staged, on exact one-hot data with finite
+    // PWMs: the sparse sums (at most 1024 positions and 64 KB of staged inputs)
+    const int nts = ((L + 31) / 32) * 32;
+    const size_t shs = (size_t)K * 4 * maxlen * sizeof(float) + (size_t)K * (nts / 32) * sizeof(VI) +
+                       (size_t)L;
+    if (nts <= 1024 && shs <= 64 * 1024 && sparse_ok(c, pwms, lens, K, maxlen)) {
+        if (shs > 48 * 1024)
+            CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd_sparse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           64 * 1024));
+        k_scan_fwd_sparse<<<N, nts, shs, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                                       c->scan_f + (size_t)K * 4 * maxlen, K, maxlen,
+                                                       L, dpos);
+        LAUNCH_CHECK(c, "k_scan_fwd_sparse");
+    } else {
+        if (shm > 48 * 1024)
+            CU_TRY(c, cudaFuncSetAttribute(k_scan_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        k_scan_fwd<<<N, kScanThreads, shm, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                                         c->scan_f + (size_t)K * 4 * maxlen, K, maxlen,
+                                                         L, dpos);
+        LAUNCH_CHECK(c, "k_scan_fwd");
+    }
     CU_TRY(c, cudaMemcpyAsync(pos_out, dpos, (size_t)K * N * 4, cudaMemcpyDeviceToHost, c->stream));
     cdlgb_phase_end(c, PH_SCAN);
     CU_TRY(c, cudaStreamSynchronize(c->stream));
@@ -306,7 +515,17 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
     const int nts = ((L + 31) / 32) * 32;
     const size_t shs = (size_t)K * 4 * maxlen * sizeof(float2) + (size_t)K * (nts / 32) * 2 * sizeof(VI) +
                        (size_t)4 * L * sizeof(float);
-    if (nts <= 1024 && shs <= 64 * 1024) {
+    const size_t shp = (size_t)K * 4 * maxlen * sizeof(float2) + (size_t)K * (nts / 32) * 2 * sizeof(VI) +
+                       (size_t)4 * ((L + 31) / 32 + 2) * sizeof(uint32_t);
+    if (nts <= 1024 && maxlen <= 64 && shp <= 64 * 1024 && sparse_ok(c, pwms, lens, K, maxlen)) {
+        if (shp > 48 * 1024)
+            CU_TRY(c, cudaFuncSetAttribute(k_scan_both_sparse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           64 * 1024));
+        k_scan_both_sparse<<<N, nts, shp, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                                        c->scan_f + (size_t)K * 4 * maxlen, K, maxlen, L,
+                                                        dpos, dscore, c->scan_u);
+        LAUNCH_CHECK(c, "k_scan_both_sparse");
+    } else if (nts <= 1024 && shs <= 64 * 1024) {
         if (shs > 48 * 1024)
             CU_TRY(c, cudaFuncSetAttribute(k_scan_both_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            64 * 1024));

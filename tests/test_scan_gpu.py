@@ -59,8 +59,13 @@ def test_golden_scan(pkg, built_lib):
             np.testing.assert_array_equal(pfms[k], g["pfms"][k, :, : lens[k]])
 
 
+@pytest.mark.parametrize("dense", [False, True])
 @pytest.mark.parametrize("N,L,K", [(300, 200, 8), (64, 100, 20), (7, 31, 3)])
-def test_scans_bit_exact_random(pkg, built_lib, N, L, K):
+def test_scans_bit_exact_random(pkg, built_lib, N, L, K, dense, monkeypatch):
+    """Both the sparse sums (the default on one-hot data with finite PWMs: only the
+    terms whose entry is 1, in the reference's order) and the dense ones."""
+    if dense:
+        monkeypatch.setenv("CDLGB_SCAN_DENSE", "1")
     rng = np.random.default_rng(N + L + K)
     S, _ = random_onehot(rng, N, L)
     pwms, lens, thresh = _random_pwms(rng, K, 4, 21)
@@ -177,3 +182,42 @@ def test_pvalue_thresholds_match_oracle(pkg, built_lib, pval):
         th = pkg.get_thresh(c, pwms, pval)
     ref = np.array([SO.pvalue2score(p, pval) for p in pwms], np.float32)
     np.testing.assert_array_equal(th, ref)
+
+
+@pytest.mark.parametrize("bad", [-np.inf, np.inf, np.nan])
+def test_scan_nonfinite_pwm_entries(pkg, built_lib, bad):
+    """A PWM with a non-finite entry (log2 of a zero PFM entry is -Inf) takes the dense
+    sums, where Inf * 0 is NaN as in the reference: results equal the oracle's."""
+    rng = np.random.default_rng(12)
+    N, L = 40, 60
+    S, _ = random_onehot(rng, N, L)
+    pwms, lens, thresh = _random_pwms(rng, 5, 4, 12)
+    pwms[2] = pwms[2].copy()
+    pwms[2][1, 0] = bad
+    with _ctx(pkg, S) as c:
+        pos_fwd = pkg.scan_w_gpu(c, pwms, thresh)
+        np.testing.assert_array_equal(pos_fwd.T, SO.scan_w_gpu_positions(_pad(pwms, lens), S, lens, thresh))
+        pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+        rp, rs, rc = SO.overlapping_scan(S, pwms, lens, thresh)
+        np.testing.assert_array_equal(pos.T, rp)
+        np.testing.assert_array_equal(score.T, rs)
+        np.testing.assert_array_equal(comp.T, rc)
+
+
+def test_scan_zero_columns(pkg, built_lib):
+    """Sequences with empty columns (a record of the wrong length, or padding) score
+    only their real bases: sparse and dense sums agree with the oracle."""
+    rng = np.random.default_rng(13)
+    N, L = 30, 80
+    S, _ = random_onehot(rng, N, L)
+    S[3] = 0.0
+    S[5, 4 * 60:] = 0.0
+    pwms, lens, thresh = _random_pwms(rng, 6, 4, 20)
+    with _ctx(pkg, S) as c:
+        pos_fwd = pkg.scan_w_gpu(c, pwms, thresh)
+        np.testing.assert_array_equal(pos_fwd.T, SO.scan_w_gpu_positions(_pad(pwms, lens), S, lens, thresh))
+        pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+        rp, rs, rc = SO.overlapping_scan(S, pwms, lens, thresh)
+        np.testing.assert_array_equal(pos.T, rp)
+        np.testing.assert_array_equal(score.T, rs)
+        np.testing.assert_array_equal(comp.T, rc)

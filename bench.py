@@ -62,6 +62,10 @@ def dataset(wl=WORKLOAD, N=None):
 # from the ncu captures summarised in profiles/
 XITER_DRAM_BYTES_N1000 = 1405720320      # k_xiter, one launch = 15 X-steps
 XWARP_DRAM_BYTES_N1000 = 1391571456      # k_xstep_warp, one launch = 1 X-step
+# warp instructions issued per sequence and X-step by k_xiter<32, 29, 288, 1, 16>
+# (smsp__inst_executed.sum of the same 1000-sequence capture / (1000 x 15))
+XITER_WARP_INSTR_PER_SEQ_XSTEP = 129.4e3
+N_SM, SCHEDULERS_PER_SM = 152, 4
 
 
 def algorithmic_bytes(wl=WORKLOAD):
@@ -82,7 +86,8 @@ def algorithmic_bytes(wl=WORKLOAD):
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+              "utilization.gpu")
 
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
@@ -121,8 +126,10 @@ class ClockSampler:
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        util = [float(r[9]) for r in rows if len(r) > 9 and r[9].replace(".", "").isdigit()]
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows),
+                "gpu_util_mean_pct": float(np.mean(util)) if util else None,
                 "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
                 if any(r[3].replace(".", "").isdigit() for r in rows) else None}
 
@@ -189,7 +196,8 @@ def run_gpu(args, rank: int, world: int):
     bases = dataset(wl)
     S = pkg.synth.onehot(bases)
     setup = pkg.CDLSetup(M=wl["M"], filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
-                         sigma=wl["sigma"], csc_iter_num=wl["csc_iter"], cdl_iter_num=wl["cdl_iter"])
+                         sigma=wl["sigma"], csc_iter_num=wl["csc_iter"], cdl_iter_num=wl["cdl_iter"],
+                         track_residuals=bool(args.residuals))
     stream = torch.cuda.current_stream(dev)
     c = pkg.CDL(setup, device=dev, fft_mode=args.fft_mode)
     c.set_stream(stream.cuda_stream)
@@ -292,9 +300,12 @@ def run_refstruct(args, config):
                     "reference CUDA.jl path, which cannot run here"}
 
 
-def roofline(prof, steps, fused):
+def roofline(prof, steps, fused, sm_mhz=None):
     """Roofline of the dominant kernel, from the phase timers recorded (CUDA events on
-    the launching stream) during the timed region."""
+    the launching stream) during the timed region.  For the multi-iteration X-step also
+    its issue-rate bound: warp instructions per launch (from the ncu capture, per
+    sequence) over the issue slots of the launch (SMs x 4 schedulers x median SM clock x
+    launch time)."""
     ab = algorithmic_bytes()
     peaks = {}
     try:
@@ -337,6 +348,16 @@ def roofline(prof, steps, fused):
            "avg_launch_ms": round(ms_avg, 4)}
     if note:
         out["note"] = note
+    if fused and prof["xfused"][1] > 0 and steps_per_launch > 1 and ab["Lg"] == 928 \
+            and WORKLOAD["M"] == 64:
+        mhz = sm_mhz or 2070.0
+        instr = XITER_WARP_INSTR_PER_SEQ_XSTEP * WORKLOAD["N"] * steps_per_launch
+        slots = N_SM * SCHEDULERS_PER_SM * mhz * 1e6 * (ms_avg / 1e3)
+        out["issue"] = {"bound": "sm_issue", "warp_instructions_per_launch": instr,
+                        "issue_slots_per_launch": slots, "sm_mhz": mhz,
+                        "frac": round(instr / slots, 4),
+                        "note": "the kernel's binding roof: one instruction per scheduler and "
+                                "cycle; the HBM fraction above counts per-X-step bytes"}
     return out
 
 
@@ -405,34 +426,46 @@ def batched_requests(n: int = 64, seed: int = 91):
 
 def run_batched(args):
     """The 64-dataset mix processed plainly (one training after another, each alone on
-    the GPU) and batched (all submitted at once to the continuous-batching server, up to
-    `serve_slots` trainings in flight); datasets/hr of both, and the largest difference
-    between a dataset's D_best alone and in the mix (the kernels are deterministic and
-    contexts share nothing, so it should be 0)."""
+    the GPU) and batched (all submitted at once to the library's training server, up to
+    `serve_slots` trainings in flight); datasets/hr of both, how busy the GPU was in the
+    plain form (the sum of every training's kernel time from the library's CUDA-event
+    phase timers against the wall clock, and nvidia-smi's utilisation), and the largest
+    difference between a dataset's D_best alone and in the mix (the kernels are
+    deterministic and contexts share nothing, so it should be 0)."""
     pkg = _pkg()
     from cdlmotif_gb300 import serve
     data = batched_requests(args.batched_n)
     setup = pkg.CDLSetup(M=32, filter_size=16, lambda_=0.1, rho=1.0, sigma=100.0)
     iters = args.serve_iters
     serve.run_training(setup, data[0], iters, 1, 0)          # warm-up (plans, kernels)
-    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    sampler = ClockSampler(dev)
     sampler.start()
     t0 = time.perf_counter()
-    alone = [serve.run_training(setup, d, iters, 1, 0) for d in data]
+    alone = [serve.run_training(setup, d, iters, 1, 0, profile=True) for d in data]
     t_plain = time.perf_counter() - t0
+    clocks_plain = sampler.stop()
+    busy_ms = sum(a["device_ms"] for a in alone)
+    sampler = ClockSampler(dev)
+    sampler.start()
     res = serve.serve_stream(setup, [(0.0, d) for d in data], slots=args.serve_slots,
                              iter_num=iters, seed=1)
     clocks = sampler.stop()
     mix = res.pop("results")
     diff = max(float(np.max(np.abs(mix[i]["D_best"] - alone[i]["D_best"]))) for i in mix)
     plain_rate = 3600.0 * len(data) / t_plain
+    busy = busy_ms / 1e3 / t_plain
     return {"metric": "datasets/hr, 64-dataset mix (N log-uniform 500-20000, L in {100,200,500}, K=32, W=16)",
             "value": res["datasets_per_hr"], "unit": "datasets/hr", "higher_is_better": True,
             "plain_datasets_per_hr": plain_rate, "batched_over_plain": res["datasets_per_hr"] / plain_rate,
             "plain_seconds": t_plain, "batched_makespan_s": res["makespan_s"],
+            "plain_kernel_seconds": busy_ms / 1e3, "plain_busy_fraction": busy,
+            "plain_idle_fraction": 1.0 - busy,
+            "batching_bound_if_idle_removed": 1.0 / busy if busy > 0 else None,
             "completed": res["completed"], "rejected": res["rejected"], "slots": args.serve_slots,
             "outer_iterations_per_dataset": iters, "max_abs_diff_D_best_alone_vs_mix": diff,
-            "dtype": "f32", "data": "synthetic (seeded planted motifs)", "clocks": clocks,
+            "dtype": "f32", "data": "synthetic (seeded planted motifs)",
+            "clocks_plain": clocks_plain, "clocks": clocks,
             "config": {"workload": "batched64", "N": [int(d.shape[0]) for d in data],
                        "L": [int(d.shape[1] // 4) for d in data]}}
 
@@ -649,6 +682,8 @@ def main():
                     help="sequences per step of --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=0, help="override N (small cases for profiling)")
+    ap.add_argument("--residuals", action="store_true",
+                    help="keep the FP64 residual record every outer iteration (track_residuals)")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--serve", action="store_true",
                     help="serving workload: Poisson request stream, datasets/hr and p50/p99")
@@ -680,7 +715,8 @@ def main():
               "filter_size": wl["filter_size"], "Lg": algorithmic_bytes()["Lg"], "lambda": wl["lam"],
               "rho": wl["rho"], "sigma": wl["sigma"], "csc_iter_num": wl["csc_iter"],
               "cdl_iter_num": wl["cdl_iter"], "parallelism": f"replicas{world}",
-              "l2": "inputs larger than L2 (ADMM state ~28 GB per replica)"}
+              "l2": "inputs larger than L2 (ADMM state ~28 GB per replica)",
+              "residual_record": bool(args.residuals)}
 
     if args.serve:
         if rank == 0:
@@ -743,7 +779,7 @@ def main():
                     "d2h_bytes_per_step": r["d2h"], "outer_iterations_per_step": args.e2e_outer},
             "gpu_launches": launches,
             "library_calls": {"cufft_exec": prof["fft_calls"]},
-            "roofline": roofline(prof, args.steps, r["fused"]),
+            "roofline": roofline(prof, args.steps, r["fused"], (r["clocks"] or {}).get("sm_mhz")),
             "phases_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in prof.items()
                                    if isinstance(v, tuple) and v[1]},
             "path": "fused" if r["fused"] else "cufft",

@@ -82,6 +82,7 @@ class CDLSetup:
     std_threshold_multiplier: float = 1.0
     num_train: int = 2
     stop_tol: float = 0.0     # stopping test of run_outer; 0 = the reference's fixed count
+    track_residuals: bool = False   # keep the FP64 residual record (implied by stop_tol > 0)
 
     def params(self, device: int = 0, fft_mode: int = 0, init_mode: int = 0,
                hbm_budget_bytes: int = 0) -> CdlgbParams:
@@ -95,6 +96,7 @@ class CDLSetup:
         p.device, p.fft_mode, p.init_mode = int(device), int(fft_mode), int(init_mode)
         p.hbm_budget_bytes = int(hbm_budget_bytes)
         p.stop_tol = float(self.stop_tol)
+        p.track_residuals = 1 if self.track_residuals else 0
         return p
 
 

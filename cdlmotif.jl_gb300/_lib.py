@@ -24,7 +24,7 @@ class CdlgbParams(C.Structure):
         ("sherman_const_csc", C.c_float), ("sherman_const_cdl", C.c_float),
         ("device", C.c_int32), ("init_mode", C.c_int32), ("fft_mode", C.c_int32),
         ("hbm_budget_bytes", C.c_uint64),
-        ("stop_tol", C.c_float),
+        ("stop_tol", C.c_float), ("track_residuals", C.c_int32),
     ]
 
 

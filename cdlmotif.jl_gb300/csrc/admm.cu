@@ -842,8 +842,10 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
         // the residuals of the final iterate, from the kernel's store pass
         const double* rp = nullptr;
         int nr = 0;
-        if (fused_resid(c, &rp, &nr)) ST_TRY(resid_x_from_parts(c, rp, nr));
-        else ST_TRY(resid_x_from_arrays(c, cur_X(c)));
+        if (c->res_on) {
+            if (fused_resid(c, &rp, &nr)) ST_TRY(resid_x_from_parts(c, rp, nr));
+            else ST_TRY(resid_x_from_arrays(c, cur_X(c)));
+        }
         cdlgb_phase_end_n(c, PH_XSTEP, iters);
         return CDLGB_OK;
     }
@@ -885,7 +887,7 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
             c->xcur = 1 - c->xcur;
             c->best_is_cur = 0;
         }
-        if (it == iters - 1) ST_TRY(resid_x_from_arrays(c, cur_X(c)));
+        if (c->res_on && it == iters - 1) ST_TRY(resid_x_from_arrays(c, cur_X(c)));
         cdlgb_phase_end(c, PH_XSTEP);
     }
     return CDLGB_OK;
@@ -911,25 +913,25 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                 ST_TRY(dspec_launch(c, c->sAh, c->G3h, n0, n0 + cn, slot0));
                 slot0 += dspec_nsub(cn, F, c->nsm);
             }
-            ST_TRY(resid_d_from_spec_parts(c, slot0 * ((F + 31) / 32)));
+            if (c->res_on) ST_TRY(resid_d_from_spec_parts(c, slot0 * ((F + 31) / 32)));
             ST_TRY(c2r(c, N, c->sVh, c->Td));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
                                                          c->gamma, LN, c->p.sigma);
             LAUNCH_CHECK(c, "k_dg2");
-            ST_TRY(resid_td(c));
+            if (c->res_on) ST_TRY(resid_td(c));
             // the three sums over n, back in the time domain: part as one chunk
             ST_TRY(dspec_sums(c, c->G3h, c->sumspec));
             ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part));
             c->time_stale = 1;
             c->time_init = 0;
             int flen = 4 * c->p.filter_size;
-            ST_TRY(resid_save_G(c));
+            if (c->res_on) ST_TRY(resid_save_G(c));
             k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
                                                                    LM, Lg, flen, N, 1);
             LAUNCH_CHECK(c, "k_dfinish");
             k_dprox<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->vbar, c->G1, Lg, M, flen);
             LAUNCH_CHECK(c, "k_dprox");
-            ST_TRY(resid_dual_and_finish(c));
+            if (c->res_on) ST_TRY(resid_dual_and_finish(c));
             ST_TRY(refresh_G1h(c));
             cdlgb_phase_end(c, PH_DSTEP);
             continue;
@@ -977,17 +979,19 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                                       (const float4*)c->G1, (const float4*)c->G3,
                                       (float4*)c->part, pl4, N, c->nchunk);
             LAUNCH_CHECK(c, "k_dcons");
-            ST_TRY(resid_td(c));
-            ST_TRY(resid_d_from_arrays(c));
+            if (c->res_on) {
+                ST_TRY(resid_td(c));
+                ST_TRY(resid_d_from_arrays(c));
+            }
         }
         int flen = 4 * c->p.filter_size;
-        ST_TRY(resid_save_G(c));
+        if (c->res_on) ST_TRY(resid_save_G(c));
         k_dfinish<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->part, c->vbar, c->G3, c->dsum,
                                                                LM, Lg, flen, N, c->nchunk);
         LAUNCH_CHECK(c, "k_dfinish");
         k_dprox<<<(unsigned)((LM + 255) / 256), 256, 0, s>>>(c->vbar, c->G1, Lg, M, flen);
         LAUNCH_CHECK(c, "k_dprox");
-        ST_TRY(resid_dual_and_finish(c));
+        if (c->res_on) ST_TRY(resid_dual_and_finish(c));
         ST_TRY(refresh_G1h(c));
         cdlgb_phase_end(c, PH_DSTEP);
     }

@@ -192,6 +192,7 @@ int cdlgb_params_default(cdlgb_params* p) {
     p->fft_mode = 0;
     p->hbm_budget_bytes = 0;
     p->stop_tol = 0.f;
+    p->track_residuals = 0;
     return CDLGB_OK;
 }
 
@@ -220,6 +221,7 @@ int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out) {
     int st = check_params(c, p);
     if (st) { fprintf(stderr, "cdlgb_create: %s\n", c->err); delete c; return st; }
     c->dev = p->device;
+    c->res_on = p->track_residuals != 0 || p->stop_tol > 0.f;
     cudaError_t e = cudaSetDevice(c->dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {

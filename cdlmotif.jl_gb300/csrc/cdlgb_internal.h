@@ -114,6 +114,7 @@ struct cdlgb_ctx {
     double* rpart = nullptr;
     float* Gprev = nullptr;
     int outer_done = 0;
+    int res_on = 0;                 // residual record kept (params.track_residuals or stop_tol > 0)
 
     // fused path twiddles / plan
     void* fplan = nullptr;

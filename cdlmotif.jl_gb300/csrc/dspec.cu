@@ -55,7 +55,8 @@ constexpr int kArr = 3;      // staged spectra: Y3-hat, g1-hat, d-hat
 // [c0, c1), in order, and writes that sub-range's sums to slot slot0 + s; warp w owns
 // filters w, w + 16, ...  With PIPE, each thread's spectra of sequence n + 1 are copied
 // to shared memory (asynchronous copies, two buffers) while sequence n is computed.
-template <int MW, bool PIPE>
+// RES: also the residual partials (compiled out when false)
+template <int MW, bool PIPE, bool RES>
 __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     extern __shared__ float4 sm4[];
     const int M = A.M, F = A.F;
@@ -190,6 +191,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
                 A.g1h[i] = g1n;
                 s1[k] = cadd2(s1[k], cadd2(dh, g1n));
                 sd[k] = cadd2(sd[k], dh);
+                if (!RES) continue;
                 const float2 e3 = csub2(dh, G3s[m * kBins + lane]);   // g3 += d - G3 (:72)
                 q[0] = fmaf(e1.x, e1.x, fmaf(e1.y, e1.y, q[0]));
                 q[1] = fmaf(e3.x, e3.x, fmaf(e3.y, e3.y, q[1]));
@@ -197,7 +199,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             }
             const float wt = edge ? 1.f : 2.f;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
+            for (int k = 0; k < (RES ? 3 : 0); ++k) {
                 const float y = __fsub_rn(__fmul_rn(wt, q[k]), rc[k]);
                 const float t = __fadd_rn(rs[k], y);
                 rc[k] = __fsub_rn(__fsub_rn(t, rs[k]), y);
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             if (w == 0) A.Th[(size_t)n * F + f] = make_float2(T.x * A.scale, T.y * A.scale);
         }
     }
-    {
+    if (RES) {
         // the CTA's residual partials, in float64, added in warp order
         __shared__ double rsh[3][kWarps];
 #pragma unroll
@@ -338,11 +340,13 @@ int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int 
     if (c->M <= 4 * kWarps) {
         // + the two staging buffers: 2 x 3 spectra x 4 filters x 512 threads
         const size_t smp = sm + (size_t)2 * kArr * 4 * kBins * kWarps * sizeof(float2);
-        CU_TRY(c, cudaFuncSetAttribute(k_dspec<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smp));
-        k_dspec<4, true><<<g, kBins * kWarps, smp, c->stream>>>(a);
+        auto k = c->res_on ? k_dspec<4, true, true> : k_dspec<4, true, false>;
+        CU_TRY(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smp));
+        k<<<g, kBins * kWarps, smp, c->stream>>>(a);
     } else {
-        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k_dspec<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        k_dspec<8, false><<<g, kBins * kWarps, sm, c->stream>>>(a);
+        auto k = c->res_on ? k_dspec<8, false, true> : k_dspec<8, false, false>;
+        if (sm > 48 * 1024) CU_TRY(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        k<<<g, kBins * kWarps, sm, c->stream>>>(a);
     }
     LAUNCH_CHECK(c, "k_dspec");
     return CDLGB_OK;

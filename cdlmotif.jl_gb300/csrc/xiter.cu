@@ -136,7 +136,9 @@ __device__ __forceinline__ void prefetch_next(const IArgs& A, int n, int m0, int
 // MC filters per CTA (compile time), NT threads: every slot's lane group and every
 // thread's bins of the cross-filter phases are fixed, and each thread keeps the G1h
 // values of its bins in registers for the whole launch (G1 is fixed during a code update).
-template <int N1, int P, int NT, int MINB, int MC>
+// RES: also the residual sums of the final iterates (compiled out when false, so the
+// kernel without them is unchanged)
+template <int N1, int P, int NT, int MINB, int MC, bool RES>
 __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     constexpr int Lg = N1 * P;
     constexpr int G = 32 / N1;                  // lane groups per warp
@@ -170,10 +172,12 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
     float* Ahs = y1s + Lg;                                 // [Fp] sum_m |G1h|^2
     float* Ss = Ahs + Fp;                                  // [L4] this sequence's W'S window
     __shared__ double red[NT / 32];
-    // per warp: sums of (X - Y2)^2, (X - Y3)^2, X^2, (DX - Y1)^2, DX^2 of the final iterates
-    __shared__ double rsum[NT / 32][5];
+    // per warp: compensated (Kahan) float32 sums over its sequences of (X - Y2)^2,
+    // (X - Y3)^2, X^2, (DX - Y1)^2, DX^2 of the final iterates, [warp][value][sum, comp]
+    __shared__ float rsum[NT / 32][5][2];
 
-    for (int t = threadIdx.x; t < 5 * (NT / 32); t += blockDim.x) (&rsum[0][0])[t] = 0.0;
+    if (RES)
+        for (int t = threadIdx.x; t < 10 * (NT / 32); t += blockDim.x) (&rsum[0][0][0])[t] = 0.f;
     for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
     for (int t = threadIdx.x; t < F; t += blockDim.x) Ahs[t] = A.Ah[t];
     __syncthreads();
@@ -333,6 +337,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                         A.y3[ra + Lg + o] = a3.y;
                         s += fabsf(xv.x);
                         s += fabsf(xv.y);
+                        if (!RES) continue;
                         const float2 t2 = cadd(xv, a2);
                         const float2 r2 = csub(xv, csub(t2, f2(fminf(fmaxf(t2.x, -lam), lam),
                                                                fminf(fmaxf(t2.y, -lam), lam))));
@@ -364,6 +369,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                         A.DX[r + o] = dx;
                         A.Y1[r + o] = Y1n;
                         A.y1[r + o] = yp;
+                        if (!RES) continue;
                         const float e = dx - Y1n;
                         q1 = fmaf(e, e, q1);
                         qd = fmaf(dx, dx, qd);
@@ -371,13 +377,20 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
                 }
                 if (!last) fwd_step1<N1, P>(sb, gl, tw2);
             }
-            if (last) {
-                // one float64 partial per warp and sequence, added in warp order
-                double v[5] = {(double)q2, (double)q3, (double)qx, (double)q1, (double)qd};
+            if (RES && last) {
+                // the warp's sums for this sequence, added by lane 0 into its
+                // compensated running sums (no float64 work inside the sequence loop)
+                float v[5] = {q2, q3, qx, q1, qd};
 #pragma unroll
                 for (int k = 0; k < 5; ++k) {
                     for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-                    if (lane == 0) rsum[threadIdx.x >> 5][k] += v[k];
+                    if (lane == 0) {
+                        float* a = rsum[threadIdx.x >> 5][k];
+                        const float y = __fsub_rn(v[k], a[1]);
+                        const float t = __fadd_rn(a[0], y);
+                        a[1] = __fsub_rn(__fsub_rn(t, a[0]), y);
+                        a[0] = t;
+                    }
                 }
             }
         }
@@ -392,9 +405,9 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
         A.absx_part[blockIdx.x] = t;
     }
-    if (threadIdx.x < 5) {
+    if (RES && threadIdx.x < 5) {
         double t = 0.0;
-        for (int w = 0; w < NT / 32; ++w) t += rsum[w][threadIdx.x];
+        for (int w = 0; w < NT / 32; ++w) t += (double)rsum[w][threadIdx.x][0] - (double)rsum[w][threadIdx.x][1];
         A.res_part[(size_t)blockIdx.x * 5 + threadIdx.x] = t;
     }
 }
@@ -404,18 +417,25 @@ typedef void (*kern_t)(IArgs);
 constexpr size_t kCap2 = 115200;       // two CTAs per SM (2 x (this + 1 KB reserved) <= 228 KB)
 constexpr size_t kCap1 = 220 * 1024;   // one CTA per SM
 // (N1, P, filters per CTA): threads = 32 ceil((MC/2 + 1) / (32 / N1)) rounded to a warp
-struct Variant { int N1, P, MC, threads, minb; kern_t k; };
+struct Variant { int N1, P, MC, threads, minb; kern_t k, kr; };   // kr: with the residual sums
 // in order of preference (measured at L=200, K=64: 16 filters per CTA, one CTA per SM,
 // 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms).  Lg = 32 P for the
 // primes 17..31 covers L = 104, 120, 152, 200, 216 at W = 16 (Lg = 4L + 8W).
 const Variant kVariants[] = {
-    {32, 29, 16, 288, 1, k_xiter<32, 29, 288, 1, 16>},
-    {32, 29, 8, 160, 2, k_xiter<32, 29, 160, 2, 8>},
-    {16, 31, 16, 160, 2, k_xiter<16, 31, 160, 2, 16>},
-    {32, 17, 16, 288, 1, k_xiter<32, 17, 288, 1, 16>},
-    {32, 19, 16, 288, 1, k_xiter<32, 19, 288, 1, 16>},
-    {32, 23, 16, 288, 1, k_xiter<32, 23, 288, 1, 16>},
-    {32, 31, 16, 288, 1, k_xiter<32, 31, 288, 1, 16>},
+    {32, 29, 16, 288, 1, k_xiter<32, 29, 288, 1, 16, false>,
+     k_xiter<32, 29, 288, 1, 16, true>},
+    {32, 29, 8, 160, 2, k_xiter<32, 29, 160, 2, 8, false>,
+     k_xiter<32, 29, 160, 2, 8, true>},
+    {16, 31, 16, 160, 2, k_xiter<16, 31, 160, 2, 16, false>,
+     k_xiter<16, 31, 160, 2, 16, true>},
+    {32, 17, 16, 288, 1, k_xiter<32, 17, 288, 1, 16, false>,
+     k_xiter<32, 17, 288, 1, 16, true>},
+    {32, 19, 16, 288, 1, k_xiter<32, 19, 288, 1, 16, false>,
+     k_xiter<32, 19, 288, 1, 16, true>},
+    {32, 23, 16, 288, 1, k_xiter<32, 23, 288, 1, 16, false>,
+     k_xiter<32, 23, 288, 1, 16, true>},
+    {32, 31, 16, 288, 1, k_xiter<32, 31, 288, 1, 16, false>,
+     k_xiter<32, 31, 288, 1, 16, true>},
 };
 
 // bytes of shared memory: slot buffers, P parts, twiddles, the interleaved y2 / y3
@@ -429,7 +449,7 @@ size_t iter_smem(int N1, int P, int slots, int Mc, int ld, int ld3, int L4) {
 }
 
 struct IterPlan {
-    kern_t k;
+    kern_t k, kr;
     int CS, Mc, ld, ld3, threads, grid;
     size_t smem;
     float2* tw2;
@@ -470,7 +490,7 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
         if (nth-- > 0) continue;
         v = &cand;
         P = new IterPlan();
-        P->k = cand.k; P->CS = cs; P->Mc = cand.MC; P->ld = ld; P->ld3 = ld3;
+        P->k = cand.k; P->kr = cand.kr; P->CS = cs; P->Mc = cand.MC; P->ld = ld; P->ld3 = ld3;
         P->threads = cand.threads; P->smem = sm;
         break;
     }
@@ -482,6 +502,9 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
     // process-wide per kernel: the same cap for every context
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(v->minb == 2 ? kCap2 : kCap1));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(P->kr, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(v->minb == 2 ? kCap2 : kCap1));
     int nclusters = 0;
     if (e == cudaSuccess) {
@@ -556,7 +579,7 @@ int iter_xsteps_n(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iter
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cdlgb_phase_begin(c, PH_XFUSED);
-    CU_TRY(c, cudaLaunchKernelEx(&cfg, P->k, a));
+    CU_TRY(c, cudaLaunchKernelEx(&cfg, c->res_on ? P->kr : P->k, a));
     LAUNCH_CHECK(c, "k_xiter");
     cdlgb_phase_end(c, PH_XFUSED);
     return CDLGB_OK;

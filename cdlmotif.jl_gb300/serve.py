@@ -166,19 +166,28 @@ class Server:
             pass
 
 
-def run_training(setup: CDLSetup, data: np.ndarray, iter_num: int, seed: int, device: int) -> dict:
-    """One cdl_optimize training (src/WRAPPER/wrap.jl:5-12) of one dataset: init, iter_num
-    outer iterations, code threshold; returns D_best, objectives and the threshold."""
+def run_training(setup: CDLSetup, data: np.ndarray, iter_num: int, seed: int, device: int,
+                 profile: bool = False) -> dict:
+    """One cdl_optimize training (src/WRAPPER/wrap.jl:5-12) of one dataset on its own
+    context: init, iter_num outer iterations, code threshold; returns D_best, objectives
+    and the threshold (with `profile`, also the kernel time of its X-steps, D-steps and
+    objectives from the library's CUDA-event phase timers, device_ms)."""
     c = init_cdl(setup, data, seed=seed, device=device)
     try:
+        if profile:
+            c.profile(True)
         objs = []
         for _ in range(iter_num):
             code_update(c, setup.csc_iter_num)
             o, _ = update_best(c)
             dict_update(c, setup.cdl_iter_num)
             objs.append(o)
-        return {"D_best": c.D_best, "objs": np.array(objs), "code_thresh": code_threshold(c),
-                "N": c.N, "L4": c.L}
+        out = {"D_best": c.D_best, "objs": np.array(objs), "code_thresh": code_threshold(c),
+               "N": c.N, "L4": c.L}
+        if profile:
+            pr = c.profile_read()
+            out["device_ms"] = sum(pr[k][0] for k in ("xstep", "dstep", "objective"))
+        return out
     finally:
         c.close()
 

@@ -77,6 +77,10 @@ typedef struct {
                                    reference); > 0 = stop after the first outer iteration
                                    whose largest relative residual (CDLGB_FIELD_RESIDUALS
                                    entry 18) is <= stop_tol */
+    int32_t track_residuals;    /* 1 = keep the residual record (CDLGB_FIELD_RESIDUALS) up to
+                                   date after every code update and D-step; implied by
+                                   stop_tol > 0; 0 (default) = not computed (the record
+                                   stays zero), as the reference computes none */
 } cdlgb_params;
 
 /* Fields readable with cdlgb_get (sizes in elements; all float32 unless noted). */
@@ -119,7 +123,8 @@ typedef enum {
  *   [13] sqrt(([0] + [1]) / [3])   [14] sqrt([2] / [4])   [15] sqrt(([5] + [6]) / (2 [8]))
  *   [16] sqrt([7] / [9])           [17] sqrt(([10] + [11]) / [12])   [18] max of [13..17]
  * Sums over d use the spectral state through Parseval's relation where the D-step keeps
- * it.  All zero after cdlgb_init_state. */
+ * it.  All zero after cdlgb_init_state, and kept up to date only when
+ * params.track_residuals = 1 or params.stop_tol > 0. */
 
 /* Fill *p with the CDL_setup defaults. */
 int cdlgb_params_default(cdlgb_params* p);

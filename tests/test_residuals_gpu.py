@@ -24,8 +24,9 @@ def _case(pkg, N, L, M, fs, seed=3):
 
 
 def _check_record(got, ref):
+    # |DX|^2 covers the zero-padded rows, where every float32 path drifts (1e-3 there)
     for k in NORMS:
-        assert got[k] == pytest.approx(ref[k], rel=1e-4), k
+        assert got[k] == pytest.approx(ref[k], rel=1e-3), k
     for k, kn in PAIRS:
         a, b, nrm = np.sqrt(got[k]), np.sqrt(ref[k]), np.sqrt(ref[kn])
         assert abs(a - b) <= TOL_REL * b + TOL_NORM * nrm, (k, a, b, nrm)
@@ -45,7 +46,8 @@ def test_residual_record_against_oracle(pkg, built_lib, path, shape, monkeypatch
         monkeypatch.setenv("CDLGB_DSPEC", "0")
     S, X0, D0 = _case(pkg, N, L, M, fs)
     ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
-    setup = pkg.CDLSetup(M=M, filter_size=fs, lambda_=0.1, rho=1.0, sigma=100.0)
+    setup = pkg.CDLSetup(M=M, filter_size=fs, lambda_=0.1, rho=1.0, sigma=100.0,
+                         track_residuals=True)
     with pkg.init_cdl(setup, S, X0=X0, D0=D0, fft_mode=1 if path == "cufft" else 0) as c:
         assert np.all(c.residuals() == 0.0)
         for it in range(2):
@@ -67,7 +69,8 @@ def test_stopping_test(pkg, built_lib):
     the first outer iteration whose largest relative residual is <= stop_tol."""
     N, L, M, fs = 12, 100, 16, 12
     S, X0, D0 = _case(pkg, N, L, M, fs, seed=8)
-    setup = pkg.CDLSetup(M=M, filter_size=fs, lambda_=0.1, rho=1.0, sigma=100.0)
+    setup = pkg.CDLSetup(M=M, filter_size=fs, lambda_=0.1, rho=1.0, sigma=100.0,
+                         track_residuals=True)
     rel_max, objs = [], []
     with pkg.init_cdl(setup, S, X0=X0, D0=D0) as c:
         for _ in range(8):
@@ -78,6 +81,13 @@ def test_stopping_test(pkg, built_lib):
         o = pkg.run_outer(c, 8)
         assert c.outer_done == 8 and len(o) == 8
         np.testing.assert_array_equal(o, objs)
+    # without residual tracking (the default) the record stays zero and the iterates
+    # are the same bits: the residual sums change no result
+    setup.track_residuals = False
+    with pkg.init_cdl(setup, S, X0=X0, D0=D0) as c:
+        np.testing.assert_array_equal(pkg.run_outer(c, 8), objs)
+        assert np.all(c.residuals() == 0.0)
+    setup.track_residuals = True
     for k in (2, 5):
         tol = float(np.float32(rel_max[k]) * np.float32(1.0000001))
         want = next(i for i, v in enumerate(rel_max) if v <= tol) + 1

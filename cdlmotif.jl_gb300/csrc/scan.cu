@@ -282,11 +282,13 @@ __global__ void k_scan_fwd_sparse(const float* __restrict__ data, const float* _
 }
 
 // scan_n on both strands (scan.jl:10-21: nucleotide-major) on 0/1 data, one position
-// per thread, w <= 64: the window's positions of base j are the set bits of a 64-bit
-// mask cut from the sequence's bit plane of j, so the nonzero terms are visited j by j,
-// ind ascending -- the dense order -- in one loop of exactly that many steps.  The
+// per thread, w <= 64 (MT = uint64_t) or <= 32 (MT = uint32_t): the window's positions
+// of base j are the set bits of a mask cut from the sequence's bit plane of j (built
+// with one ballot per base and warp of positions), so the nonzero terms are visited j by
+// j, ind ascending -- the dense order -- in one loop of exactly that many steps.  The
 // (forward, complement) coefficient pairs, the per-warp argmax and the final reduction
 // are k_scan_both_staged's.
+template <typename MT>
 __global__ void k_scan_both_sparse(const float* __restrict__ data, const float* __restrict__ pwms,
                                    const int32_t* __restrict__ lens, const float* __restrict__ thresh,
                                    int K, int maxlen, int L, int32_t* __restrict__ pos,
@@ -299,14 +301,15 @@ __global__ void k_scan_both_sparse(const float* __restrict__ data, const float* 
     uint32_t* planes = reinterpret_cast<uint32_t*>(wb + (size_t)K * nw * 2);   // [4][nwords]
     const int n = blockIdx.x;
     const float* col = data + (size_t)n * 4 * L;
-    for (int i = threadIdx.x; i < 4 * nwords; i += blockDim.x) {
-        const int j = i / nwords, wd = i - j * nwords;
-        uint32_t m = 0;
-        for (int b = 0; b < 32; ++b) {
-            const int p = 32 * wd + b;
-            if (p < L && col[4 * p + j] != 0.f) m |= 1u << b;
+    {
+        // blockDim.x = 32 ceil(L / 32): warp w's ballots are word w of the planes
+        const uint32_t bits = threadIdx.x < L ? base_bits(col, threadIdx.x) : 0u;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t b = __ballot_sync(0xffffffffu, (bits >> j) & 1u);
+            if (lane == 0) planes[j * nwords + wid] = b;
         }
-        planes[i] = m;
+        if (threadIdx.x < 8) planes[(threadIdx.x >> 1) * nwords + nw + (threadIdx.x & 1)] = 0u;
     }
     const int per = 4 * maxlen;
     for (int i = threadIdx.x; i < K * per; i += blockDim.x) {
@@ -322,32 +325,39 @@ __global__ void k_scan_both_sparse(const float* __restrict__ data, const float* 
     __syncthreads();
     const int l = threadIdx.x;
     const int wi = l >> 5, sh = l & 31;
+    constexpr int MB = 8 * (int)sizeof(MT);
     for (int k = 0; k < K; ++k) {
         const int w = lens[k];
         VI bf{-INFINITY, 0x7fffffff}, bc{-INFINITY, 0x7fffffff};
         if (l <= L - w) {
-            const uint64_t keep = w >= 64 ? ~0ull : ((1ull << w) - 1);
-            uint64_t mj[4];
+            const MT keep = w >= MB ? ~(MT)0 : (((MT)1 << w) - 1);
+            MT mj[4];
             int cnt = 0;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const uint32_t* pl = planes + j * nwords + wi;
-                const uint64_t lo = ((uint64_t)pl[1] << 32) | pl[0];
-                uint64_t m = lo >> sh;
-                if (sh) m |= (uint64_t)pl[2] << (64 - sh);
+                MT m;
+                if (MB == 32) {
+                    m = (MT)__funnelshift_r(pl[0], pl[1], sh);
+                } else {
+                    const uint64_t lo = ((uint64_t)pl[1] << 32) | pl[0];
+                    uint64_t m64 = lo >> sh;
+                    if (sh) m64 |= (uint64_t)pl[2] << (64 - sh);
+                    m = (MT)m64;
+                }
                 mj[j] = m & keep;
-                cnt += __popcll(mj[j]);
+                cnt += MB == 32 ? __popc((uint32_t)mj[j]) : __popcll((unsigned long long)mj[j]);
             }
             const float2* p = pw + (size_t)k * per;
             float sf = 0.f, sc = 0.f;
             int j = 0;
-            uint64_t m = mj[0];
+            MT m = mj[0];
             for (int t = 0; t < cnt; ++t) {
                 while (m == 0) {
                     ++j;
                     m = j == 1 ? mj[1] : (j == 2 ? mj[2] : mj[3]);
                 }
-                const int kk = __ffsll((long long)m) - 1;
+                const int kk = (MB == 32 ? __ffs((int)(uint32_t)m) : __ffsll((long long)m)) - 1;
                 m &= m - 1;
                 const float2 q = p[j * maxlen + kk];
                 sf = __fadd_rn(sf, q.x);
@@ -518,12 +528,12 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
     const size_t shp = (size_t)K * 4 * maxlen * sizeof(float2) + (size_t)K * (nts / 32) * 2 * sizeof(VI) +
                        (size_t)4 * ((L + 31) / 32 + 2) * sizeof(uint32_t);
     if (nts <= 1024 && maxlen <= 64 && shp <= 64 * 1024 && sparse_ok(c, pwms, lens, K, maxlen)) {
+        auto kern = maxlen <= 32 ? k_scan_both_sparse<uint32_t> : k_scan_both_sparse<uint64_t>;
         if (shp > 48 * 1024)
-            CU_TRY(c, cudaFuncSetAttribute(k_scan_both_sparse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           64 * 1024));
-        k_scan_both_sparse<<<N, nts, shp, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
-                                                        c->scan_f + (size_t)K * 4 * maxlen, K, maxlen, L,
-                                                        dpos, dscore, c->scan_u);
+            CU_TRY(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        kern<<<N, nts, shp, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                         c->scan_f + (size_t)K * 4 * maxlen, K, maxlen, L,
+                                         dpos, dscore, c->scan_u);
         LAUNCH_CHECK(c, "k_scan_both_sparse");
     } else if (nts <= 1024 && shs <= 64 * 1024) {
         if (shs > 48 * 1024)

@@ -70,8 +70,10 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     float2* G1s = reinterpret_cast<float2*>(sm4);          // [M][32]
     float2* G3s = G1s + (size_t)M * kBins;                 // [M][32]
     float2* Dgs = G3s + (size_t)M * kBins;                 // [M][32]
-    float* pB = reinterpret_cast<float*>(Dgs + (size_t)M * kBins);   // [kWarps][32]
-    float4* pQT = reinterpret_cast<float4*>(pB + kWarps * kBins);    // [kWarps][32]: Q, T
+    // the warps' partial sums of B, Q.x, Q.y, T.x, T.y per bin, [5][kWarps][32], and
+    // their totals, [5][32]: each total is summed once, by one thread, in warp order
+    float* pp = reinterpret_cast<float*>(Dgs + (size_t)M * kBins);
+    float* tot = pp + 5 * kWarps * kBins;
     for (int i = threadIdx.x; i < M * kBins; i += blockDim.x) {
         const int m = i / kBins, ff = blockIdx.x * kBins + i % kBins;
         const bool in = ff < F;
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     __syncthreads();
     const int fl = on ? f : 0;                             // lanes past F load bin 0
     // staging: [2][kArr][MW][threads], each thread's own slots
-    float2* stg = reinterpret_cast<float2*>(pQT + kWarps * kBins);
+    float2* stg = reinterpret_cast<float2*>(tot + 5 * kBins);
     const int nt = blockDim.x, tid = threadIdx.x;
     auto stage = [&](int n, int buf) {
         const size_t base = (size_t)n * M * F + fl;
@@ -159,19 +161,25 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             Q = cfma2(y, h, Q);
             T = cfma2(y, d, T);
         }
-        pB[w * kBins + lane] = B;
-        pQT[w * kBins + lane] = make_float4(Q.x, Q.y, T.x, T.y);
+        pp[(0 * kWarps + w) * kBins + lane] = B;
+        pp[(1 * kWarps + w) * kBins + lane] = Q.x;
+        pp[(2 * kWarps + w) * kBins + lane] = Q.y;
+        pp[(3 * kWarps + w) * kBins + lane] = T.x;
+        pp[(4 * kWarps + w) * kBins + lane] = T.y;
         __syncthreads();
-        B = 0.f;
-        Q = T = make_float2(0.f, 0.f);
+        if (w < 5) {
+            // warp w sums component w over the warps for its lane's bin, warp 0 first
+            // (the order every thread summed all of them in before: the same bits)
+            const float* src = pp + w * kWarps * kBins + lane;
+            float acc = 0.f;
 #pragma unroll
-        for (int v = 0; v < kWarps; ++v) {
-            B += pB[v * kBins + lane];
-            const float4 qt = pQT[v * kBins + lane];
-            Q = cadd2(Q, make_float2(qt.x, qt.y));
-            T = cadd2(T, make_float2(qt.z, qt.w));
+            for (int v = 0; v < kWarps; ++v) acc += src[v * kBins];
+            tot[w * kBins + lane] = acc;
         }
-        __syncthreads();                                   // partials read before reuse
+        __syncthreads();                                   // totals written; partials read
+        B = tot[lane];
+        Q = make_float2(tot[kBins + lane], tot[2 * kBins + lane]);
+        T = make_float2(tot[3 * kBins + lane], tot[4 * kBins + lane]);
         if (on) {
             const float inv = 1.f / (B + A.kd);
             const float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
@@ -336,7 +344,8 @@ int dspec_launch(cdlgb_ctx* c, const float2* Yh, const float2* G3h, int c0, int 
     a.N = c->N; a.M = c->M; a.F = c->F; a.c0 = c0; a.c1 = c1; a.slot0 = slot0;
     a.kd = c->p.sherman_const_cdl; a.scale = 1.f / (float)c->Lg;
     const dim3 g((unsigned)((c->F + kBins - 1) / kBins), (unsigned)dspec_nsub(c1 - c0, c->F, c->nsm));
-    const size_t sm = (size_t)3 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * (4 + 8 + 8);
+    const size_t sm = (size_t)3 * c->M * kBins * sizeof(float2) + (size_t)kWarps * kBins * 5 * sizeof(float) +
+                      (size_t)5 * kBins * sizeof(float);
     if (c->M <= 4 * kWarps) {
         // + the two staging buffers: 2 x 3 spectra x 4 filters x 512 threads
         const size_t smp = sm + (size_t)2 * kArr * 4 * kBins * kWarps * sizeof(float2);

@@ -401,6 +401,111 @@ __global__ void k_scan_both_sparse(const float* __restrict__ data, const float* 
     }
 }
 
+// k_scan_both_sparse for PWMs of at most 16 columns: the four bases' 16-bit window masks
+// are packed into two words, lo = A | C << 16 and hi = G | T << 16, so that ascending bit
+// order is the nucleotide-major order and bit b is the coefficient pair at row b of the
+// staged table (rows of 16 columns per base): no per-base bookkeeping beyond one switch
+// from lo to hi per window.
+__global__ void k_scan_both_sparse16(const float* __restrict__ data, const float* __restrict__ pwms,
+                                     const int32_t* __restrict__ lens, const float* __restrict__ thresh,
+                                     int K, int maxlen, int L, int32_t* __restrict__ pos,
+                                     float* __restrict__ score, uint8_t* __restrict__ comp) {
+    extern __shared__ float4 sm4q[];
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nwords = (L + 31) / 32 + 2;
+    float2* pw = reinterpret_cast<float2*>(sm4q);                   // [K][4][16]
+    VI* wb = reinterpret_cast<VI*>(pw + (size_t)K * 64);             // [K][nw][2]
+    uint32_t* planes = reinterpret_cast<uint32_t*>(wb + (size_t)K * nw * 2);   // [4][nwords]
+    const int n = blockIdx.x;
+    const float* col = data + (size_t)n * 4 * L;
+    {
+        const uint32_t bits = threadIdx.x < L ? base_bits(col, threadIdx.x) : 0u;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t b = __ballot_sync(0xffffffffu, (bits >> j) & 1u);
+            if (lane == 0) planes[j * nwords + wid] = b;
+        }
+        if (threadIdx.x < 8) planes[(threadIdx.x >> 1) * nwords + nw + (threadIdx.x & 1)] = 0u;
+    }
+    for (int i = threadIdx.x; i < K * 64; i += blockDim.x) {
+        const int k = i >> 6, j = (i >> 4) & 3, kk = i & 15;
+        const int w = lens[k];
+        float f = 0.f, cc = 0.f;
+        if (kk < w) {
+            f = pwms[k + K * (j + 4 * kk)];
+            cc = pwms[k + K * ((3 - j) + 4 * (w - 1 - kk))];
+        }
+        pw[i] = make_float2(f, cc);
+    }
+    __syncthreads();
+    const int l = threadIdx.x;
+    const int wi = l >> 5, sh = l & 31;
+    uint32_t win[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t* pl = planes + j * nwords + wi;
+        win[j] = __funnelshift_r(pl[0], pl[1], sh);     // positions l .. l + 31 of base j
+    }
+    for (int k = 0; k < K; ++k) {
+        const int w = lens[k];
+        VI bf{-INFINITY, 0x7fffffff}, bc{-INFINITY, 0x7fffffff};
+        if (l <= L - w) {
+            const uint32_t keep = (1u << w) - 1u;         // w <= 16
+            uint32_t lo = (win[0] & keep) | ((win[1] & keep) << 16);
+            uint32_t hi = (win[2] & keep) | ((win[3] & keep) << 16);
+            const int cnt = __popc(lo) + __popc(hi);
+            const float2* p = pw + (size_t)k * 64;
+            float sf = 0.f, sc = 0.f;
+            for (int t = 0; t < cnt; ++t) {
+                if (lo == 0) {
+                    lo = hi;
+                    hi = 0;
+                    p += 32;
+                }
+                const int b = __ffs((int)lo) - 1;
+                lo &= lo - 1;
+                const float2 q = p[b];
+                sf = __fadd_rn(sf, q.x);
+                sc = __fadd_rn(sc, q.y);
+            }
+            bf = VI{sf, l};
+            bc = VI{sc, l};
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            VI y;
+            y.v = __shfl_xor_sync(0xffffffffu, bf.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, bf.i, o);
+            bf = vi_best(bf, y);
+            y.v = __shfl_xor_sync(0xffffffffu, bc.v, o);
+            y.i = __shfl_xor_sync(0xffffffffu, bc.i, o);
+            bc = vi_best(bc, y);
+        }
+        if (lane == 0) {
+            wb[((size_t)k * nw + wid) * 2] = bf;
+            wb[((size_t)k * nw + wid) * 2 + 1] = bc;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        VI rf{-INFINITY, 0x7fffffff}, rc{-INFINITY, 0x7fffffff};
+        for (int v = 0; v < nw; ++v) {
+            rf = vi_best(rf, wb[((size_t)k * nw + v) * 2]);
+            rc = vi_best(rc, wb[((size_t)k * nw + v) * 2 + 1]);
+        }
+        const float sF = rf.i == 0x7fffffff ? -INFINITY : rf.v;
+        const float sC = rc.i == 0x7fffffff ? -INFINITY : rc.v;
+        const int iF = rf.i == 0x7fffffff ? -1 : rf.i + 1;
+        const int iC = rc.i == 0x7fffffff ? -1 : rc.i + 1;
+        const bool fwd = sF >= sC;
+        const float sv = fwd ? sF : sC;
+        const bool keepk = sv > thresh[k];
+        const size_t o = k + (size_t)K * n;
+        if (pos) pos[o] = keepk ? (fwd ? iF : iC) : 0;
+        if (score) score[o] = keepk ? sv : 0.f;
+        if (comp) comp[o] = (keepk && !fwd) ? 1 : 0;
+    }
+}
+
 // the sparse scans apply: exact 0/1 data, finite PWM entries (within each motif's
 // length), not turned off by CDLGB_SCAN_DENSE
 bool sparse_ok(const cdlgb_ctx* c, const float* pwms, const int32_t* lens, int K, int maxlen) {
@@ -527,7 +632,17 @@ int scan_both(cdlgb_ctx* c, const float* pwms, const int32_t* lens, const float*
                        (size_t)4 * L * sizeof(float);
     const size_t shp = (size_t)K * 4 * maxlen * sizeof(float2) + (size_t)K * (nts / 32) * 2 * sizeof(VI) +
                        (size_t)4 * ((L + 31) / 32 + 2) * sizeof(uint32_t);
-    if (nts <= 1024 && maxlen <= 64 && shp <= 64 * 1024 && sparse_ok(c, pwms, lens, K, maxlen)) {
+    const size_t shq = (size_t)K * 64 * sizeof(float2) + (size_t)K * (nts / 32) * 2 * sizeof(VI) +
+                       (size_t)4 * ((L + 31) / 32 + 2) * sizeof(uint32_t);
+    if (nts <= 1024 && maxlen <= 16 && shq <= 64 * 1024 && sparse_ok(c, pwms, lens, K, maxlen)) {
+        if (shq > 48 * 1024)
+            CU_TRY(c, cudaFuncSetAttribute(k_scan_both_sparse16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           64 * 1024));
+        k_scan_both_sparse16<<<N, nts, shq, c->stream>>>(scan_data(c), c->scan_f, c->scan_i,
+                                                          c->scan_f + (size_t)K * 4 * maxlen, K, maxlen, L,
+                                                          dpos, dscore, c->scan_u);
+        LAUNCH_CHECK(c, "k_scan_both_sparse16");
+    } else if (nts <= 1024 && maxlen <= 64 && shp <= 64 * 1024 && sparse_ok(c, pwms, lens, K, maxlen)) {
         auto kern = maxlen <= 32 ? k_scan_both_sparse<uint32_t> : k_scan_both_sparse<uint64_t>;
         if (shp > 48 * 1024)
             CU_TRY(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));

@@ -221,3 +221,19 @@ def test_scan_zero_columns(pkg, built_lib):
         np.testing.assert_array_equal(pos.T, rp)
         np.testing.assert_array_equal(score.T, rs)
         np.testing.assert_array_equal(comp.T, rc)
+
+
+@pytest.mark.parametrize("lo,hi", [(1, 17), (9, 17), (12, 33), (30, 40)])
+def test_sparse_scan_width_classes(pkg, built_lib, lo, hi):
+    """Every sparse two-strand kernel -- packed 16-bit masks (PWMs of at most 16
+    columns), 32-bit and 64-bit masks -- against the oracle, bit for bit."""
+    rng = np.random.default_rng(lo * 100 + hi)
+    N, L = 50, 150
+    S, _ = random_onehot(rng, N, L)
+    pwms, lens, thresh = _random_pwms(rng, 9, lo, hi)
+    with _ctx(pkg, S) as c:
+        pos, score, comp = pkg.overlapping_scan(c, pwms, thresh)
+        rp, rs, rc = SO.overlapping_scan(S, pwms, lens, thresh)
+        np.testing.assert_array_equal(pos.T, rp)
+        np.testing.assert_array_equal(score.T, rs)
+        np.testing.assert_array_equal(comp.T, rc)

@@ -501,7 +501,7 @@ double host_uniform(uint64_t seed, uint64_t i) {
     return ((double)(h >> 11) + 0.5) * (1.0 / 9007199254740992.0);
 }
 
-struct PlanEntry { int dir; long long batch; cufftHandle h; };
+struct PlanEntry { int dir; long long batch; cufftHandle h; void* work; };
 typedef std::vector<PlanEntry> PlanCache;
 
 // R2C (dir 0) or C2R (dir 1) plan of length Lg over `batch` contiguous columns
@@ -514,12 +514,24 @@ int get_plan(cdlgb_ctx* c, int dir, long long batch, cufftHandle* out) {
     size_t ws = 0;
     cufftHandle h;
     FFT_TRY(c, cufftCreate(&h));
+    // the work area comes from the context's stream-ordered allocations, not from cuFFT
+    FFT_TRY(c, cufftSetAutoAllocation(h, 0));
     if (dir == 0)
         FFT_TRY(c, cufftMakePlanMany64(h, 1, n, in_r, 1, c->Lg, in_c, 1, c->F, CUFFT_R2C, batch, &ws));
     else
         FFT_TRY(c, cufftMakePlanMany64(h, 1, n, in_c, 1, c->F, in_r, 1, c->Lg, CUFFT_C2R, batch, &ws));
-    FFT_TRY(c, cufftSetStream(h, c->stream));
-    pc.push_back({dir, batch, h});
+    void* work = nullptr;
+    int st = dev_alloc(c, &work, ws);
+    if (st != CDLGB_OK) { cufftDestroy(h); return st; }
+    cufftResult r = work ? cufftSetWorkArea(h, work) : CUFFT_SUCCESS;
+    if (r == CUFFT_SUCCESS) r = cufftSetStream(h, c->stream);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(h);
+        dev_free(c, work);
+        return cdlgb_seterr(c, CDLGB_ECUDA, "cuFFT plan of %lld rows: work area / stream, status %d",
+                            batch, (int)r);
+    }
+    pc.push_back({dir, batch, h, work});
     *out = h;
     return CDLGB_OK;
 }
@@ -532,7 +544,10 @@ int set_plan_streams(cdlgb_ctx* c) {
 
 void free_plans(cdlgb_ctx* c) {
     if (!c->plans) return;
-    for (auto& e : *(PlanCache*)c->plans) cufftDestroy(e.h);
+    for (auto& e : *(PlanCache*)c->plans) {
+        cufftDestroy(e.h);
+        dev_free(c, e.work);
+    }
     delete (PlanCache*)c->plans;
     c->plans = nullptr;
 }
@@ -625,10 +640,7 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
 
 int admm_alloc(cdlgb_ctx* c) {
     const size_t LMN = c->LMN, LN = c->LN, LM = c->LM;
-    auto A = [&](void** p, size_t bytes) -> int {
-        CU_TRY(c, cudaMalloc(p, bytes));
-        return CDLGB_OK;
-    };
+    auto A = [&](void** p, size_t bytes) -> int { return dev_alloc(c, p, bytes); };
     ST_TRY(A((void**)&c->Xb[0], LMN * 4));
     ST_TRY(A((void**)&c->Xb[1], LMN * 4));
     ST_TRY(A((void**)&c->y2, LMN * 4));
@@ -689,7 +701,12 @@ int admm_alloc(cdlgb_ctx* c) {
     c->nred = 152 * 4;
     ST_TRY(A((void**)&c->dred, (size_t)c->nred * 4 * sizeof(double)));
     ST_TRY(A((void**)&c->dscalar, 8 * sizeof(double)));
-    CU_TRY(c, cudaMallocHost((void**)&c->hscalar, 8 * sizeof(double)));
+    c->hscalar = host_scalars_get();
+    c->hscalar_own = false;
+    if (!c->hscalar) {
+        CU_TRY(c, cudaMallocHost((void**)&c->hscalar, 8 * sizeof(double)));
+        c->hscalar_own = true;
+    }
     ST_TRY(A((void**)&c->dres, RESIDUAL_COUNT * sizeof(double)));
     ST_TRY(A((void**)&c->rpart, resid_part_doubles(c->N, c->F, c->dslots) * sizeof(double)));
     ST_TRY(A((void**)&c->Gprev, 2 * LM * 4));
@@ -700,16 +717,21 @@ void admm_free(cdlgb_ctx* c) {
     float** fl[] = {&c->Xb[0], &c->Xb[1], &c->y2, &c->y3, &c->d, &c->g1, &c->g3, &c->Y1,
                     &c->y1, &c->DX, &c->Td, &c->G2, &c->g2, &c->sU, &c->G1, &c->G3,
                     &c->dsum, &c->Dbest, &c->vbar, &c->Ah, &c->sA, &c->sB, &c->part};
-    for (auto p : fl) { if (*p) cudaFree(*p); *p = nullptr; }
+    for (auto p : fl) { dev_free(c, *p); *p = nullptr; }
     float2** cl[] = {&c->G1h, &c->sUh, &c->sVh, &c->sAh, &c->sBh, &c->sCh, &c->Dhs,
                      &c->g1h, &c->Dg, &c->G3h, &c->spart, &c->sumspec};
-    for (auto p : cl) { if (*p) cudaFree(*p); *p = nullptr; }
-    if (c->dred) cudaFree(c->dred);
-    if (c->dscalar) cudaFree(c->dscalar);
-    if (c->hscalar) cudaFreeHost(c->hscalar);
-    if (c->dres) cudaFree(c->dres);
-    if (c->rpart) cudaFree(c->rpart);
-    if (c->Gprev) cudaFree(c->Gprev);
+    for (auto p : cl) { dev_free(c, *p); *p = nullptr; }
+    dev_free(c, c->dred);
+    dev_free(c, c->dscalar);
+    if (c->hscalar) {
+        // the slot may still be the target of a copy in flight on the stream
+        cudaStreamSynchronize(c->stream);
+        if (c->hscalar_own) cudaFreeHost(c->hscalar);
+        else host_scalars_put(c->hscalar);
+    }
+    dev_free(c, c->dres);
+    dev_free(c, c->rpart);
+    dev_free(c, c->Gprev);
     c->dred = nullptr; c->dscalar = nullptr; c->hscalar = nullptr;
     c->dres = nullptr; c->rpart = nullptr; c->Gprev = nullptr;
     free_plans(c);

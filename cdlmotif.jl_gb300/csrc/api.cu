@@ -254,8 +254,8 @@ int cdlgb_destroy(cdlgb_ctx* c) {
     admm_free(c);
     fused_free(c);
     scan_free(c);
-    if (c->S) cudaFree(c->S);
-    if (c->S_bg) cudaFree(c->S_bg);
+    dev_free(c, c->S);
+    dev_free(c, c->S_bg);
     Ring* r = (Ring*)c->ring;
     if (r) {
         for (int i = 0; i < 2 * kRing; ++i) cudaEventDestroy(r->ev[i]);
@@ -301,11 +301,10 @@ static int upload_data(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, 
         return check_onehot(c);
     }
     uint8_t* d = nullptr;
-    CU_TRY(c, cudaMallocAsync((void**)&d, n / 4, c->stream));
-    CU_TRY(c, cudaMemcpyAsync(d, codes, n / 4, cudaMemcpyHostToDevice, c->stream));
+    CU_TRY(c, dev_copy_in(c, (void**)&d, codes, n / 4));
     k_encode_onehot<<<grid_for(n / 4, 256), 256, 0, c->stream>>>(d, (float4*)c->S, n / 4);
     cudaError_t e = cudaGetLastError();
-    cudaFreeAsync(d, c->stream);
+    dev_free(c, d);
     if (e != cudaSuccess) return cdlgb_seterr(c, CDLGB_ECUDA, "k_encode_onehot: %s", cudaGetErrorString(e));
     CU_TRY(c, cudaStreamSynchronize(c->stream));
     c->onehot_exact = true;      // 0/1 by construction
@@ -334,8 +333,8 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
         CU_TRY(c, cudaStreamSynchronize(c->stream));
         admm_free(c);
         fused_free(c);
-        if (c->S) cudaFree(c->S);
-        if (c->S_bg) cudaFree(c->S_bg);
+        dev_free(c, c->S);
+        dev_free(c, c->S_bg);
         c->S = c->S_bg = nullptr;
         c->bg_valid = c->use_bg = 0;
         c->loaded = c->initialized = false;
@@ -358,6 +357,7 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
     size_t need = admm_footprint(&p, L4, N, c->fused);
     size_t freeb = 0, total = 0;
     CU_TRY(c, cudaMemGetInfo(&freeb, &total));
+    freeb += devmem_reusable(c->dev);      // held by the library's pool, free for reuse
     size_t budget = p.hbm_budget_bytes ? (size_t)p.hbm_budget_bytes
                                        : (freeb > (1ull << 30) ? freeb - (1ull << 30) : 0);
     if (need > budget)
@@ -365,7 +365,7 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
                             "dataset needs %.2f GB of device memory, budget is %.2f GB (N=%d, 4L=%d, M=%d)",
                             need / 1e9, budget / 1e9, N, L4, c->M);
     size_t n = (size_t)L4 * N;
-    CU_TRY(c, cudaMalloc((void**)&c->S, n * 4));
+    ST_TRY(dev_alloc(c, (void**)&c->S, n * 4));
     int st = admm_alloc(c);
     if (st == CDLGB_OK && c->fused) st = fused_setup(c);
     if (st != CDLGB_OK) {
@@ -373,7 +373,7 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
         cudaGetLastError();
         admm_free(c);
         fused_free(c);
-        cudaFree(c->S);
+        dev_free(c, c->S);
         c->S = nullptr;
         return cdlgb_seterr(c, st, "%s", msg.c_str());
     }

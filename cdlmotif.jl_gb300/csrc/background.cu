@@ -178,10 +178,10 @@ int make_background(cdlgb_ctx* c, int k, unsigned long long seed) {
     const int N = c->N, L = c->L4 / 4;
     if (L > 32000) return cdlgb_seterr(c, CDLGB_EINVAL, "make_background: L=%d above 32000", L);
     const size_t n = (size_t)c->L4 * N;
-    if (!c->S_bg) CU_TRY(c, cudaMalloc((void**)&c->S_bg, n * 4));
+    if (!c->S_bg) ST_TRY(dev_alloc(c, (void**)&c->S_bg, n * 4));
     uint8_t* lists = nullptr;
     int32_t* err = nullptr;
-    CU_TRY(c, cudaMallocAsync((void**)&lists, (size_t)N * L + 16, c->stream));
+    ST_TRY(dev_alloc(c, (void**)&lists, (size_t)N * L + 16));
     err = reinterpret_cast<int32_t*>(lists + (((size_t)N * L + 3) & ~(size_t)3));
     CU_TRY(c, cudaMemsetAsync(err, 0, 4, c->stream));
     ShArgs a;
@@ -191,7 +191,7 @@ int make_background(cdlgb_ctx* c, int k, unsigned long long seed) {
     LAUNCH_CHECK(c, "k_klet_shuffle");
     int32_t herr = 0;
     CU_TRY(c, cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, c->stream));
-    CU_TRY(c, cudaFreeAsync(lists, c->stream));
+    dev_free(c, lists);
     CU_TRY(c, cudaStreamSynchronize(c->stream));
     if (herr) {
         c->bg_valid = 0;

@@ -107,6 +107,7 @@ struct cdlgb_ctx {
     int nred = 0;
     double* dscalar = nullptr;                        // device scalars
     double* hscalar = nullptr;                        // pinned host mirror
+    bool hscalar_own = false;                         // from cudaMallocHost, not the slab
     double obj_best = 0.0;
     // residual record (RESIDUAL_COUNT float64), its per-block partials, G1 and G3 of
     // the D-step before their update (2 LM), outer iterations of the last run_outer
@@ -172,6 +173,17 @@ void cdlgb_phase_begin(cdlgb_ctx* c, int ph);
 void cdlgb_phase_end(cdlgb_ctx* c, int ph);
 void cdlgb_phase_end_n(cdlgb_ctx* c, int ph, int units);   // interval covering `units` steps
 
+// ---- devmem.cpp: stream-ordered device memory of a context (its device's pool, its
+// stream) and pinned host scalars ----
+cudaError_t dev_malloc(cdlgb_ctx* c, void** p, size_t bytes);
+cudaError_t dev_copy_in(cdlgb_ctx* c, void** p, const void* host, size_t bytes);   // alloc + copy
+int dev_alloc(cdlgb_ctx* c, void** p, size_t bytes);      // dev_malloc with the error recorded
+void dev_free(cdlgb_ctx* c, void* p);
+size_t devmem_reusable(int dev);          // reserved by the pool and not in use
+int devmem_hold(int dev, int delta);      // > 0 holds: the pool keeps what is freed
+double* host_scalars_get();               // 8 pinned doubles, nullptr when none is left
+void host_scalars_put(double* p);
+
 // ---- admm.cu ----
 int admm_alloc(cdlgb_ctx* c);
 void admm_free(cdlgb_ctx* c);
@@ -194,13 +206,13 @@ size_t fused_scratch_bytes(int Lg, int M, int N);
 
 // ---- xwarp.cu (register-FFT variant of the fused X-step) ----
 void* warp_plan_create(cdlgb_ctx* c, int* status);
-void warp_plan_free(void* p);
+void warp_plan_free(cdlgb_ctx* c, void* p);
 int warp_xstep(cdlgb_ctx* c, void* p, const float* Xin, float* Xout);
 int warp_absx(void* p, const double** part, int* n);
 int warp_variant_exists(int Lg, int M);
 // multi-iteration fused X-step (xiter.cu): all iterations of one code update per launch
 void* iter_plan_create(cdlgb_ctx* c, int* status);
-void iter_plan_free(void* p);
+void iter_plan_free(cdlgb_ctx* c, void* p);
 int iter_xsteps(cdlgb_ctx* c, void* p, const float* Xin, float* Xout, int iters);
 int iter_absx(void* p, const double** part, int* n);
 int iter_plan_cluster(void* p);
@@ -236,7 +248,7 @@ int fused_resid(cdlgb_ctx* c, const double** part, int* n);
 int noalloc_warm_current_device();
 // streaming forward transforms of the D-step (dstream.cu)
 void* dfwd_plan_create(cdlgb_ctx* c, int* status);
-void dfwd_plan_free(void* p);
+void dfwd_plan_free(cdlgb_ctx* c, void* p);
 int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh);
 int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn, float scale);
 void* fused_dfwd(cdlgb_ctx* c);
@@ -246,10 +258,10 @@ int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 template <typename T>
 inline int ensure_scratch(cdlgb_ctx* c, T** p, size_t* cap, size_t n) {
     if (*cap >= n) return CDLGB_OK;
-    if (*p) cudaFree(*p);
+    dev_free(c, *p);
     *p = nullptr;
     *cap = 0;
-    CU_TRY(c, cudaMalloc((void**)p, n * sizeof(T)));
+    ST_TRY(dev_alloc(c, (void**)p, n * sizeof(T)));
     *cap = n;
     return CDLGB_OK;
 }

@@ -238,8 +238,7 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     P->smem = ((size_t)v->P * v->N1 + (size_t)groups * buf) * sizeof(float2);
     std::vector<float2> tw2 = regfft_twiddles(v->N1, v->P);
     cudaError_t e = regfft_upload_tables();
-    if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = dev_copy_in(c, (void**)&P->tw2, tw2.data(), tw2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(P->ki, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     int per_sm = 0, per_sm_inv = 0;
@@ -248,7 +247,7 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     if (e != cudaSuccess || per_sm < 1 || per_sm_inv < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "D-step transform setup failed: %s",
                                e != cudaSuccess ? cudaGetErrorString(e) : "no CTA fits");
-        if (P->tw2) cudaFree(P->tw2);
+        dev_free(c, P->tw2);
         delete P;
         return nullptr;
     }
@@ -260,10 +259,10 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     return P;
 }
 
-void dfwd_plan_free(void* p) {
+void dfwd_plan_free(cdlgb_ctx* c, void* p) {
     FwdPlan* P = (FwdPlan*)p;
     if (!P) return;
-    if (P->tw2) cudaFree(P->tw2);
+    dev_free(c, P->tw2);
     delete P;
 }
 

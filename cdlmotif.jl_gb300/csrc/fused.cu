@@ -20,6 +20,8 @@
 // X written once, plus the per-sequence vectors.
 #include "cdlgb_internal.h"
 
+#include <mutex>
+
 #include <algorithm>
 
 #include <cooperative_groups.h>
@@ -549,6 +551,26 @@ size_t fused_scratch_bytes(int Lg, int M, int N) {
     return (size_t)Lg * 8 + 152 * 8 * 8 * sizeof(double);
 }
 
+// The odd primes' trig table in constant memory, uploaded once per device: every
+// context reads the same values, and a context's setup must not write the table under
+// another context's kernels.
+static cudaError_t upload_trig_once() {
+    static std::mutex mu;
+    static bool done[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31);
+    for (int p : kPrimes)
+        for (int m = 0; m < p; ++m)
+            trig[trig_off(p) + m] = make_float2((float)cos(2.0 * M_PI * m / p), (float)sin(2.0 * M_PI * m / p));
+    e = cudaMemcpyToSymbol(c_trig, trig.data(), trig.size() * sizeof(float2));
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+    return e;
+}
+
 int fused_setup(cdlgb_ctx* c) {
     FusedPlan* P = new FusedPlan();
     c->fplan = P;
@@ -571,16 +593,11 @@ int fused_setup(cdlgb_ctx* c) {
     P->B = (P->Mc + 1) / 2;
     P->smem = smem_bytes(P->Lg, P->F, P->Mc);
     // trig tables of the odd primes, twiddles exp(-2 pi i t / Lg), in double then rounded
-    std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31);
-    for (int p : kPrimes)
-        for (int m = 0; m < p; ++m)
-            trig[trig_off(p) + m] = make_float2((float)cos(2.0 * M_PI * m / p), (float)sin(2.0 * M_PI * m / p));
-    CU_TRY(c, cudaMemcpyToSymbol(c_trig, trig.data(), trig.size() * sizeof(float2)));
+    CU_TRY(c, upload_trig_once());
     std::vector<float2> tw(P->Lg);
     for (int t = 0; t < P->Lg; ++t)
         tw[t] = make_float2((float)cos(2.0 * M_PI * t / P->Lg), (float)-sin(2.0 * M_PI * t / P->Lg));
-    CU_TRY(c, cudaMalloc((void**)&P->tw, P->Lg * sizeof(float2)));
-    CU_TRY(c, cudaMemcpy(P->tw, tw.data(), P->Lg * sizeof(float2), cudaMemcpyHostToDevice));
+    CU_TRY(c, dev_copy_in(c, (void**)&P->tw, tw.data(), P->Lg * sizeof(float2)));
     // the attribute is process-wide per kernel: always the same cap, never a
     // context's own size (contexts with different Lg run concurrently)
     CU_TRY(c, cudaFuncSetAttribute(k_xstep_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -604,18 +621,18 @@ int fused_setup(cdlgb_ctx* c) {
                             P->CS, P->smem);
     if (nclusters > c->N) nclusters = c->N;
     P->grid = nclusters * P->CS;
-    CU_TRY(c, cudaMalloc((void**)&P->absx_part, (size_t)P->grid * sizeof(double)));
+    ST_TRY(dev_alloc(c, (void**)&P->absx_part, (size_t)P->grid * sizeof(double)));
     return CDLGB_OK;
 }
 
 void fused_free(cdlgb_ctx* c) {
     FusedPlan* P = (FusedPlan*)c->fplan;
     if (!P) return;
-    if (P->tw) cudaFree(P->tw);
-    if (P->absx_part) cudaFree(P->absx_part);
-    warp_plan_free(P->warp);
-    iter_plan_free(P->iter);
-    dfwd_plan_free(P->dfwd);
+    dev_free(c, P->tw);
+    dev_free(c, P->absx_part);
+    warp_plan_free(c, P->warp);
+    iter_plan_free(c, P->iter);
+    dfwd_plan_free(c, P->dfwd);
     delete P;
     c->fplan = nullptr;
 }
@@ -681,8 +698,8 @@ int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* c
     auto free_all = [&](int keep) {
         for (int i = 0; i < (int)cands.size(); ++i) {
             if (i == keep) continue;
-            if (cands[i].kind == 1) iter_plan_free(cands[i].plan);
-            else warp_plan_free(cands[i].plan);
+            if (cands[i].kind == 1) iter_plan_free(c, cands[i].plan);
+            else warp_plan_free(c, cands[i].plan);
         }
     };
     int st = CDLGB_OK;
@@ -771,8 +788,8 @@ int fused_autotune(cdlgb_ctx* c, int maxc, double* ms, int32_t* kind, int32_t* c
     if (rc != CDLGB_OK) { free_all(-1); return rc; }
     CU_TRY(c, cudaStreamSynchronize(s));
     // keep the winner
-    iter_plan_free(P->iter);
-    warp_plan_free(P->warp);
+    iter_plan_free(c, P->iter);
+    warp_plan_free(c, P->warp);
     P->iter = nullptr;
     P->warp = nullptr;
     if (cands[best].kind == 1) P->iter = cands[best].plan;

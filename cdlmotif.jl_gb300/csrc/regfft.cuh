@@ -12,6 +12,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -378,8 +379,17 @@ __device__ __forceinline__ void repack_X(float2* __restrict__ bufs, int BUF, int
     }
 }
 
-// Uploads this translation unit's trig tables.
+// Uploads this translation unit's trig tables, once per device: every context reads
+// the same values, and a context's setup must not write them under another context's
+// kernels.
 inline cudaError_t regfft_upload_tables() {
+    static std::mutex mu;
+    static bool done[64];
+    int dev = 0;
+    cudaError_t e0 = cudaGetDevice(&dev);
+    if (e0 != cudaSuccess) return e0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
     std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31);
     for (int p : kPrimesW)
         for (int m = 0; m < p; ++m)
@@ -388,6 +398,7 @@ inline cudaError_t regfft_upload_tables() {
     for (int j = 0; j < 32; ++j) w32[j] = make_float2((float)cos(2.0 * M_PI * j / 32), (float)-sin(2.0 * M_PI * j / 32));
     cudaError_t e = cudaMemcpyToSymbol(c_trigw, trig.data(), trig.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_w32, w32.data(), 32 * sizeof(float2));
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }
 

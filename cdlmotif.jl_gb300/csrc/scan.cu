@@ -941,9 +941,9 @@ int touzet_thresholds(cdlgb_ctx* c, const float* pwms, const int32_t* lens, int 
 }
 
 void scan_free(cdlgb_ctx* c) {
-    if (c->scan_i) cudaFree(c->scan_i);
-    if (c->scan_f) cudaFree(c->scan_f);
-    if (c->scan_u) cudaFree(c->scan_u);
+    dev_free(c, c->scan_i);
+    dev_free(c, c->scan_f);
+    dev_free(c, c->scan_u);
     c->scan_i = nullptr; c->scan_f = nullptr; c->scan_u = nullptr;
     c->scan_i_cap = c->scan_f_cap = c->scan_u_cap = 0;
 }

@@ -193,6 +193,9 @@ int cdlgb_server_create(const cdlgb_params* p, const cdlgb_server_config* cfg, c
         }
         s->budget = (uint64_t)((double)fr * 0.85);
     }
+    // the library's device memory pool keeps what finished datasets free for the next
+    // ones while the server lives
+    devmem_hold(cfg->device, +1);
     s->t0 = clk::now();
     for (int i = 0; i < cfg->slots; ++i) s->workers.emplace_back(worker, s);
     *out = s;
@@ -353,6 +356,7 @@ int cdlgb_server_destroy(cdlgb_server* s) {
         s->cv.notify_all();
     }
     for (auto& t : s->workers) t.join();
+    devmem_hold(s->cfg.device, -1);
     delete s;
     return CDLGB_OK;
 }

@@ -497,8 +497,7 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
     if (!P) return nullptr;
     std::vector<float2> tw2 = regfft_twiddles(v->N1, v->P);
     cudaError_t e = regfft_upload_tables();
-    if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = dev_copy_in(c, (void**)&P->tw2, tw2.data(), tw2.size() * sizeof(float2));
     // process-wide per kernel: the same cap for every context
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -524,26 +523,27 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
     if (e == cudaSuccess && nclusters >= 1) {
         if (nclusters > c->N) nclusters = c->N;
         P->grid = nclusters * P->CS;
-        e = cudaMalloc((void**)&P->absx_part, (size_t)P->grid * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc((void**)&P->res_part, (size_t)P->grid * 5 * sizeof(double));
+        e = dev_malloc(c, (void**)&P->absx_part, (size_t)P->grid * sizeof(double));
+        if (e == cudaSuccess) e = dev_malloc(c, (void**)&P->res_part, (size_t)P->grid * 5 * sizeof(double));
     }
     if (e != cudaSuccess || nclusters < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "multi-iteration X-step setup failed: %s",
                                e != cudaSuccess ? cudaGetErrorString(e) : "no cluster fits");
-        if (P->tw2) cudaFree(P->tw2);
-        if (P->absx_part) cudaFree(P->absx_part);
+        dev_free(c, P->tw2);
+        dev_free(c, P->absx_part);
+        dev_free(c, P->res_part);
         delete P;
         return nullptr;
     }
     return P;
 }
 
-void iter_plan_free(void* p) {
+void iter_plan_free(cdlgb_ctx* c, void* p) {
     IterPlan* P = (IterPlan*)p;
     if (!P) return;
-    if (P->tw2) cudaFree(P->tw2);
-    if (P->absx_part) cudaFree(P->absx_part);
-    if (P->res_part) cudaFree(P->res_part);
+    dev_free(c, P->tw2);
+    dev_free(c, P->absx_part);
+    dev_free(c, P->res_part);
     delete P;
 }
 

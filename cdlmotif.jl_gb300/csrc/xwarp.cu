@@ -375,8 +375,7 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
     const int N1 = v->N1, Pp = v->P;
     std::vector<float2> tw2 = regfft_twiddles(N1, Pp);
     cudaError_t e = regfft_upload_tables();
-    if (e == cudaSuccess) e = cudaMalloc((void**)&P->tw2, tw2.size() * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMemcpy(P->tw2, tw2.data(), tw2.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = dev_copy_in(c, (void**)&P->tw2, tw2.data(), tw2.size() * sizeof(float2));
     // process-wide per kernel: the same cap for every context
     if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, 110 * 1024);
     int nclusters = 0;
@@ -397,27 +396,27 @@ void* warp_plan_create(cdlgb_ctx* c, int* status) {
     if (e != cudaSuccess || nclusters < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "register-FFT X-step setup failed: %s",
                                e != cudaSuccess ? cudaGetErrorString(e) : "no cluster fits");
-        if (P->tw2) cudaFree(P->tw2);
+        dev_free(c, P->tw2);
         delete P;
         return nullptr;
     }
     if (nclusters > c->N) nclusters = c->N;
     P->grid = nclusters * P->CS;
-    e = cudaMalloc((void**)&P->absx_part, (size_t)P->grid * sizeof(double));
+    e = dev_malloc(c, (void**)&P->absx_part, (size_t)P->grid * sizeof(double));
     if (e != cudaSuccess) {
-        *status = cdlgb_seterr(c, CDLGB_ECUDA, "cudaMalloc: %s", cudaGetErrorString(e));
-        cudaFree(P->tw2);
+        *status = cdlgb_seterr(c, CDLGB_ECUDA, "device allocation: %s", cudaGetErrorString(e));
+        dev_free(c, P->tw2);
         delete P;
         return nullptr;
     }
     return P;
 }
 
-void warp_plan_free(void* p) {
+void warp_plan_free(cdlgb_ctx* c, void* p) {
     WarpPlan* P = (WarpPlan*)p;
     if (!P) return;
-    if (P->tw2) cudaFree(P->tw2);
-    if (P->absx_part) cudaFree(P->absx_part);
+    dev_free(c, P->tw2);
+    dev_free(c, P->absx_part);
     delete P;
 }
 

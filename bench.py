@@ -8,9 +8,11 @@ iteration of cdl_optimize (src/WRAPPER/wrap.jl:6-11): 15 X-steps, update_best!,
 1 D-step.
 
   value  device-resident: state and data already in HBM.
-  e2e    through the public C ABI with host buffers: every step uploads the one-hot
-         data from pinned host memory (cdlgb_load_data), initialises the state
-         (cdlgb_init_state), runs E outer iterations (cdlgb_run_outer) and reads the
+  e2e    through the public C ABI with host buffers: every step is one training of
+         cdl_optimize (src/WRAPPER/wrap.jl:1-32): it uploads the one-hot data from
+         pinned host memory (cdlgb_load_data), initialises the state
+         (cdlgb_init_state), runs E = iter_num = 10 outer iterations (the reference's
+         default, src/SETUP/WRAPPER_setup.jl:10; cdlgb_run_outer) and reads the
          objectives and D_best back; the unit is the same (outer iterations/s).
 
 ``--impl reference`` times the CPU restatement of the reference (oracle/cdl_cpu.cpp:
@@ -250,7 +252,7 @@ def run_gpu(args, rank: int, world: int):
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e_steps = max(2, args.steps // 2)
+    e_steps = max(2, args.steps // 5)      # one training (E outer iterations) each
     for _ in range(e_steps):
         c.load_data(S_pin)                   # H2D of the step's inputs
         c.init_state(seed=wl["seed"])
@@ -470,6 +472,72 @@ def run_batched(args):
                        "L": [int(d.shape[1] // 4) for d in data]}}
 
 
+def run_interference(args, n_small: int = 5):
+    """What one dataset's life (cdlgb_create, load, init, 3 outer iterations, code
+    threshold, destroy) costs a training that runs beside it in the same process: an
+    N = 20000 training (L = 200, K = 32, W = 16) loops outer iterations on one host
+    thread while N = 1000 datasets (same L, K, W) are trained one after another on
+    another.  Reported: the big training's ms per outer iteration alone and during,
+    the GPU time it loses per small dataset (the outer iterations it would have done
+    alone in that wall time, minus those it did, times its ms per iteration), and the
+    small datasets' median call times alone and beside it.  A loss near the small
+    dataset's own kernel time means its set-up and teardown stalled nothing."""
+    import threading
+    pkg = _pkg()
+    setup = pkg.CDLSetup(M=32, filter_size=16, lambda_=0.1, rho=1.0, sigma=100.0)
+    big = pkg.synth.onehot(pkg.synth.plant_dataset(71, 20000, 200, [10, 14], [0.3, 0.3])[0])
+    small = pkg.synth.onehot(pkg.synth.plant_dataset(72, 1000, 200, [10, 14], [0.3, 0.3])[0])
+
+    def one():
+        t = {}
+        t0 = time.perf_counter()
+        c = pkg.CDL(setup)
+        t["create"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); c.load_data(small); t["load"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); c.init_state(seed=3); t["init"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); pkg.run_outer(c, 3); t["outer3"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); pkg.code_threshold(c); t["threshold"] = time.perf_counter() - t0
+        t0 = time.perf_counter(); c.close(); t["destroy"] = time.perf_counter() - t0
+        return t
+
+    def med(ts):
+        return {k: 1e3 * float(np.median([t[k] for t in ts])) for k in ts[0]}
+
+    one()                                             # warm-up (modules, tables)
+    alone = med([one() for _ in range(n_small)])
+    stop = threading.Event()
+    done = [0]
+
+    def background():
+        with pkg.init_cdl(setup, big) as c:
+            while not stop.is_set():
+                pkg.run_outer(c, 1)
+                done[0] += 1
+
+    th = threading.Thread(target=background)
+    th.start()
+    try:
+        time.sleep(3.0)
+        d0, t0 = done[0], time.perf_counter()
+        time.sleep(2.0)
+        big_alone_ms = 1e3 * (time.perf_counter() - t0) / max(1, done[0] - d0)
+        d0, t0 = done[0], time.perf_counter()
+        beside = [one() for _ in range(n_small)]
+        el = time.perf_counter() - t0
+        got = done[0] - d0
+    finally:
+        stop.set()
+        th.join()
+    lost = (1e3 * el / big_alone_ms - got) * big_alone_ms / n_small
+    return {"metric": "GPU time a running N=20000 training loses per N=1000 dataset trained beside it",
+            "value": lost, "unit": "ms", "higher_is_better": False,
+            "big_ms_per_outer_alone": big_alone_ms, "big_ms_per_outer_beside": 1e3 * el / max(1, got),
+            "small_calls_ms_alone": alone, "small_calls_ms_beside": med(beside),
+            "small_datasets": n_small, "dtype": "f32", "data": "synthetic (seeded planted motifs)",
+            "config": {"workload": "interference", "big": {"N": 20000, "L": 200, "K": 32},
+                       "small": {"N": 1000, "L": 200, "K": 32, "outer_iterations": 3}}}
+
+
 def search_inputs(wl=WORKLOAD, K=32, N=None):
     """The search-stage inputs on the bench dataset: the planted motifs' cores (two
     columns trimmed per side, so that extend! has columns to find) and random
@@ -675,7 +743,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference", "refstruct"])
     ap.add_argument("--fft-mode", type=int, default=0, help="0 auto, 1 cuFFT, 2 fused")
-    ap.add_argument("--e2e-outer", type=int, default=3)
+    ap.add_argument("--e2e-outer", type=int, default=10,
+                    help="outer iterations per end-to-end step (one training: iter_num)")
     ap.add_argument("--cpu-sample", type=int, default=1000,
                     help="sequences of the CPU baseline leg (one outer iteration)")
     ap.add_argument("--ref-sample", type=int, default=2000,
@@ -693,6 +762,8 @@ def main():
     ap.add_argument("--batched", action="store_true",
                     help="64-dataset mix: plain (one at a time) vs batched (served) datasets/hr")
     ap.add_argument("--batched-n", type=int, default=64)
+    ap.add_argument("--interference", action="store_true",
+                    help="GPU time a running training loses per dataset trained beside it")
     ap.add_argument("--precision", action="store_true",
                     help="precision study: float32 GPU path vs an all-FP64 GPU reference")
     ap.add_argument("--precision-reference-defaults", action="store_true",
@@ -733,6 +804,10 @@ def main():
     if args.batched:
         if rank == 0:
             print(json.dumps(run_batched(args)))
+        return
+    if args.interference:
+        if rank == 0:
+            print(json.dumps(run_interference(args)))
         return
 
     if args.impl == "reference":

@@ -552,14 +552,27 @@ void free_plans(cdlgb_ctx* c) {
     c->plans = nullptr;
 }
 
-int r2c(cdlgb_ctx* c, long long batch, float* in, float2* out) {
+// the register-FFT row kernels where the context's length has them (the streaming
+// transforms' plan), else cuFFT
+static void* row_plan(cdlgb_ctx* c) {
+    return c->fused && !c->rows_cufft ? fused_dfwd(c) : nullptr;
+}
+
+// `grp`: the rows come in groups of grp that belong to one object (the M filter rows of
+// a sequence: grp = M; one row per sequence: grp = 1).  The row kernels transform two
+// rows as one complex FFT, whose rounding of either row depends on the other, so they
+// pair rows only inside a group: a sequence's bits never depend on another sequence's
+// data, which keeps every per-sequence result independent of N and of the batch.
+int r2c(cdlgb_ctx* c, long long batch, float* in, float2* out, int grp) {
+    if (void* rp = row_plan(c)) return rows_r2c(c, rp, (long)batch, in, out, grp);
     cufftHandle p;
     ST_TRY(get_plan(c, 0, batch, &p));
     FFT_TRY(c, cufftExecR2C(p, (cufftReal*)in, (cufftComplex*)out));
     c->fft_calls++;
     return CDLGB_OK;
 }
-int c2r(cdlgb_ctx* c, long long batch, float2* in, float* out) {
+int c2r(cdlgb_ctx* c, long long batch, float2* in, float* out, int grp) {
+    if (void* rp = row_plan(c)) return rows_c2r(c, rp, (long)batch, in, out, grp);
     cufftHandle p;
     ST_TRY(get_plan(c, 1, batch, &p));
     FFT_TRY(c, cufftExecC2R(p, (cufftComplex*)in, (cufftReal*)out));
@@ -601,7 +614,7 @@ int device_sms() {
 
 // G1h = rfft(G1) and A = sum_m |G1h|^2
 int refresh_G1h(cdlgb_ctx* c) {
-    ST_TRY(r2c(c, c->M, c->G1, c->G1h));
+    ST_TRY(r2c(c, c->M, c->G1, c->G1h, c->M));
     k_colnorm<<<(c->F + 127) / 128, 128, 0, c->stream>>>(c->G1h, c->Ah, c->F, c->M);
     LAUNCH_CHECK(c, "k_colnorm");
     return CDLGB_OK;
@@ -830,13 +843,13 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     // DX = real(ifft(sum_m D-hat .* X-hat)) (CDL_setup.jl:197-203); G2 = DX
     for (int n0 = 0; n0 < N; n0 += c->chunk) {
         const int cn = std::min(c->chunk, N - n0);
-        ST_TRY(r2c(c, (long long)M * cn, X + (size_t)n0 * M * Lg, c->sAh));
+        ST_TRY(r2c(c, (long long)M * cn, X + (size_t)n0 * M * Lg, c->sAh, M));
         size_t FN = (size_t)c->F * cn;
         k_spec_dot<<<(unsigned)((FN + 255) / 256), 256, 0, s>>>(c->sAh, c->G1h, c->sVh + (size_t)n0 * c->F,
                                                               c->F, M, cn, 1.f / (float)Lg);
         LAUNCH_CHECK(c, "k_spec_dot");
     }
-    ST_TRY(c2r(c, N, c->sVh, c->DX));
+    ST_TRY(c2r(c, N, c->sVh, c->DX, 1));
     CU_TRY(c, cudaMemcpyAsync(c->G2, c->DX, LN * 4, cudaMemcpyDeviceToDevice, s));
     c->initialized = true;
     double obj = 0;
@@ -884,7 +897,7 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
             const int Lg = c->Lg;
             k_xprep_ln<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->y1, c->DX, c->Y1, c->sU, LN);
             LAUNCH_CHECK(c, "k_xprep_ln");
-            ST_TRY(r2c(c, N, c->sU, c->sUh));
+            ST_TRY(r2c(c, N, c->sU, c->sUh, 1));
             const int nfb = (F + 127) / 128;
             for (int n0 = 0; n0 < N; n0 += c->chunk) {
                 const int cn = std::min(c->chunk, N - n0);
@@ -893,14 +906,14 @@ int admm_code_update(cdlgb_ctx* c, int iters) {
                     (const float4*)(Xin + off), (float4*)(c->y2 + off), (float4*)(c->y3 + off),
                     (float4*)c->sA, cl / 4, c->p.lambda);
                 LAUNCH_CHECK(c, "k_xprep");
-                ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
+                ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh, M));
                 k_xsolve<<<(unsigned)((size_t)nfb * cn), 128, 0, s>>>(
                     c->sAh, c->sUh + (size_t)n0 * F, c->G1h, c->Ah, c->sVh + (size_t)n0 * F, F, M, nfb,
                     c->p.sherman_const_csc, 1.f / (float)Lg);
                 LAUNCH_CHECK(c, "k_xsolve");
-                ST_TRY(c2r(c, (long long)M * cn, c->sAh, Xout + off));
+                ST_TRY(c2r(c, (long long)M * cn, c->sAh, Xout + off, M));
             }
-            ST_TRY(c2r(c, N, c->sVh, c->DX));
+            ST_TRY(c2r(c, N, c->sVh, c->DX, 1));
             k_mask_update<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Y1, c->DX, c->y1, c->S, c->Lg,
                                                                  c->L4, c->gamma, LN, c->p.rho);
             LAUNCH_CHECK(c, "k_mask_update");
@@ -925,8 +938,8 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             // the state in the frequency domain: only Y3 is transformed (dspec.cu)
             k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
             LAUNCH_CHECK(c, "k_sub");
-            ST_TRY(r2c(c, N, c->sU, c->sUh));
-            ST_TRY(r2c(c, M, c->G3, c->G3h));
+            ST_TRY(r2c(c, N, c->sU, c->sUh, 1));
+            ST_TRY(r2c(c, M, c->G3, c->G3h, M));
             void* fw = fused_dfwd(c);
             int slot0 = 0;
             for (int n0 = 0; n0 < N; n0 += c->schunk) {
@@ -936,14 +949,14 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                 slot0 += dspec_nsub(cn, F, c->nsm);
             }
             if (c->res_on) ST_TRY(resid_d_from_spec_parts(c, slot0 * ((F + 31) / 32)));
-            ST_TRY(c2r(c, N, c->sVh, c->Td));
+            ST_TRY(c2r(c, N, c->sVh, c->Td, 1));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
                                                          c->gamma, LN, c->p.sigma);
             LAUNCH_CHECK(c, "k_dg2");
             if (c->res_on) ST_TRY(resid_td(c));
             // the three sums over n, back in the time domain: part as one chunk
             ST_TRY(dspec_sums(c, c->G3h, c->sumspec));
-            ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part));
+            ST_TRY(c2r(c, 3LL * M, c->sumspec, c->part, 3 * M));
             c->time_stale = 1;
             c->time_init = 0;
             int flen = 4 * c->p.filter_size;
@@ -961,7 +974,7 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
         {
             k_sub<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->G2, c->g2, c->sU, LN);
             LAUNCH_CHECK(c, "k_sub");
-            ST_TRY(r2c(c, N, c->sU, c->sUh));
+            ST_TRY(r2c(c, N, c->sU, c->sUh, 1));
             void* fw = c->fused && c->Dhs ? fused_dfwd(c) : nullptr;
             for (int n0 = 0; n0 < N; n0 += c->chunk) {
                 const int cn = std::min(c->chunk, N - n0);
@@ -982,16 +995,16 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
                         (const float4*)c->G1, (const float4*)c->G3, (float4*)c->sA, (float4*)c->sB,
                         cl / 4, LM / 4);
                     LAUNCH_CHECK(c, "k_dprep");
-                    ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh));
-                    ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh));
-                    ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh));
+                    ST_TRY(r2c(c, (long long)M * cn, c->sA, c->sAh, M));
+                    ST_TRY(r2c(c, (long long)M * cn, c->sB, c->sBh, M));
+                    ST_TRY(r2c(c, (long long)M * cn, c->d + off, c->sCh, M));
                     ST_TRY(dsolve_launch(c, cn, c->sAh, c->sBh, c->sCh, c->sUh + (size_t)n0 * F,
                                          c->sVh + (size_t)n0 * F, 1.f / (float)Lg));
-                    ST_TRY(c2r(c, (long long)M * cn, c->sCh, c->d + off));
+                    ST_TRY(c2r(c, (long long)M * cn, c->sCh, c->d + off, M));
                 }
             }
             c->dh_valid = fw != nullptr;
-            ST_TRY(c2r(c, N, c->sVh, c->Td));
+            ST_TRY(c2r(c, N, c->sVh, c->Td, 1));
             k_dg2<<<grid_for(LN, kBlock), kBlock, 0, s>>>(c->Td, c->g2, c->G2, c->S, Lg, c->L4,
                                                          c->gamma, LN, c->p.sigma);
             LAUNCH_CHECK(c, "k_dg2");
@@ -1112,7 +1125,7 @@ int admm_sync_time_state(cdlgb_ctx* c) {
             } else {
                 CU_TRY(c, cudaMemcpyAsync(c->sAh, sq, sp * 8, cudaMemcpyDeviceToDevice, c->stream));
             }
-            ST_TRY(c2r(c, (long long)M * cn, c->sAh, dst[q] + (size_t)n0 * M * Lg));
+            ST_TRY(c2r(c, (long long)M * cn, c->sAh, dst[q] + (size_t)n0 * M * Lg, M));
             ST_TRY(dspec_scale(c, dst[q] + (size_t)n0 * M * Lg, tp, 1.f / (float)Lg));
         }
     c->time_stale = 0;

@@ -353,6 +353,7 @@ static int load_impl(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, in
     if (f < 0)
         return cdlgb_seterr(c, CDLGB_ENOTSUP, "fused path does not support Lg=%d, M=%d", c->Lg, c->M);
     c->fused = f;
+    if (const char* e = getenv("CDLGB_ROWFFT")) c->rows_cufft = atoi(e) == 0;
     // admission by HBM footprint
     size_t need = admm_footprint(&p, L4, N, c->fused);
     size_t freeb = 0, total = 0;

@@ -138,6 +138,8 @@ struct cdlgb_ctx {
     int64_t ph_n[PH_COUNT] = {};
     int64_t launches = 0;           // our own kernel launches
     int64_t fft_calls = 0;          // cuFFT exec calls
+    bool rows_cufft = false;        // CDLGB_ROWFFT=0: row transforms on cuFFT even where
+                                    // the register-FFT row kernels exist
 };
 
 int cdlgb_seterr(cdlgb_ctx* c, int code, const char* fmt, ...);
@@ -251,6 +253,10 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status);
 void dfwd_plan_free(cdlgb_ctx* c, void* p);
 int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, float2* Hh, float2* Dh);
 int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn, float scale);
+// batched R2C / C2R of R contiguous rows on the register FFT (cuFFT's layouts and
+// scaling); two rows share a transform only inside a group of grp consecutive rows
+int rows_r2c(cdlgb_ctx* c, void* p, long R, const float* in, float2* out, int grp);
+int rows_c2r(cdlgb_ctx* c, void* p, long R, const float2* in, float* out, int grp);
 void* fused_dfwd(cdlgb_ctx* c);
 int fused_xsteps(cdlgb_ctx* c, const float* Xin, float* Xout, int iters);
 

@@ -198,24 +198,151 @@ __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
     }
 }
 
+// Batched real transforms of R contiguous rows, in the layouts of the cuFFT batched plans
+// they replace (rows of Lg floats; half-spectra of F = Lg/2 + 1 bins; unnormalised both
+// ways, so C2R returns Lg times the input row).  The rows come in groups of grp
+// consecutive rows (R a multiple of grp); inside a group, rows 2j and 2j + 1 form one
+// complex transform of a lane group (the last row of an odd group is paired with zeros),
+// so no row's rounding depends on a row of another group.  The forward split is
+// split_store's; the inverse packs Z = A + i B from both half-spectra and drops the
+// imaginary parts of bins 0 and Lg/2, as k_dinv does.
+template <int N1, int P>
+__global__ void __launch_bounds__(256, 2) k_rows_r2c(const float* __restrict__ x, float2* __restrict__ X,
+                                                     const float2* __restrict__ tw2g, long R, int grp) {
+    constexpr int Lg = N1 * P;
+    constexpr int G = 32 / N1;
+    constexpr int RS = N1 + 1;
+    constexpr int BUF = (P * RS + 1) & ~1;
+    constexpr int F = Lg / 2 + 1;
+    extern __shared__ float4 smem4[];
+    float2* tw2 = reinterpret_cast<float2*>(smem4);
+    float2* bufs = tw2 + P * N1;
+    for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = tw2g[t];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int gw = (threadIdx.x >> 5) * G + lane / N1;
+    const int gl = lane % N1;
+    const int groups = (blockDim.x >> 5) * G;
+    float2* sb = bufs + (size_t)gw * BUF;
+    const int ppg = (grp + 1) / 2;                         // pairs per group
+    const long items = (R / grp) * ppg;
+    const long stride = (long)gridDim.x * groups;
+    const long rounds = (items + stride - 1) / stride;
+    for (long r = 0; r < rounds; ++r) {
+        const long item = r * stride + (long)blockIdx.x * groups + gw;
+        const bool act = item < items;
+        const long g = act ? item / ppg : 0;
+        const int j = act ? (int)(item - g * ppg) : 0;
+        const long a = g * grp + 2 * j;
+        const bool hb = 2 * j + 1 < grp;
+        if (act) {
+            const float* xa = x + (size_t)a * Lg + gl;
+#pragma unroll 16
+            for (int n2 = 0; n2 < P; ++n2) {
+                const int o = N1 * n2;
+                sb[n2 * RS + gl] = f2(__ldg(xa + o), hb ? __ldg(xa + Lg + o) : 0.f);
+            }
+            fwd_step1<N1, P>(sb, gl, tw2);
+        }
+        __syncwarp();
+        fwd_step2<N1, P>(sb, gl, act);
+        if (act) {
+            float2* oa = X + (size_t)a * F;
+            for (int f = gl; f < F; f += N1) {
+                const float2 z1 = sb[f], z2 = sb[f == 0 ? 0 : Lg - f];
+                oa[f] = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+                if (hb) oa[F + f] = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int N1, int P>
+__global__ void __launch_bounds__(256, 2) k_rows_c2r(const float2* __restrict__ X, float* __restrict__ x,
+                                                     const float2* __restrict__ tw2g, long R, int grp) {
+    constexpr int Lg = N1 * P;
+    constexpr int G = 32 / N1;
+    constexpr int RS = N1 + 1;
+    constexpr int BUF = (P * RS + 1) & ~1;
+    constexpr int F = Lg / 2 + 1;
+    constexpr int half = Lg / 2;
+    extern __shared__ float4 smem4[];
+    float2* tw2 = reinterpret_cast<float2*>(smem4);
+    float2* bufs = tw2 + P * N1;
+    for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = tw2g[t];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int gw = (threadIdx.x >> 5) * G + lane / N1;
+    const int gl = lane % N1;
+    const int groups = (blockDim.x >> 5) * G;
+    float2* sb = bufs + (size_t)gw * BUF;
+    const int ppg = (grp + 1) / 2;                         // pairs per group
+    const long items = (R / grp) * ppg;
+    const long stride = (long)gridDim.x * groups;
+    const long rounds = (items + stride - 1) / stride;
+    for (long r = 0; r < rounds; ++r) {
+        const long item = r * stride + (long)blockIdx.x * groups + gw;
+        const bool act = item < items;
+        const long g = act ? item / ppg : 0;
+        const int j = act ? (int)(item - g * ppg) : 0;
+        const long a = g * grp + 2 * j;
+        const bool hb = 2 * j + 1 < grp;
+        if (act) {
+            const float2* ia = X + (size_t)a * F;
+#pragma unroll 5
+            for (int f = gl; f < F; f += N1) {
+                const float2 A = __ldg(ia + f), B = hb ? __ldg(ia + F + f) : f2(0.f, 0.f);
+                if (f == 0 || f == half) {
+                    sb[f] = f2(A.x, B.x);
+                } else {
+                    sb[f] = f2(A.x - B.y, A.y + B.x);
+                    sb[Lg - f] = f2(A.x + B.y, B.x - A.y);
+                }
+            }
+        }
+        __syncwarp();
+        inv_step2<N1, P, false>(sb, gl, act, tw2);
+        if (act) {
+            inv_step1<N1, P, true>(sb, gl, tw2);
+            float* ra = x + (size_t)a * Lg + gl;
+#pragma unroll 4
+            for (int n2 = 0; n2 < P; ++n2) {
+                const float2 v = sb[n2 * RS + gl];
+                ra[N1 * n2] = v.x;
+                if (hb) ra[Lg + N1 * n2] = v.y;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 typedef void (*kern_t)(FArgs);
 typedef void (*kinv_t)(IArgsD);
-struct Variant { int N1, P; kern_t k; kinv_t ki; };
+typedef void (*kr2c_t)(const float*, float2*, const float2*, long, int);
+typedef void (*kc2r_t)(const float2*, float*, const float2*, long, int);
+struct Variant { int N1, P; kern_t k; kinv_t ki; kr2c_t kf; kc2r_t kb; };
+#define DSTREAM_VARIANT(N1, P) {N1, P, k_dfwd<N1, P>, k_dinv<N1, P>, k_rows_r2c<N1, P>, k_rows_c2r<N1, P>}
 const Variant kVariants[] = {
-    {32, 29, k_dfwd<32, 29>, k_dinv<32, 29>},
-    {16, 31, k_dfwd<16, 31>, k_dinv<16, 31>},
-    {32, 17, k_dfwd<32, 17>, k_dinv<32, 17>},
-    {32, 19, k_dfwd<32, 19>, k_dinv<32, 19>},
-    {32, 23, k_dfwd<32, 23>, k_dinv<32, 23>},
-    {32, 31, k_dfwd<32, 31>, k_dinv<32, 31>},
+    DSTREAM_VARIANT(32, 29),
+    DSTREAM_VARIANT(16, 31),
+    DSTREAM_VARIANT(32, 17),
+    DSTREAM_VARIANT(32, 19),
+    DSTREAM_VARIANT(32, 23),
+    DSTREAM_VARIANT(32, 31),
 };
+#undef DSTREAM_VARIANT
 
 struct FwdPlan {
     kern_t k;
     kinv_t ki;
+    kr2c_t kf;
+    kc2r_t kb;
     int N1, P;
     size_t smem;
-    int grid, grid_inv;
+    int grid, grid_inv, grid_rows_f, grid_rows_b;
     float2* tw2;
 };
 
@@ -232,7 +359,7 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
         if (cand.N1 * cand.P == c->Lg) v = &cand;
     if (!v) return nullptr;
     FwdPlan* P = new FwdPlan();
-    P->k = v->k; P->ki = v->ki; P->N1 = v->N1; P->P = v->P;
+    P->k = v->k; P->ki = v->ki; P->kf = v->kf; P->kb = v->kb; P->N1 = v->N1; P->P = v->P;
     const int threads = 256, groups = (threads / 32) * (32 / v->N1);
     const size_t buf = ((size_t)v->P * (v->N1 + 1) + 1) & ~(size_t)1;
     P->smem = ((size_t)v->P * v->N1 + (size_t)groups * buf) * sizeof(float2);
@@ -241,10 +368,14 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     if (e == cudaSuccess) e = dev_copy_in(c, (void**)&P->tw2, tw2.data(), tw2.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(P->k, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(P->ki, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    int per_sm = 0, per_sm_inv = 0;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->kf, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(P->kb, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    int per_sm = 0, per_sm_inv = 0, per_sm_f = 0, per_sm_b = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, P->k, threads, P->smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_inv, P->ki, threads, P->smem);
-    if (e != cudaSuccess || per_sm < 1 || per_sm_inv < 1) {
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_f, P->kf, threads, P->smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_b, P->kb, threads, P->smem);
+    if (e != cudaSuccess || per_sm < 1 || per_sm_inv < 1 || per_sm_f < 1 || per_sm_b < 1) {
         *status = cdlgb_seterr(c, CDLGB_ECUDA, "D-step transform setup failed: %s",
                                e != cudaSuccess ? cudaGetErrorString(e) : "no CTA fits");
         dev_free(c, P->tw2);
@@ -256,6 +387,8 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     P->grid = per_sm * sms;
     P->grid_inv = per_sm_inv * sms;
+    P->grid_rows_f = per_sm_f * sms;
+    P->grid_rows_b = per_sm_b * sms;
     return P;
 }
 
@@ -288,5 +421,31 @@ int dinv_run(cdlgb_ctx* c, void* p, const float2* Dh, int n0, int cn, float scal
     a.scale = scale;
     P->ki<<<P->grid_inv, 256, P->smem, c->stream>>>(a);
     LAUNCH_CHECK(c, "k_dinv");
+    return CDLGB_OK;
+}
+
+// R2C / C2R of R contiguous rows with the register FFT (the cuFFT batched plans' layouts)
+static unsigned rows_grid(long R, int grp, int cap, int N1) {
+    const long lane_groups = (256 / 32) * (32 / N1);
+    const long items = (R / grp) * ((grp + 1) / 2);
+    const long need = (items + lane_groups - 1) / lane_groups;
+    return (unsigned)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+int rows_r2c(cdlgb_ctx* c, void* p, long R, const float* in, float2* out, int grp) {
+    FwdPlan* P = (FwdPlan*)p;
+    if (grp < 1 || R % grp)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "row transform: %ld rows in groups of %d", R, grp);
+    P->kf<<<rows_grid(R, grp, P->grid_rows_f, P->N1), 256, P->smem, c->stream>>>(in, out, P->tw2, R, grp);
+    LAUNCH_CHECK(c, "k_rows_r2c");
+    return CDLGB_OK;
+}
+
+int rows_c2r(cdlgb_ctx* c, void* p, long R, const float2* in, float* out, int grp) {
+    FwdPlan* P = (FwdPlan*)p;
+    if (grp < 1 || R % grp)
+        return cdlgb_seterr(c, CDLGB_EINVAL, "row transform: %ld rows in groups of %d", R, grp);
+    P->kb<<<rows_grid(R, grp, P->grid_rows_b, P->N1), 256, P->smem, c->stream>>>(in, out, P->tw2, R, grp);
+    LAUNCH_CHECK(c, "k_rows_c2r");
     return CDLGB_OK;
 }

@@ -187,8 +187,8 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
     the FP64 oracle after 3 outer iterations.  The two run the same statements with
     different FP32 rounding, which the ADMM amplifies by itself (the FP32-ordered oracle
     drifts ~1e-4 from FP64 in 2-3 outer iterations): the objectives agree to 1e-5, and
-    every field of the spectral run is as close to FP64 as the time-domain run's, up
-    to 2.5x (or the 1e-4 tolerance)."""
+    the objectives and every field of the spectral run are as close to FP64 as the
+    time-domain run's, up to 2.5x (or the 1e-5 / 1e-4 tolerance)."""
     N, L, M, fs = shape
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(19, N, L, [8, 12], [0.4, 0.4])
@@ -206,7 +206,8 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
             out[spec] = {f: c.get(f) for f in ("X", "d", "g1", "g3", "G1", "G3", "D_best", "Td")}
             out[spec]["objs"] = objs
     np.testing.assert_allclose(out["1"]["objs"], out["0"]["objs"], rtol=TOL_OBJ)
-    np.testing.assert_allclose(out["1"]["objs"], objs_ref, rtol=TOL_OBJ)
+    dev = lambda o: np.abs(np.asarray(o) - objs_ref) / np.abs(objs_ref)
+    assert np.all(dev(out["1"]["objs"]) <= np.maximum(TOL_OBJ, 2.5 * dev(out["0"]["objs"])))
     for f in ("X", "d", "g1", "g3", "G1", "G3", "D_best", "Td"):
         env = max(TOL_X, 2.5 * rel(out["0"][f], getattr(ref, f)))
         assert rel(out["1"][f], getattr(ref, f)) < env, f

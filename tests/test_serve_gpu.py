@@ -105,3 +105,34 @@ def test_server_refuses_what_never_fits(pkg, built_lib):
     with serve.Server(setup, slots=1, iter_num=1, hbm_budget=fp) as srv:
         rid = srv.submit(d)
         assert srv.poll(rid, wait_ms=-1)["state"] == "done"
+
+
+@pytest.mark.gpu
+def test_device_memory_comes_back(pkg, built_lib):
+    """Contexts allocate stream-ordered from the library's device pool: after a
+    training's context is destroyed (and the device synchronised) its memory is back,
+    so repeated trainings do not grow the process's footprint; a server keeps what its
+    finished datasets free for reuse while it lives and gives it back when it ends."""
+    torch = pytest.importorskip("torch")
+    from cdlmotif_gb300 import serve
+    setup = pkg.CDLSetup(M=32, filter_size=16, lambda_=0.1, rho=1.0, sigma=100.0)
+    bases, _, _ = pkg.synth.plant_dataset(5, 2000, 200, [10], [0.3])
+    S = pkg.synth.onehot(bases)
+    need = serve.footprint_bytes(setup, 200, 2000)
+    slack = 128 << 20
+    serve.run_training(setup, S, iter_num=1, seed=1, device=0)    # modules, tables, pinned slab
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        serve.run_training(setup, S, iter_num=1, seed=1, device=0)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] >= free0 - slack
+    with serve.Server(setup, slots=2, iter_num=1, seed=1) as s:
+        ids = [s.submit(S) for _ in range(3)]
+        for rid in ids:
+            assert s.poll(rid, wait_ms=-1)["state"] == "done"
+        torch.cuda.synchronize()
+        held = torch.cuda.mem_get_info()[0]
+        assert held <= free0 - need // 2          # the pool keeps the freed blocks
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] >= free0 - slack

@@ -430,7 +430,8 @@ def run_batched(args):
     """The 64-dataset mix processed plainly (one training after another, each alone on
     the GPU) and batched (all submitted at once to the library's training server, up to
     `serve_slots` trainings in flight); datasets/hr of both, how busy the GPU was in the
-    plain form (the sum of every training's kernel time from the library's CUDA-event
+    plain form (the sum of every training's device time -- data upload, initialisation,
+    X-steps, D-steps, objectives, code threshold -- from the library's CUDA-event
     phase timers against the wall clock, and nvidia-smi's utilisation), and the largest
     difference between a dataset's D_best alone and in the mix (the kernels are
     deterministic and contexts share nothing, so it should be 0)."""
@@ -464,6 +465,7 @@ def run_batched(args):
             "plain_kernel_seconds": busy_ms / 1e3, "plain_busy_fraction": busy,
             "plain_idle_fraction": 1.0 - busy,
             "batching_bound_if_idle_removed": 1.0 / busy if busy > 0 else None,
+            "batched_fraction_of_bound": (res["datasets_per_hr"] / plain_rate) * busy,
             "completed": res["completed"], "rejected": res["rejected"], "slots": args.serve_slots,
             "outer_iterations_per_dataset": iters, "max_abs_diff_D_best_alone_vs_mix": diff,
             "dtype": "f32", "data": "synthetic (seeded planted motifs)",

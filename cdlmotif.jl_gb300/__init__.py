@@ -285,7 +285,7 @@ class CDL:
     def profile(self, enable: bool = True):
         _check(self._h, _lib.lib().cdlgb_profile(self._h, 1 if enable else 0))
 
-    PHASES = ("xstep", "dstep", "objective", "xfused", "spare_a", "spare_b", "scan", "spare")
+    PHASES = ("xstep", "dstep", "objective", "xfused", "setup", "threshold", "scan", "spare")
 
     def profile_read(self, reset: bool = True) -> dict:
         ms = (C.c_double * 8)()

@@ -294,8 +294,16 @@ __global__ void k_encode_onehot(const uint8_t* __restrict__ codes, float4* __res
 }
 
 // Uploads the data: the float one-hot matrix as given, or (codes != NULL) one byte per
-// base, expanded on the device.
+// base, expanded on the device (timed as part of the set-up phase).
+static int upload_data_timed(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, size_t n);
 static int upload_data(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, size_t n) {
+    cdlgb_phase_begin(c, PH_SETUP);
+    const int st = upload_data_timed(c, onehot, codes, n);
+    cdlgb_phase_end(c, PH_SETUP);
+    return st;
+}
+
+static int upload_data_timed(cdlgb_ctx* c, const float* onehot, const uint8_t* codes, size_t n) {
     if (onehot) {
         CU_TRY(c, cudaMemcpyAsync(c->S, onehot, n * 4, cudaMemcpyHostToDevice, c->stream));
         return check_onehot(c);
@@ -427,7 +435,10 @@ int cdlgb_dims(const cdlgb_ctx* c, int32_t* L4, int32_t* N, int32_t* M, int32_t*
 int cdlgb_init_state(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     NEED_LOADED(c);
     c->initialized = false;
-    return admm_init(c, X0, D0, seed);
+    cdlgb_phase_begin(c, PH_SETUP);
+    const int st = admm_init(c, X0, D0, seed);
+    cdlgb_phase_end(c, PH_SETUP);
+    return st;
 }
 
 int cdlgb_code_update(cdlgb_ctx* c, int32_t num_iter) {
@@ -482,7 +493,10 @@ int cdlgb_run_outer(cdlgb_ctx* c, int32_t iter_num, double* objs) {
 int cdlgb_code_threshold(cdlgb_ctx* c, double* thresh) {
     NEED_INIT(c);
     if (!thresh) return cdlgb_seterr(c, CDLGB_EINVAL, "thresh is NULL");
-    return admm_code_threshold(c, thresh);
+    cdlgb_phase_begin(c, PH_THRESH);
+    const int st = admm_code_threshold(c, thresh);
+    cdlgb_phase_end(c, PH_THRESH);
+    return st;
 }
 
 int cdlgb_get(cdlgb_ctx* c, int32_t field, void* dst, size_t bytes) {

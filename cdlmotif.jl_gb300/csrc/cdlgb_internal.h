@@ -17,8 +17,8 @@ enum cdlgb_phase {
     PH_DSTEP,         // one whole D-step iteration
     PH_OBJ,           // objective / update_best
     PH_XFUSED,        // the fused X-step kernel alone
-    PH_SPARE_A,       // unused (keeps the reported slot order)
-    PH_SPARE_B,       // unused
+    PH_SETUP,         // the data upload's copy and kernels, and the state initialisation
+    PH_THRESH,        // the code threshold
     PH_SCAN,
     PH_COUNT
 };

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import RequestInfo, ServerConfig, ptr
-from . import CDLSetup, CDLGBError, init_cdl, code_update, dict_update, update_best, code_threshold
+from . import CDL, CDLSetup, CDLGBError, init_cdl, code_update, dict_update, update_best, code_threshold
 
 STATES = {0: "pending", 1: "running", 2: "done", 3: "failed"}
 
@@ -170,12 +170,15 @@ def run_training(setup: CDLSetup, data: np.ndarray, iter_num: int, seed: int, de
                  profile: bool = False) -> dict:
     """One cdl_optimize training (src/WRAPPER/wrap.jl:5-12) of one dataset on its own
     context: init, iter_num outer iterations, code threshold; returns D_best, objectives
-    and the threshold (with `profile`, also the kernel time of its X-steps, D-steps and
-    objectives from the library's CUDA-event phase timers, device_ms)."""
-    c = init_cdl(setup, data, seed=seed, device=device)
+    and the threshold (with `profile`, also the device time of all of it from the
+    library's CUDA-event phase timers, device_ms: the data upload's copy and kernels,
+    the initialisation, X-steps, D-steps, objectives and the code threshold)."""
+    c = CDL(setup, device=device)
     try:
         if profile:
             c.profile(True)
+        c.load_data(data)
+        c.init_state(None, None, seed)
         objs = []
         for _ in range(iter_num):
             code_update(c, setup.csc_iter_num)
@@ -186,7 +189,7 @@ def run_training(setup: CDLSetup, data: np.ndarray, iter_num: int, seed: int, de
                "N": c.N, "L4": c.L}
         if profile:
             pr = c.profile_read()
-            out["device_ms"] = sum(pr[k][0] for k in ("xstep", "dstep", "objective"))
+            out["device_ms"] = sum(pr[k][0] for k in ("setup", "xstep", "dstep", "objective", "threshold"))
         return out
     finally:
         c.close()

@@ -364,11 +364,13 @@ int cdlgb_ar_pair_pfms(cdlgb_ar* ar, cdlgb_ctx* ctx, const int32_t* pairs, int32
  * e.g. CUDA.jl's task stream; NULL returns to a stream owned by the context. */
 int cdlgb_set_stream(cdlgb_ctx* ctx, void* cuda_stream);
 
-/* Enable per-phase CUDA-event timers (X-step, D-step, objective, fused kernels, scan). */
+/* Enable per-phase CUDA-event timers (X-step, D-step, objective, fused kernels, data
+ * upload + state initialisation, code threshold, scan). */
 int cdlgb_profile(cdlgb_ctx* ctx, int32_t enable);
 
 /* Read the accumulated phase times: ms[8], counts[8] (order: X-step, D-step,
- * objective, fused X kernel, two unused slots, scan, reserved),
+ * objective, fused X kernel, set-up (the data upload's copy and kernels, and
+ * cdlgb_init_state), code threshold, scan, reserved),
  * the number of this library's kernel launches and of cuFFT executions. */
 int cdlgb_profile_read(cdlgb_ctx* ctx, double* ms, int64_t* counts, int64_t* launches,
                        int64_t* fft_calls, int32_t reset);

@@ -302,6 +302,14 @@ def run_refstruct(args, config):
                     "reference CUDA.jl path, which cannot run here"}
 
 
+def measured_hbm_peak() -> float:
+    """The measured HBM copy bandwidth (GB/s) of MEASURED_PEAKS.json, else the fallback."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+    except Exception:
+        return 6800.0
+
+
 def roofline(prof, steps, fused, sm_mhz=None):
     """Roofline of the dominant kernel, from the phase timers recorded (CUDA events on
     the launching stream) during the timed region.  For the multi-iteration X-step also
@@ -540,6 +548,48 @@ def run_interference(args, n_small: int = 5):
                        "small": {"N": 1000, "L": 200, "K": 32, "outer_iterations": 3}}}
 
 
+def run_lengths(args, Ls=(100, 200, 500), N: int = 5000, K: int = 32, outer: int = 3):
+    """Per transform length: the batched mix's lengths (L = 100, 200, 500 with W = 16:
+    Lg = 528, 928, 2128) on N = 5000 sequences with K = 32 filters, `outer` timed outer
+    iterations after one untimed: outer iterations/s, the X-step and D-step device time
+    per outer iteration from the library's phase timers, and the kernel path each length
+    takes (register-FFT lengths run the multi-iteration X-step and the spectral D-step
+    on the register-FFT transforms; the others the generic in-kernel FFT X-step).  The
+    X-step's and D-step's algorithmic bytes over their time give each one's HBM rate."""
+    import torch
+    pkg = _pkg()
+    peak = measured_hbm_peak()
+    out = []
+    for L in Ls:
+        wl = dict(WORKLOAD, N=N, L=L, M=K, name=f"len_n{N}_l{L}_k{K}")
+        S = pkg.synth.onehot(dataset(wl))
+        setup = pkg.CDLSetup(M=K, filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
+                             sigma=wl["sigma"])
+        ab = algorithmic_bytes(wl)
+        with pkg.init_cdl(setup, S, seed=wl["seed"]) as c:
+            pkg.run_outer(c, 1)
+            c.profile(True)
+            c.profile_read(reset=True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pkg.run_outer(c, outer)
+            torch.cuda.synchronize()
+            sec = time.perf_counter() - t0
+            pr = c.profile_read()
+            xs, ds = pr["xstep"][0] / outer, pr["dstep"][0] / outer
+            out.append({"L": L, "Lg": ab["Lg"], "N": N, "K": K, "outer_iter_per_s": outer / sec,
+                        "xstep_ms_per_outer": xs, "dstep_ms_per_outer": ds,
+                        "objective_ms_per_outer": pr["objective"][0] / outer,
+                        "xstep_frac_of_hbm_peak": (15 * ab["xstep"] / (xs / 1e3)) / (peak * 1e9) if xs else None,
+                        "dstep_frac_of_hbm_peak": (ab["dstep"] / (ds / 1e3)) / (peak * 1e9) if ds else None,
+                        "fused_xstep_launches_per_outer": pr["xfused"][1] / outer,
+                        "cufft_exec_per_outer": pr["fft_calls"] / outer})
+    return {"metric": "outer iterations/s per transform length (N=5000, K=32, W=16)",
+            "value": None, "unit": "outer_iter/s", "lengths": out, "hbm_peak_gbs": peak,
+            "dtype": "f32", "data": "synthetic (seeded planted motifs)",
+            "config": {"workload": "lengths", "L": list(Ls), "N": N, "K": K}}
+
+
 def search_inputs(wl=WORKLOAD, K=32, N=None):
     """The search-stage inputs on the bench dataset: the planted motifs' cores (two
     columns trimmed per side, so that extend! has columns to find) and random
@@ -764,6 +814,8 @@ def main():
     ap.add_argument("--batched", action="store_true",
                     help="64-dataset mix: plain (one at a time) vs batched (served) datasets/hr")
     ap.add_argument("--batched-n", type=int, default=64)
+    ap.add_argument("--lengths", action="store_true",
+                    help="outer iterations/s and phase times at the batched mix's transform lengths")
     ap.add_argument("--interference", action="store_true",
                     help="GPU time a running training loses per dataset trained beside it")
     ap.add_argument("--precision", action="store_true",
@@ -806,6 +858,10 @@ def main():
     if args.batched:
         if rank == 0:
             print(json.dumps(run_batched(args)))
+        return
+    if args.lengths:
+        if rank == 0:
+            print(json.dumps(run_lengths(args)))
         return
     if args.interference:
         if rank == 0:

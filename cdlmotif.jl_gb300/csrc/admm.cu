@@ -169,6 +169,17 @@ __global__ void k_dprep(const float4* __restrict__ X, const float4* __restrict__
     }
 }
 
+// Y3 = projectionX!(X + y3) (csc_kernels.jl:68-82) of a chunk, for the spectral D-step on
+// lengths without the streaming transforms: X + 0 on the rows l % 4 == 0 (every row
+// starts at a multiple of 4 floats, so those are the .x lanes), where every X-step
+// leaves y3 = +0 exactly (projectionX! keeps X + y3 there, so y3' = (y3 + X) - Y3 = +0,
+// as initialisation sets it), and 0 on the others -- the values k_dfwd transforms.
+__global__ void k_y3(const float4* __restrict__ X, float4* __restrict__ Y3, size_t n4) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x)
+        Y3[i] = make_float4(X[i].x + 0.f, 0.f, 0.f, 0.f);
+}
+
 __global__ void k_sub(const float* __restrict__ a, const float* __restrict__ b,
                       float* __restrict__ o, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -625,14 +636,28 @@ float* cur_X(cdlgb_ctx* c) { return c->Xb[c->xcur]; }
 }  // namespace
 
 // ============================================================================ API-level
+// The D-step keeps d, g1, g3 as half-spectra (dspec.cu) on the fused path and on the
+// automatically chosen cuFFT-transform path (not when cuFFT transforms are asked for
+// explicitly, the form kept next to the reference's own), for M up to dspec_max_m();
+// CDLGB_DSPEC=0 keeps them in the time domain.  With the spectral state, the
+// time-domain d, g1, g3 are only a reader's copy, allocated at the first read.
+bool spectral_state(const cdlgb_params* p, int fused) {
+    if (p->M > dspec_max_m() || (!fused && p->fft_mode != 0)) return false;
+    const char* e = getenv("CDLGB_DSPEC");
+    return !e || atoi(e) != 0;
+}
+
 size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused) {
     size_t gamma = 4 * (size_t)p->filter_size, Lg = L4 + 2 * gamma, F = Lg / 2 + 1;
     size_t M = p->M, LMN = Lg * M * N, LN = Lg * N, LM = Lg * M;
+    const bool spec = spectral_state(p, fused);
     size_t b = 0;
     b += (size_t)N * L4 * 4;                    // data
-    b += 7 * LMN * 4;                           // X x2, y2, y3, d, g1, g3
-    if (fused) b += (size_t)N * M * F * 8 * 2;  // d-hat, g1-hat (spectral D-step)
-    if (fused) {
+    b += 4 * LMN * 4;                           // X x2, y2, y3
+    if (!spec) b += 3 * LMN * 4;                // d, g1, g3 (time-domain D-step)
+    if (fused || spec) b += (size_t)N * M * F * 8;   // d-hat
+    if (spec) b += (size_t)N * M * F * 8;            // g1-hat
+    if (spec) {
         // spectral D-step: the sums' slots and the Y3 half-spectra beyond the cuFFT chunk
         const size_t sch = spec_chunk_for(N, (int)M, (int)Lg), ch = chunk_for(N, (int)M, (int)Lg);
         b += (size_t)dspec_slots(N, (int)sch, (int)F, device_sms()) * 2 * M * F * 8;
@@ -658,15 +683,19 @@ int admm_alloc(cdlgb_ctx* c) {
     ST_TRY(A((void**)&c->Xb[1], LMN * 4));
     ST_TRY(A((void**)&c->y2, LMN * 4));
     ST_TRY(A((void**)&c->y3, LMN * 4));
-    ST_TRY(A((void**)&c->d, LMN * 4));
-    ST_TRY(A((void**)&c->g1, LMN * 4));
-    ST_TRY(A((void**)&c->g3, LMN * 4));
-    // the previous D-step's d-hat (fused path): (N, M, F) complex; with the spectral
-    // D-step also g1-hat and g3-hat, G3-hat and the sums' spectra
-    if (c->fused) {
+    const bool spec = spectral_state(&c->p, c->fused);
+    if (!spec) {
+        ST_TRY(A((void**)&c->d, LMN * 4));
+        ST_TRY(A((void**)&c->g1, LMN * 4));
+        ST_TRY(A((void**)&c->g3, LMN * 4));
+    }
+    // the previous D-step's d-hat (N, M, F) complex (the fused path's time-domain
+    // D-step keeps it too); with the spectral D-step also g1-hat (g3-hat is g1-hat
+    // minus one shared spectrum), G3-hat and the sums' spectra
+    if (c->fused || spec) {
         const size_t nmf = (size_t)c->N * c->M * c->F;
         ST_TRY(A((void**)&c->Dhs, nmf * 8));
-        if (c->M <= dspec_max_m()) {
+        if (spec) {
             ST_TRY(A((void**)&c->g1h, nmf * 8));
             ST_TRY(A((void**)&c->Dg, (size_t)c->M * c->F * 8));
             ST_TRY(A((void**)&c->G3h, (size_t)c->M * c->F * 8));
@@ -752,9 +781,17 @@ void admm_free(cdlgb_ctx* c) {
 
 int cdlgb_set_plan_streams(cdlgb_ctx* c) { return set_plan_streams(c); }
 
+// the time-domain d, g1, g3 of the spectral form, allocated at their first reader
+static int ensure_time_state(cdlgb_ctx* c) {
+    for (float** p : {&c->d, &c->g1, &c->g3})
+        if (!*p) ST_TRY(dev_alloc(c, (void**)p, c->LMN * 4));
+    return CDLGB_OK;
+}
+
 // the initial time-domain dictionary state: d = G1 broadcast over n, g1 = g3 = 0
 static int write_time_init(cdlgb_ctx* c) {
     const size_t LMN = c->LMN;
+    ST_TRY(ensure_time_state(c));
     k_bcast_plane<<<grid_for(LMN / 4, kBlock), kBlock, 0, c->stream>>>(
         (float4*)c->d, (const float4*)c->G1, c->LM / 4, LMN / 4);
     LAUNCH_CHECK(c, "k_bcast_plane");
@@ -785,10 +822,7 @@ int admm_init(cdlgb_ctx* c, const float* X0, const float* D0, uint64_t seed) {
     c->dspec = 0;
     c->time_stale = 0;
     c->time_init = 0;
-    if (c->g1h && c->fused && fused_dfwd(c)) {
-        const char* e = getenv("CDLGB_DSPEC");
-        if (!e || atoi(e) != 0) c->dspec = 1;
-    }
+    if (c->g1h) c->dspec = 1;                 // spectral_state() held at allocation
     // D0 (CDL_setup.jl:182-183), masked by P_D
     std::vector<float> D(LM, 0.f);
     if (D0) {
@@ -944,7 +978,20 @@ int admm_dict_update(cdlgb_ctx* c, int iters) {
             int slot0 = 0;
             for (int n0 = 0; n0 < N; n0 += c->schunk) {
                 const int cn = std::min(c->schunk, N - n0);
-                ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, nullptr, nullptr));
+                if (fw) {
+                    ST_TRY(dfwd_run(c, fw, cur_X(c), n0, cn, c->sAh, nullptr, nullptr));
+                } else {
+                    // lengths without the streaming transforms: Y3 formed in the time
+                    // domain and transformed, a cuFFT chunk at a time
+                    for (int m0 = n0; m0 < n0 + cn; m0 += c->chunk) {
+                        const int cm = std::min(c->chunk, n0 + cn - m0);
+                        const size_t cl = (size_t)cm * M * Lg;
+                        k_y3<<<grid_for(cl / 4, kBlock), kBlock, 0, s>>>(
+                            (const float4*)(cur_X(c) + (size_t)m0 * M * Lg), (float4*)c->sA, cl / 4);
+                        LAUNCH_CHECK(c, "k_y3");
+                        ST_TRY(r2c(c, (long long)M * cm, c->sA, c->sAh + (size_t)(m0 - n0) * M * F, M));
+                    }
+                }
                 ST_TRY(dspec_launch(c, c->sAh, c->G3h, n0, n0 + cn, slot0));
                 slot0 += dspec_nsub(cn, F, c->nsm);
             }
@@ -1112,6 +1159,7 @@ int admm_sync_time_state(cdlgb_ctx* c) {
     if (!c->dspec) return CDLGB_OK;
     if (c->time_init) return write_time_init(c);    // no D-step since the initialisation
     if (!c->time_stale) return CDLGB_OK;
+    ST_TRY(ensure_time_state(c));
     const int M = c->M, Lg = c->Lg, F = c->F;
     const float2* src[3] = {c->Dhs, c->g1h, c->g1h};
     float* dst[3] = {c->d, c->g1, c->g3};

@@ -405,7 +405,11 @@ int dfwd_run(cdlgb_ctx* c, void* p, const float* X, int n0, int cn, float2* Yh, 
     FwdPlan* P = (FwdPlan*)p;
     const size_t off = (size_t)n0 * c->M * c->Lg;
     FArgs a;
-    a.X = X + off; a.y3 = c->y3 + off; a.g1 = c->g1 + off; a.g3 = c->g3 + off; a.d = c->d + off;
+    // g1, g3, d are read only for H-hat and d-hat (the time-domain D-step, where they exist)
+    a.X = X + off; a.y3 = c->y3 + off;
+    a.g1 = c->g1 ? c->g1 + off : nullptr;
+    a.g3 = c->g3 ? c->g3 + off : nullptr;
+    a.d = c->d ? c->d + off : nullptr;
     a.G1 = c->G1; a.G3 = c->G3; a.Yh = Yh; a.Hh = Hh; a.Dh = Dh; a.tw2 = P->tw2;
     a.cn = cn; a.M = c->M;
     P->k<<<P->grid, 256, P->smem, c->stream>>>(a);

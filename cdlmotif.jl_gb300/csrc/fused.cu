@@ -523,7 +523,11 @@ size_t smem_bytes(int Lg, int F, int Mc) {
     return (2 * NS * Lg + Lg + 3 * Fp) * sizeof(float2) + (size_t)Lg * sizeof(float);
 }
 
-constexpr size_t kSmemCap = 110 * 1024;   // two CTAs per SM
+// Two CTAs per SM.  Longer transforms whose layout needs one CTA per SM (Lg = 2128 at
+// K = 32 fits 216 KB at four CTAs per cluster) ran slower on this kernel than on the
+// cuFFT-transform path (100 against 82 ms per outer iteration at N = 5000), so they
+// are left to that path.
+constexpr size_t kSmemCap = 110 * 1024;
 
 bool choose_cluster(int Lg, int M, int* CS, int* Mc) {
     int F = Lg / 2 + 1;

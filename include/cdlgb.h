@@ -135,7 +135,10 @@ int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out);
 int cdlgb_destroy(cdlgb_ctx* ctx);
 const char* cdlgb_last_error(const cdlgb_ctx* ctx);
 
-/* Device memory a dataset of N sequences x L bases needs, for admission control. */
+/* Device memory a dataset of N sequences x L bases needs, for admission control.  Where
+ * the D-step keeps d, g1, g3 as half-spectra (the default for M <= 128), their
+ * time-domain copies (3 x 4 Lg M N bytes) are allocated only when first read through
+ * cdlgb_get and are not counted here. */
 int cdlgb_footprint(const cdlgb_params* p, int32_t L, int32_t N, uint64_t* bytes);
 
 /* Upload the one-hot data matrix (4L, N) col-major (dna2dummy layout,

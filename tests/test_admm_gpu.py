@@ -180,10 +180,12 @@ def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
         assert rel(c.DX[:, g:g + L4], ref.DX[:, g:g + L4]) < 10 * TOL_X
 
 
-@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12)])
+@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12), (5, 100, 16, 16), (4, 30, 5, 3)])
 def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeypatch):
-    """The D-step with d, g1, g3 held as half-spectra (the default where the streaming
-    transforms exist) against the same D-step in the time domain (CDLGB_DSPEC=0) and
+    """The D-step with d, g1, g3 held as half-spectra (the default on the fused path:
+    Y3 transformed by the streaming register-FFT kernels, or for the other lengths --
+    Lg = 528 = 2^4 3 11 and 144 = 2^4 3^2 here -- formed in the time domain and
+    transformed by cuFFT) against the same D-step in the time domain (CDLGB_DSPEC=0) and
     the FP64 oracle after 3 outer iterations.  The two run the same statements with
     different FP32 rounding, which the ADMM amplifies by itself (the FP32-ordered oracle
     drifts ~1e-4 from FP64 in 2-3 outer iterations): the objectives agree to 1e-5, and
@@ -236,6 +238,41 @@ def test_multi_iteration_other_lengths(pkg, built_lib, L, M):
     with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=2) as c:
         kinds = [x["kernel"] for x in c.autotune()["candidates"]]
         assert "multi-iteration" in kinds
+
+
+@pytest.mark.parametrize("L,M,fused", [(500, 32, False), (100, 32, True)])
+def test_lengths_without_register_ffts(pkg, built_lib, monkeypatch, L, M, fused):
+    """Lengths without a register-FFT variant, as the automatic choice runs them, with
+    the D-step on the spectral state (Y3 formed in the time domain and transformed by
+    cuFFT): Lg = 528 = 2^4 3 11 on the generic in-kernel-FFT X-step, Lg = 2128 = 2^4 7 19
+    (whose generic layout would need one CTA per SM) on the cuFFT-transform X-step.  2
+    outer iterations on 3 sequences against the FP64 oracle at the stated tolerance
+    (DX and Td, derived fields, at 10x), and against the time-domain D-step
+    (CDLGB_DSPEC=0), which takes another path (other bits) to the same tolerance."""
+    fs, N = 16, 3
+    synth = pkg.synth
+    bases, _, _ = synth.plant_dataset(23, N, L, [8, 12], [0.4, 0.4])
+    S = synth.onehot(bases)
+    Lg = 4 * L + 8 * fs
+    X0 = synth.init_X0(6, N, M, Lg)
+    D0 = synth.init_D0_unit_norm(6, M, Lg, 4 * fs)
+    ref = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    objs_ref = O.run_outer(ref, 2)
+    out = {}
+    for spec in ("1", "0"):
+        monkeypatch.setenv("CDLGB_DSPEC", spec)
+        with pkg.init_cdl(_setup(pkg, M, fs, 0.1, 1.0, 100.0), S, X0=X0, D0=D0, fft_mode=0) as c:
+            c.profile(True)
+            objs = pkg.run_outer(c, 2)
+            np.testing.assert_allclose(objs, objs_ref, rtol=TOL_OBJ)
+            for f, tol in (("X", TOL_X), ("d", TOL_X), ("G1", TOL_X), ("D_best", TOL_X),
+                           ("DX", 10 * TOL_X), ("Td", 10 * TOL_X)):
+                assert rel(getattr(c, f), getattr(ref, f)) < tol, (spec, f)
+            pr = c.profile_read()
+            assert pr["xstep"][1] > 0
+            assert pr["xfused"][1] == (pr["xstep"][1] if fused else 0)
+            out[spec] = c.d
+    assert not np.array_equal(out["1"], out["0"])
 
 
 @pytest.mark.parametrize("shape", [(5, 200, 64, 16, "4"), (5, 200, 64, 16, "8"),

@@ -80,6 +80,33 @@ struct XArgs {
 };
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+
+// L2 prefetch of the rows the CTA reads for sequence n (its Mc filter rows of X, y2,
+// y3; rank 0 also Y1, y1, DX and the W'S window), issued by the 32 lanes of one warp
+// while the current sequence is transformed.  Bulk prefetches are hints: nothing waits
+// on them.  Every row is a multiple of 16 bytes long (Lg and L4 are multiples of 4
+// floats); a base pointer that is not 16-byte aligned skips the hint.
+__device__ __forceinline__ void l2_hint(const void* p, unsigned bytes) {
+    if (((uintptr_t)p & 15) == 0)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void prefetch_sequence(const XArgs& A, int n, int m0, int rank, int lane) {
+    if (n >= A.N) return;
+    const unsigned rb = (unsigned)A.Lg * 4u;
+    const size_t r0 = ((size_t)n * A.M + m0) * A.Lg;
+    const int rows = 3 * A.Mc, extra = rank == 0 ? 4 : 0;
+    for (int q = lane; q < rows + extra; q += 32) {
+        if (q < rows) {
+            const float* base = q < A.Mc ? A.Xin : q < 2 * A.Mc ? A.y2 : A.y3;
+            l2_hint(base + r0 + (size_t)(q % A.Mc) * A.Lg, rb);
+        } else if (q < rows + 3) {
+            const float* base = q == rows ? A.Y1 : q == rows + 1 ? A.y1 : A.DX;
+            l2_hint(base + (size_t)n * A.Lg, rb);
+        } else {
+            l2_hint(A.S + (size_t)n * A.L4, (unsigned)A.L4 * 4u);
+        }
+    }
+}
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return f2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -348,6 +375,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_xstep_fused(XArgs A) {
         }
         __syncthreads();
 
+        // the next sequence's rows into L2 while this one is transformed
+        if (threadIdx.x >= 32 && threadIdx.x < 64)
+            prefetch_sequence(A, n + nclusters, m0, rank, threadIdx.x & 31);
+
         // ---- 2. forward FFTs
         float2* R = fft_all<-1>(bufA, bufB, NS, Lg, fac, A.nfac, tws);
         float2* other = (R == bufA) ? bufB : bufA;
@@ -529,10 +560,14 @@ size_t smem_bytes(int Lg, int F, int Mc) {
 // are left to that path.
 constexpr size_t kSmemCap = 110 * 1024;
 
+// The smallest cluster whose CTAs fit two per SM; CDLGB_CLUSTER forces a cluster size
+// (when it fits), as for the register-FFT kernels.
 bool choose_cluster(int Lg, int M, int* CS, int* Mc) {
     int F = Lg / 2 + 1;
+    int want = 0;
+    if (const char* e = getenv("CDLGB_CLUSTER")) want = atoi(e);
     for (int cs : {1, 2, 4, 8}) {
-        if (M % cs) continue;
+        if (M % cs || (want && cs != want)) continue;
         int mc = M / cs;
         if (smem_bytes(Lg, F, mc) <= kSmemCap) { *CS = cs; *Mc = mc; return true; }
     }

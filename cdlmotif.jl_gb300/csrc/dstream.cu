@@ -328,6 +328,7 @@ struct Variant { int N1, P; kern_t k; kinv_t ki; kr2c_t kf; kc2r_t kb; };
 const Variant kVariants[] = {
     DSTREAM_VARIANT(32, 29),
     DSTREAM_VARIANT(16, 31),
+    DSTREAM_VARIANT(16, 33),
     DSTREAM_VARIANT(32, 17),
     DSTREAM_VARIANT(32, 19),
     DSTREAM_VARIANT(32, 23),

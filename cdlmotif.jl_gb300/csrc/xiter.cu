@@ -428,6 +428,8 @@ const Variant kVariants[] = {
      k_xiter<32, 29, 160, 2, 8, true>},
     {16, 31, 16, 160, 2, k_xiter<16, 31, 160, 2, 16, false>,
      k_xiter<16, 31, 160, 2, 16, true>},
+    {16, 33, 16, 160, 2, k_xiter<16, 33, 160, 2, 16, false>,
+     k_xiter<16, 33, 160, 2, 16, true>},
     {32, 17, 16, 288, 1, k_xiter<32, 17, 288, 1, 16, false>,
      k_xiter<32, 17, 288, 1, 16, true>},
     {32, 19, 16, 288, 1, k_xiter<32, 19, 288, 1, 16, false>,

@@ -180,11 +180,12 @@ def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
         assert rel(c.DX[:, g:g + L4], ref.DX[:, g:g + L4]) < 10 * TOL_X
 
 
-@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12), (5, 100, 16, 16), (4, 30, 5, 3)])
+@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12), (5, 100, 16, 16),
+                                   (5, 120, 16, 12), (4, 30, 5, 3)])
 def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeypatch):
     """The D-step with d, g1, g3 held as half-spectra (the default on the fused path:
-    Y3 transformed by the streaming register-FFT kernels, or for the other lengths --
-    Lg = 528 = 2^4 3 11 and 144 = 2^4 3^2 here -- formed in the time domain and
+    Y3 transformed by the streaming register-FFT kernels -- Lg = 928, 496 and 528 here --
+    or for the other lengths -- Lg = 576 = 2^6 3^2 and 144 = 2^4 3^2 -- formed in the time domain and
     transformed by cuFFT) against the same D-step in the time domain (CDLGB_DSPEC=0) and
     the FP64 oracle after 3 outer iterations.  The two run the same statements with
     different FP32 rounding, which the ADMM amplifies by itself (the FP32-ordered oracle
@@ -216,11 +217,12 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
         assert rel(out["1"][f], out["0"][f]) < 2 * env, f
 
 
-@pytest.mark.parametrize("L,M", [(104, 32), (120, 32), (152, 64), (216, 32)])
+@pytest.mark.parametrize("L,M", [(104, 32), (120, 32), (152, 64), (216, 32), (100, 32)])
 def test_multi_iteration_other_lengths(pkg, built_lib, L, M):
     """The multi-iteration kernel at the other register-FFT lengths Lg = 32 P (P = 17,
-    19, 23, 31; W = 16): it is among the candidates for the shape, and 2 outer
-    iterations on 5 sequences match the FP64 oracle at the stated tolerance."""
+    19, 23, 31) and 16 x 33 (a composite per-lane DFT length; W = 16): it is among the
+    candidates for the shape, and 2 outer iterations on 5 sequences match the FP64
+    oracle at the stated tolerance."""
     fs = 16
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(17, 5, L, [8, 12], [0.4, 0.4])
@@ -240,16 +242,16 @@ def test_multi_iteration_other_lengths(pkg, built_lib, L, M):
         assert "multi-iteration" in kinds
 
 
-@pytest.mark.parametrize("L,M,fused", [(500, 32, False), (100, 32, True)])
-def test_lengths_without_register_ffts(pkg, built_lib, monkeypatch, L, M, fused):
+@pytest.mark.parametrize("L,M,fs,fused", [(500, 32, 16, False), (120, 32, 12, True)])
+def test_lengths_without_register_ffts(pkg, built_lib, monkeypatch, L, M, fs, fused):
     """Lengths without a register-FFT variant, as the automatic choice runs them, with
     the D-step on the spectral state (Y3 formed in the time domain and transformed by
-    cuFFT): Lg = 528 = 2^4 3 11 on the generic in-kernel-FFT X-step, Lg = 2128 = 2^4 7 19
+    cuFFT): Lg = 576 = 2^6 3^2 on the generic in-kernel-FFT X-step, Lg = 2128 = 2^4 7 19
     (whose generic layout would need one CTA per SM) on the cuFFT-transform X-step.  2
     outer iterations on 3 sequences against the FP64 oracle at the stated tolerance
     (DX and Td, derived fields, at 10x), and against the time-domain D-step
     (CDLGB_DSPEC=0), which takes another path (other bits) to the same tolerance."""
-    fs, N = 16, 3
+    N = 3
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(23, N, L, [8, 12], [0.4, 0.4])
     S = synth.onehot(bases)

@@ -17,16 +17,19 @@
 
 namespace {
 
-// cos/sin(2 pi m / p) for the per-lane DFT lengths p (the odd primes 3..31 and 33: the
-// symmetric direct DFT-P below needs P odd, not prime), concatenated; exp(-2 pi i j / 32)
-__constant__ float2 c_trigw[3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33];
+// cos/sin(2 pi m / p) for the per-lane DFT lengths p (the odd primes 3..31 and the odd
+// composites 21, 25, 27, 33: the symmetric direct DFT-P below needs P odd, not prime),
+// concatenated; exp(-2 pi i j / 32)
+const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 33, 21, 25, 27};
+constexpr int kTrigW = 3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33 + 21 + 25 + 27;
+__constant__ float2 c_trigw[kTrigW];
 __constant__ float2 c_w32[32];
 
 __host__ __device__ constexpr int toff(int p) {
     return p == 3 ? 0 : p == 5 ? 3 : p == 7 ? 8 : p == 11 ? 15 : p == 13 ? 26 : p == 17 ? 39
-         : p == 19 ? 56 : p == 23 ? 75 : p == 29 ? 98 : p == 31 ? 127 : p == 33 ? 158 : -1;
+         : p == 19 ? 56 : p == 23 ? 75 : p == 29 ? 98 : p == 31 ? 127 : p == 33 ? 158
+         : p == 21 ? 191 : p == 25 ? 212 : p == 27 ? 237 : -1;
 }
-const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 33};
 
 __host__ __device__ constexpr int brev(int k, int bits) {
     int r = 0;
@@ -391,7 +394,7 @@ inline cudaError_t regfft_upload_tables() {
     if (e0 != cudaSuccess) return e0;
     std::lock_guard<std::mutex> lk(mu);
     if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
-    std::vector<float2> trig(3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33);
+    std::vector<float2> trig(kTrigW);
     for (int p : kPrimesW)
         for (int m = 0; m < p; ++m)
             trig[toff(p) + m] = make_float2((float)cos(2.0 * M_PI * m / p), (float)sin(2.0 * M_PI * m / p));

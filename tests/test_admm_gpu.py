@@ -217,13 +217,15 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
         assert rel(out["1"][f], out["0"][f]) < 2 * env, f
 
 
-@pytest.mark.parametrize("L,M", [(104, 32), (120, 32), (152, 64), (216, 32), (100, 32)])
-def test_multi_iteration_other_lengths(pkg, built_lib, L, M):
-    """The multi-iteration kernel at the other register-FFT lengths Lg = 32 P (P = 17,
-    19, 23, 31) and 16 x 33 (a composite per-lane DFT length; W = 16): it is among the
-    candidates for the shape, and 2 outer iterations on 5 sequences match the FP64
-    oracle at the stated tolerance."""
-    fs = 16
+@pytest.mark.parametrize("L,M,fs", [(104, 32, 16), (120, 32, 16), (152, 64, 16), (216, 32, 16),
+                                    (100, 32, 16), (52, 32, 16), (68, 16, 16), (100, 32, 4),
+                                    (136, 32, 16), (168, 64, 16), (184, 32, 16)])
+def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
+    """The multi-iteration kernel at the other register-FFT lengths Lg = 4L + 8W:
+    32 P for P = 17, 19, 23, 31 and the odd composites 21, 25, 27 (Lg = 672, 800, 864),
+    16 P for P = 33, 21, 25 and 27 (Lg = 528, 336, 400; 432 = L 100 at the reference's
+    default W = 4): it is among the candidates for the shape, and 2 outer iterations on
+    5 sequences match the FP64 oracle at the stated tolerance."""
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(17, 5, L, [8, 12], [0.4, 0.4])
     S = synth.onehot(bases)

@@ -548,9 +548,11 @@ def run_interference(args, n_small: int = 5):
                        "small": {"N": 1000, "L": 200, "K": 32, "outer_iterations": 3}}}
 
 
-def run_lengths(args, Ls=(100, 200, 500), N: int = 5000, K: int = 32, outer: int = 3):
+def run_lengths(args, shapes=((100, 16), (200, 16), (500, 16), (200, 4)), N: int = 5000, K: int = 32,
+                outer: int = 3):
     """Per transform length: the batched mix's lengths (L = 100, 200, 500 with W = 16:
-    Lg = 528, 928, 2128) on N = 5000 sequences with K = 32 filters, `outer` timed outer
+    Lg = 528, 928, 2128) and L = 200 at the reference's default W = 4 (Lg = 832) on
+    N = 5000 sequences with K = 32 filters, `outer` timed outer
     iterations after one untimed: outer iterations/s, the X-step and D-step device time
     per outer iteration from the library's phase timers, and the kernel path each length
     takes (register-FFT lengths run the multi-iteration X-step and the spectral D-step
@@ -560,8 +562,8 @@ def run_lengths(args, Ls=(100, 200, 500), N: int = 5000, K: int = 32, outer: int
     pkg = _pkg()
     peak = measured_hbm_peak()
     out = []
-    for L in Ls:
-        wl = dict(WORKLOAD, N=N, L=L, M=K, name=f"len_n{N}_l{L}_k{K}")
+    for L, W in shapes:
+        wl = dict(WORKLOAD, N=N, L=L, M=K, filter_size=W, name=f"len_n{N}_l{L}_w{W}_k{K}")
         S = pkg.synth.onehot(dataset(wl))
         setup = pkg.CDLSetup(M=K, filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
                              sigma=wl["sigma"])
@@ -577,7 +579,7 @@ def run_lengths(args, Ls=(100, 200, 500), N: int = 5000, K: int = 32, outer: int
             sec = time.perf_counter() - t0
             pr = c.profile_read()
             xs, ds = pr["xstep"][0] / outer, pr["dstep"][0] / outer
-            out.append({"L": L, "Lg": ab["Lg"], "N": N, "K": K, "outer_iter_per_s": outer / sec,
+            out.append({"L": L, "W": W, "Lg": ab["Lg"], "N": N, "K": K, "outer_iter_per_s": outer / sec,
                         "xstep_ms_per_outer": xs, "dstep_ms_per_outer": ds,
                         "objective_ms_per_outer": pr["objective"][0] / outer,
                         "xstep_frac_of_hbm_peak": (15 * ab["xstep"] / (xs / 1e3)) / (peak * 1e9) if xs else None,
@@ -587,7 +589,7 @@ def run_lengths(args, Ls=(100, 200, 500), N: int = 5000, K: int = 32, outer: int
     return {"metric": "outer iterations/s per transform length (N=5000, K=32, W=16)",
             "value": None, "unit": "outer_iter/s", "lengths": out, "hbm_peak_gbs": peak,
             "dtype": "f32", "data": "synthetic (seeded planted motifs)",
-            "config": {"workload": "lengths", "L": list(Ls), "N": N, "K": K}}
+            "config": {"workload": "lengths", "L_W": [list(x) for x in shapes], "N": N, "K": K}}
 
 
 def search_inputs(wl=WORKLOAD, K=32, N=None):

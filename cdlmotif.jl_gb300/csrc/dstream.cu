@@ -19,6 +19,7 @@ namespace dstream {
 const Variant* variants_1(int* n);
 const Variant* variants_2(int* n);
 const Variant* variants_3(int* n);
+const Variant* variants_4(int* n);
 }  // namespace dstream
 
 namespace {
@@ -34,7 +35,7 @@ using dstream::kc2r_t;
 const std::vector<Variant>& all_variants() {
     static const std::vector<Variant> all = [] {
         std::vector<Variant> v;
-        for (auto f : {dstream::variants_1, dstream::variants_2, dstream::variants_3}) {
+        for (auto f : {dstream::variants_1, dstream::variants_2, dstream::variants_3, dstream::variants_4}) {
             int n = 0;
             const Variant* p = f(&n);
             v.insert(v.end(), p, p + n);

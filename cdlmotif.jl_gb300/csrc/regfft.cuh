@@ -17,18 +17,19 @@
 
 namespace {
 
-// cos/sin(2 pi m / p) for the per-lane DFT lengths p (the odd primes 3..31 and the odd
-// composites 21, 25, 27, 33: the symmetric direct DFT-P below needs P odd, not prime),
-// concatenated; exp(-2 pi i j / 32)
-const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 33, 21, 25, 27};
-constexpr int kTrigW = 3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33 + 21 + 25 + 27;
+// cos/sin(2 pi m / p) for the per-lane DFT lengths p (the odd primes 3..31, the odd
+// composites 21, 25, 27, 33 and the even 26, 28, 30: the symmetric direct DFT-P below
+// needs no prime), concatenated; exp(-2 pi i j / 32)
+const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 33, 21, 25, 27, 26, 28, 30};
+constexpr int kTrigW = 3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33 + 21 + 25 + 27 + 26 + 28 + 30;
 __constant__ float2 c_trigw[kTrigW];
 __constant__ float2 c_w32[32];
 
 __host__ __device__ constexpr int toff(int p) {
     return p == 3 ? 0 : p == 5 ? 3 : p == 7 ? 8 : p == 11 ? 15 : p == 13 ? 26 : p == 17 ? 39
          : p == 19 ? 56 : p == 23 ? 75 : p == 29 ? 98 : p == 31 ? 127 : p == 33 ? 158
-         : p == 21 ? 191 : p == 25 ? 212 : p == 27 ? 237 : -1;
+         : p == 21 ? 191 : p == 25 ? 212 : p == 27 ? 237 : p == 26 ? 264 : p == 28 ? 290
+         : p == 30 ? 318 : -1;
 }
 
 __host__ __device__ constexpr int brev(int k, int bits) {
@@ -110,54 +111,32 @@ __device__ __forceinline__ void dft_reg(float2 (&x)[N]) {
     }
 }
 
-// Forward step 1, in place on this lane's column of the group buffer: inputs
-// z[n2] at T[n2][n1], DFT-P over n2, twiddle by w_Lg^(n1 k2), outputs at T[k2][n1].
-template <int N1, int P>
-__device__ __forceinline__ void fwd_step1(float2* __restrict__ T, int n1,
-                                          const float2* __restrict__ tw2) {
-    constexpr int H = (P - 1) / 2;
-    constexpr int OFF = toff(P);
-    constexpr int RS = N1 + 1;
-    float2 x0 = T[n1];
-    float2 s[H], d[H];
-    float2 y0 = x0;
-#pragma unroll
-    for (int j = 1; j <= H; ++j) {
-        float2 a = T[j * RS + n1], b = T[(P - j) * RS + n1];
-        s[j - 1] = cadd(a, b);
-        d[j - 1] = csub(a, b);
-        y0 = cadd(y0, s[j - 1]);
-    }
-    T[n1] = y0;
-#pragma unroll
-    for (int k = 1; k <= H; ++k) {
-        float2 A = x0, B = f2(0.f, 0.f);
-#pragma unroll
-        for (int j = 1; j <= H; ++j) {
-            const float2 cs = c_trigw[OFF + (j * k) % P];
-            A = rfma(s[j - 1], cs.x, A);
-            B = rfma(d[j - 1], cs.y, B);
-        }
-        float2 ib = mul_i<-1>(B);
-        T[k * RS + n1] = cmul(cadd(A, ib), tw2[k * N1 + n1]);
-        T[(P - k) * RS + n1] = cmul(csub(A, ib), tw2[(P - k) * N1 + n1]);
-    }
-}
-
-// Inverse step 1, in place on this lane's column: inputs T[k2][n1] (already
-// twiddled), inverse DFT-P over k2, outputs x[n1 + N1 n2] at T[n2][n1].
-// With TW, the conjugate twiddles are applied here, as the inputs are loaded, instead
-// of by inv_step2 (the same products, so the same bits).
-template <int N1, int P, bool TW = false>
-__device__ __forceinline__ void inv_step1(float2* __restrict__ T, int n1,
-                                          const float2* __restrict__ tw2 = nullptr) {
-    constexpr int H = (P - 1) / 2;
+// The per-lane DFT-P over a column (SIGN -1 forward, +1 inverse), in the symmetric
+// direct form: x_j and x_{P-j} enter as s_j = x_j + x_{P-j} and d_j = x_j - x_{P-j},
+// output k and P - k share A = x0 + sum_j s_j cos(2 pi j k / P) and
+// B = sum_j d_j sin(2 pi j k / P), X[k] = A + SIGN i B and X[P-k] = A - SIGN i B.  For
+// an even P the middle input x_{P/2} enters A with the sign (-1)^k (as e = x0 + x_{P/2}
+// or o = x0 - x_{P/2}), and the outputs 0 and P/2 are e + sum_j s_j and
+// (-1)^{P/2} part + sum_j (-1)^j s_j.  Inputs z[n2] at T[n2][n1]; with TW (inverse) the
+// conjugate twiddles are applied as the inputs are loaded; with OTW (forward) the
+// outputs are multiplied by the twiddles w_Lg^(n1 k2) as they are stored.
+template <int N1, int P, int SIGN, bool TW, bool OTW>
+__device__ __forceinline__ void dft_p_col(float2* __restrict__ T, int n1, const float2* __restrict__ tw2) {
+    constexpr bool EVEN = (P % 2) == 0;
+    constexpr int H = EVEN ? P / 2 - 1 : (P - 1) / 2;
     constexpr int OFF = toff(P);
     constexpr int RS = N1 + 1;
     float2 x0 = T[n1];
     if (TW) x0 = cmulc(x0, tw2[n1]);
+    float2 e = x0, o = x0;
+    if (EVEN) {
+        float2 xh = T[(P / 2) * RS + n1];
+        if (TW) xh = cmulc(xh, tw2[(P / 2) * N1 + n1]);
+        e = cadd(x0, xh);
+        o = csub(x0, xh);
+    }
     float2 s[H], d[H];
-    float2 y0 = x0;
+    float2 y0 = e;
 #pragma unroll
     for (int j = 1; j <= H; ++j) {
         float2 a = T[j * RS + n1], b = T[(P - j) * RS + n1];
@@ -170,19 +149,48 @@ __device__ __forceinline__ void inv_step1(float2* __restrict__ T, int n1,
         y0 = cadd(y0, s[j - 1]);
     }
     T[n1] = y0;
+    if (EVEN) {
+        float2 ym = ((P / 2) % 2 == 0) ? e : o;
+#pragma unroll
+        for (int j = 1; j <= H; ++j) ym = (j % 2) ? csub(ym, s[j - 1]) : cadd(ym, s[j - 1]);
+        T[(P / 2) * RS + n1] = OTW ? cmul(ym, tw2[(P / 2) * N1 + n1]) : ym;
+    }
 #pragma unroll
     for (int k = 1; k <= H; ++k) {
-        float2 A = x0, B = f2(0.f, 0.f);
+        float2 A = (EVEN && (k % 2)) ? o : e, B = f2(0.f, 0.f);
 #pragma unroll
         for (int j = 1; j <= H; ++j) {
             const float2 cs = c_trigw[OFF + (j * k) % P];
             A = rfma(s[j - 1], cs.x, A);
             B = rfma(d[j - 1], cs.y, B);
         }
-        float2 ib = mul_i<1>(B);
-        T[k * RS + n1] = cadd(A, ib);
-        T[(P - k) * RS + n1] = csub(A, ib);
+        float2 ib = mul_i<SIGN>(B);
+        if (OTW) {
+            T[k * RS + n1] = cmul(cadd(A, ib), tw2[k * N1 + n1]);
+            T[(P - k) * RS + n1] = cmul(csub(A, ib), tw2[(P - k) * N1 + n1]);
+        } else {
+            T[k * RS + n1] = cadd(A, ib);
+            T[(P - k) * RS + n1] = csub(A, ib);
+        }
     }
+}
+
+// Forward step 1, in place on this lane's column of the group buffer: inputs
+// z[n2] at T[n2][n1], DFT-P over n2, twiddle by w_Lg^(n1 k2), outputs at T[k2][n1].
+template <int N1, int P>
+__device__ __forceinline__ void fwd_step1(float2* __restrict__ T, int n1,
+                                          const float2* __restrict__ tw2) {
+    dft_p_col<N1, P, -1, false, true>(T, n1, tw2);
+}
+
+// Inverse step 1, in place on this lane's column: inputs T[k2][n1] (already
+// twiddled), inverse DFT-P over k2, outputs x[n1 + N1 n2] at T[n2][n1].
+// With TW, the conjugate twiddles are applied here, as the inputs are loaded, instead
+// of by inv_step2 (the same products, so the same bits).
+template <int N1, int P, bool TW = false>
+__device__ __forceinline__ void inv_step1(float2* __restrict__ T, int n1,
+                                          const float2* __restrict__ tw2 = nullptr) {
+    dft_p_col<N1, P, 1, TW, false>(T, n1, tw2);
 }
 
 // Forward step 2: rows of T -> DFT-N1 -> natural-order spectrum Z (same buffer).

@@ -70,13 +70,13 @@ struct cdlgb_server {
 namespace {
 
 // the padded length of the serving form: the smallest L' >= L whose transform length
-// 4L' + 8W is one the multi-iteration X-step kernel covers (xiter.cu: 16 x P, P = 21, 25,
-// 27, 31, 33, and 32 x P, P = 17, 19, 21, 23, 25, 27, 29, 31) if that costs at most 8 %
-// more transform columns, else the
+// 4L' + 8W is one the multi-iteration X-step kernel covers (16 x P and 32 x P for the
+// per-lane lengths of xiter_v*.cu) if that costs at most 8 % more transform columns, else the
 // smallest whose transform length is a multiple of 16 with prime factors <= 31 (the
 // generic in-kernel FFTs)
 int friendly_L(int L, int fs) {
-    static const int kRegLg[] = {336, 400, 432, 496, 528, 544, 608, 672, 736, 800, 864, 928, 992};
+    static const int kRegLg[] = {336, 400, 416, 432, 448, 480, 496, 528, 544, 608, 672, 736,
+                                 800, 832, 864, 896, 928, 960, 992};
     const int lg = 4 * L + 8 * fs;
     for (int n : kRegLg)
         if (lg <= n && n <= 1.08 * lg && (n - 8 * fs) % 4 == 0) return (n - 8 * fs) / 4;

@@ -27,6 +27,8 @@ const Variant* variants_1(int* n);
 const Variant* variants_2(int* n);
 const Variant* variants_3(int* n);
 const Variant* variants_4(int* n);
+const Variant* variants_5(int* n);
+const Variant* variants_6(int* n);
 }  // namespace xiter
 
 namespace {
@@ -38,12 +40,13 @@ constexpr size_t kCap2 = 115200;       // two CTAs per SM (2 x (this + 1 KB rese
 constexpr size_t kCap1 = 220 * 1024;   // one CTA per SM
 
 // in order of preference (measured at L=200, K=64: 16 filters per CTA, one CTA per SM,
-// 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms).  At W = 16 (Lg =
-// 4L + 8W) the lengths cover L = 52, 68, 76, 92, 100, 104, 120, 136, 152, 168, 184, 200, 216.
+// 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms).  Lg = 16 P and 32 P
+// for P = 17..33 (every odd P from 21 and the even 26, 28, 30; Lg = 4L + 8W).
 const std::vector<Variant>& all_variants() {
     static const std::vector<Variant> all = [] {
         std::vector<Variant> v;
-        for (auto f : {xiter::variants_1, xiter::variants_2, xiter::variants_3, xiter::variants_4}) {
+        for (auto f : {xiter::variants_1, xiter::variants_2, xiter::variants_3, xiter::variants_4,
+                       xiter::variants_5, xiter::variants_6}) {
             int n = 0;
             const Variant* p = f(&n);
             v.insert(v.end(), p, p + n);

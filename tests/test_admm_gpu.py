@@ -219,13 +219,17 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
 
 @pytest.mark.parametrize("L,M,fs", [(104, 32, 16), (120, 32, 16), (152, 64, 16), (216, 32, 16),
                                     (100, 32, 16), (52, 32, 16), (68, 16, 16), (100, 32, 4),
-                                    (136, 32, 16), (168, 64, 16), (184, 32, 16)])
+                                    (136, 32, 16), (168, 64, 16), (184, 32, 16),
+                                    (200, 32, 4), (200, 32, 12), (208, 64, 16), (96, 32, 4),
+                                    (104, 16, 4), (88, 32, 16)])
 def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
     """The multi-iteration kernel at the other register-FFT lengths Lg = 4L + 8W:
     32 P for P = 17, 19, 23, 31 and the odd composites 21, 25, 27 (Lg = 672, 800, 864),
     16 P for P = 33, 21, 25 and 27 (Lg = 528, 336, 400; 432 = L 100 at the reference's
-    default W = 4): it is among the candidates for the shape, and 2 outer iterations on
-    5 sequences match the FP64 oracle at the stated tolerance."""
+    default W = 4), and the even per-lane lengths P = 26, 28, 30: 32 P = 832 (L 200 at
+    W = 4), 896 (L 200 at W = 12), 960, and 16 P = 416, 448, 480: it is among the
+    candidates for the shape, and 2 outer iterations on 5 sequences match the FP64
+    oracle at the stated tolerance."""
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(17, 5, L, [8, 12], [0.4, 0.4])
     S = synth.onehot(bases)

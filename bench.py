@@ -818,6 +818,8 @@ def main():
     ap.add_argument("--batched-n", type=int, default=64)
     ap.add_argument("--lengths", action="store_true",
                     help="outer iterations/s and phase times at the batched mix's transform lengths")
+    ap.add_argument("--length-shapes", default="100:16,200:16,500:16,200:4",
+                    help="L:W pairs for --lengths")
     ap.add_argument("--interference", action="store_true",
                     help="GPU time a running training loses per dataset trained beside it")
     ap.add_argument("--precision", action="store_true",
@@ -863,7 +865,8 @@ def main():
         return
     if args.lengths:
         if rank == 0:
-            print(json.dumps(run_lengths(args)))
+            shapes = tuple(tuple(int(v) for v in x.split(":")) for x in args.length_shapes.split(","))
+            print(json.dumps(run_lengths(args, shapes=shapes)))
         return
     if args.interference:
         if rank == 0:

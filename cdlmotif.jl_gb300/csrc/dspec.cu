@@ -68,18 +68,23 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
     const bool on = f < F;
     const bool edge = f == 0 || f == F - 1;
     float2* G1s = reinterpret_cast<float2*>(sm4);          // [M][32]
-    float2* G3s = G1s + (size_t)M * kBins;                 // [M][32]
-    float2* Dgs = G3s + (size_t)M * kBins;                 // [M][32]
+    // Ks = G1-hat + G3-hat + Dg: H = (G1 - g1) + (G3 - g3) with g3 = g1 - Dg is
+    // Ks - 2 g1, one shared spectrum instead of three (G3s is kept for the residuals)
+    float2* Ks = G1s + (size_t)M * kBins;                  // [M][32]
+    float2* G3s = Ks + (size_t)M * kBins;                  // [M][32]
     // the warps' partial sums of B, Q.x, Q.y, T.x, T.y per bin, [5][kWarps][32], and
     // their totals, [5][32]: each total is summed once, by one thread, in warp order
-    float* pp = reinterpret_cast<float*>(Dgs + (size_t)M * kBins);
+    float* pp = reinterpret_cast<float*>(G3s + (size_t)M * kBins);
     float* tot = pp + 5 * kWarps * kBins;
     for (int i = threadIdx.x; i < M * kBins; i += blockDim.x) {
         const int m = i / kBins, ff = blockIdx.x * kBins + i % kBins;
         const bool in = ff < F;
-        G1s[i] = in ? A.G1h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
-        G3s[i] = in ? A.G3h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
-        Dgs[i] = in ? A.Dg[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        const float2 g1 = in ? A.G1h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        const float2 g3 = in ? A.G3h[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        const float2 dg = in ? A.Dg[(size_t)m * F + ff] : make_float2(0.f, 0.f);
+        G1s[i] = g1;
+        G3s[i] = g3;
+        Ks[i] = cadd2(cadd2(g1, g3), dg);
     }
     float2 s1[MW], sd[MW];
 #pragma unroll
@@ -152,9 +157,8 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             const float2 y = use ? yv[k] : make_float2(0.f, 0.f);
             float2 d = use ? dv[k] : make_float2(0.f, 0.f);
             if (edge) d.y = 0.f;
-            // H = (G1 - g1) + (G3 - g3) with g3 = g1 - Dg  (train.jl:52-54)
-            const float2 g3 = csub2(g1v[k], Dgs[ms * kBins + lane]);
-            const float2 h = use ? cadd2(csub2(G1s[ms * kBins + lane], g1v[k]), csub2(G3s[ms * kBins + lane], g3))
+            // H = (G1 - g1) + (G3 - g3) with g3 = g1 - Dg  (train.jl:52-54), = Ks - 2 g1
+            const float2 h = use ? csub2(Ks[ms * kBins + lane], cadd2(g1v[k], g1v[k]))
                                  : make_float2(0.f, 0.f);
             hv[k] = h;
             B = fmaf(y.x, y.x, fmaf(y.y, y.y, B));

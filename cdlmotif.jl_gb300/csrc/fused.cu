@@ -606,6 +606,9 @@ static cudaError_t upload_trig_once() {
         for (int m = 0; m < p; ++m)
             trig[trig_off(p) + m] = make_float2((float)cos(2.0 * M_PI * m / p), (float)sin(2.0 * M_PI * m / p));
     e = cudaMemcpyToSymbol(c_trig, trig.data(), trig.size() * sizeof(float2));
+    // the copy may return before it lands; the contexts' streams do not wait on the
+    // legacy stream, so wait for it there
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }

@@ -272,10 +272,14 @@ int cdlgb_ar_record(cdlgb_ar* a, cdlgb_ctx* c, double thresh, int32_t train_num,
         kl[k] = a->filter_lengths[k];
         kt[k] = a->training_num[k];
     }
-    AR_CU(a, cudaMemcpy(a->kmap, km.data(), K * sizeof(int), cudaMemcpyHostToDevice));
-    AR_CU(a, cudaMemcpy(a->klen, kl.data(), K * sizeof(int), cudaMemcpyHostToDevice));
-    AR_CU(a, cudaMemcpy(a->ktrain, kt.data(), K * sizeof(int), cudaMemcpyHostToDevice));
-    AR_CU(a, cudaMemcpy(a->dthresh, a->thresh.data(), a->T * sizeof(float), cudaMemcpyHostToDevice));
+    // on the record's stream, ahead of the kernels that read them (a blocking copy from
+    // pageable memory may return before it lands, and that stream does not wait on the
+    // legacy stream); each call returns once its host bytes are staged
+    AR_CU(a, cudaMemcpyAsync(a->kmap, km.data(), K * sizeof(int), cudaMemcpyHostToDevice, a->stream));
+    AR_CU(a, cudaMemcpyAsync(a->klen, kl.data(), K * sizeof(int), cudaMemcpyHostToDevice, a->stream));
+    AR_CU(a, cudaMemcpyAsync(a->ktrain, kt.data(), K * sizeof(int), cudaMemcpyHostToDevice, a->stream));
+    AR_CU(a, cudaMemcpyAsync(a->dthresh, a->thresh.data(), a->T * sizeof(float), cudaMemcpyHostToDevice,
+                             a->stream));
     if (added) *added = cnt;
     return CDLGB_OK;
 }

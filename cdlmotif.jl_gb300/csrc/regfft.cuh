@@ -410,6 +410,9 @@ inline cudaError_t regfft_upload_tables() {
     for (int j = 0; j < 32; ++j) w32[j] = make_float2((float)cos(2.0 * M_PI * j / 32), (float)-sin(2.0 * M_PI * j / 32));
     cudaError_t e = cudaMemcpyToSymbol(c_trigw, trig.data(), trig.size() * sizeof(float2));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_w32, w32.data(), 32 * sizeof(float2));
+    // a copy from pageable memory may return before it lands, and the contexts' streams
+    // do not wait on the legacy stream: wait for the copies there (not on other streams)
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }

@@ -111,6 +111,66 @@ def test_quirk_scan_position_one_is_not_found():
 
 
 # ------------------------------------------------------------------ scan oracle
+def _stepped_state(seed=3):
+    """A small state one full outer iteration in (d differs from G1 per sequence, the
+    duals are non-zero), for the ordering tests."""
+    rng = np.random.default_rng(seed)
+    N, L, M, fs = 4, 10, 3, 2
+    S, _ = random_onehot(rng, N, L)
+    Lg = 4 * L + 8 * fs
+    X0 = rng.standard_normal((N, M, Lg)).astype(np.float32)
+    D0 = rng.standard_normal((M, Lg)).astype(np.float32)
+    c = O.init_cdl(S, M, fs, 1.0, 100.0, 0.1, X0=X0, D0=D0)
+    O.run_outer(c, 1)
+    return c
+
+
+def test_quirk_xstep_reads_consensus_G1_not_d():
+    """Quirk Q5 (src/CDL/train.jl:18-27): code_update! builds the Sherman-Morrison system
+    from G1-hat, the consensus dictionary, never from the per-sequence copies d: the
+    X-step's result does not move when d and d-hat change, and does when G1-hat does."""
+    import copy
+    base = _stepped_state()
+    a, b, g = copy.deepcopy(base), copy.deepcopy(base), copy.deepcopy(base)
+    b.d = (b.d * 3.0 + 1.0).astype(b.d.dtype)
+    b.dh = np.fft.fft(b.d.astype(np.complex128), axis=-1).astype(b.dh.dtype)
+    g.G1h = (g.G1h * 1.5).astype(g.G1h.dtype)
+    for st in (a, b, g):
+        O.code_update(st, 1)
+    np.testing.assert_array_equal(a.X, b.X)
+    np.testing.assert_array_equal(a.DX, b.DX)
+    assert not np.array_equal(a.X, g.X)
+
+
+def test_quirk_dual_update_ordering():
+    """Quirk Q6 (src/CDL/train.jl:7-14, 35, 40): y1 += DX - Y1 and y3 += X - Y3 use the
+    Y1 and Y3 of the previous X-step (update_Y1! and projectionX! run after the
+    solve), y2 += X - Y2 uses the Y2 that shrink! has just formed from the X and y2
+    entering this X-step."""
+    import copy
+    c = _stepped_state()
+    X0, DX0, Y1o, Y3o = c.X.copy(), c.DX.copy(), c.Y1.copy(), c.Y3.copy()
+    y1o, y2o, y3o = c.y1.copy(), c.y2.copy(), c.y3.copy()
+    Y2n = O.shrink(X0 + y2o, c.lam).astype(c.dtype)                # :7, fresh
+    O.code_update(c, 1)
+    np.testing.assert_array_equal(c.y1, y1o + DX0 - Y1o)           # :12, previous Y1
+    np.testing.assert_array_equal(c.y2, y2o + X0 - Y2n)            # :13, fresh Y2
+    np.testing.assert_array_equal(c.y3, y3o + X0 - Y3o)            # :14, previous Y3
+    assert not np.array_equal(c.Y1, Y1o) and not np.array_equal(c.Y3, Y3o)
+
+
+def test_quirk_td_uses_d_hat_before_the_dictionary_solve():
+    """Quirk Q6, D-step (src/CDL/train.jl:56-60): Td = real(ifft(sum_m Y3-hat d-hat))
+    is formed from d-hat before sherman_CDL_combine replaces it in the same D-step."""
+    c = _stepped_state()
+    Y3h, dh_old = c.Y3h.copy(), c.dh.copy()
+    Td_old = np.real(np.fft.ifft(np.sum(Y3h * dh_old, axis=1), axis=-1)).astype(c.dtype)
+    O.dict_update(c, 1)
+    np.testing.assert_allclose(c.Td, Td_old, rtol=1e-6, atol=1e-6)
+    Td_new = np.real(np.fft.ifft(np.sum(Y3h * c.dh, axis=1), axis=-1)).astype(c.dtype)
+    assert not np.allclose(c.Td, Td_new, rtol=1e-3, atol=1e-3)
+
+
 def test_scan_oracle_integer_brute_force():
     """With integer PWM entries and one-hot data the FP32 scores are exact integers;
     compare the oracle's scans with a direct count."""

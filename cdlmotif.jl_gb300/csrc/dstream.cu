@@ -20,6 +20,7 @@ const Variant* variants_1(int* n);
 const Variant* variants_2(int* n);
 const Variant* variants_3(int* n);
 const Variant* variants_4(int* n);
+const Variant* variants_5(int* n);
 }  // namespace dstream
 
 namespace {
@@ -35,7 +36,8 @@ using dstream::kc2r_t;
 const std::vector<Variant>& all_variants() {
     static const std::vector<Variant> all = [] {
         std::vector<Variant> v;
-        for (auto f : {dstream::variants_1, dstream::variants_2, dstream::variants_3, dstream::variants_4}) {
+        for (auto f : {dstream::variants_1, dstream::variants_2, dstream::variants_3, dstream::variants_4,
+                       dstream::variants_5}) {
             int n = 0;
             const Variant* p = f(&n);
             v.insert(v.end(), p, p + n);

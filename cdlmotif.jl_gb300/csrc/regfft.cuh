@@ -18,10 +18,11 @@
 namespace {
 
 // cos/sin(2 pi m / p) for the per-lane DFT lengths p (the odd primes 3..31, the odd
-// composites 21, 25, 27, 33 and the even 26, 28, 30: the symmetric direct DFT-P below
-// needs no prime), concatenated; exp(-2 pi i j / 32)
-const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 33, 21, 25, 27, 26, 28, 30};
-constexpr int kTrigW = 3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33 + 21 + 25 + 27 + 26 + 28 + 30;
+// composites 21, 25, 27, 33 and the even 18, 20, 22, 24, 26, 28, 30: the symmetric
+// direct DFT-P below needs no prime), concatenated; exp(-2 pi i j / 32)
+const int kPrimesW[] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 33, 21, 25, 27, 26, 28, 30, 18, 20, 22, 24};
+constexpr int kTrigW = 3 + 5 + 7 + 11 + 13 + 17 + 19 + 23 + 29 + 31 + 33 + 21 + 25 + 27 + 26 + 28 + 30 +
+                       18 + 20 + 22 + 24;
 __constant__ float2 c_trigw[kTrigW];
 __constant__ float2 c_w32[32];
 
@@ -29,7 +30,7 @@ __host__ __device__ constexpr int toff(int p) {
     return p == 3 ? 0 : p == 5 ? 3 : p == 7 ? 8 : p == 11 ? 15 : p == 13 ? 26 : p == 17 ? 39
          : p == 19 ? 56 : p == 23 ? 75 : p == 29 ? 98 : p == 31 ? 127 : p == 33 ? 158
          : p == 21 ? 191 : p == 25 ? 212 : p == 27 ? 237 : p == 26 ? 264 : p == 28 ? 290
-         : p == 30 ? 318 : -1;
+         : p == 30 ? 318 : p == 18 ? 348 : p == 20 ? 366 : p == 22 ? 386 : p == 24 ? 408 : -1;
 }
 
 __host__ __device__ constexpr int brev(int k, int bits) {

@@ -29,6 +29,7 @@ const Variant* variants_3(int* n);
 const Variant* variants_4(int* n);
 const Variant* variants_5(int* n);
 const Variant* variants_6(int* n);
+const Variant* variants_7(int* n);
 }  // namespace xiter
 
 namespace {
@@ -41,12 +42,12 @@ constexpr size_t kCap1 = 220 * 1024;   // one CTA per SM
 
 // in order of preference (measured at L=200, K=64: 16 filters per CTA, one CTA per SM,
 // 6.7 ms per X-step; 8 filters per CTA, two CTAs per SM, 7.6 ms).  Lg = 16 P and 32 P
-// for P = 17..33 (every odd P from 21 and the even 26, 28, 30; Lg = 4L + 8W).
+// for per-lane lengths P from 17 to 33 (Lg = 4L + 8W), listed in xiter_v*.cu.
 const std::vector<Variant>& all_variants() {
     static const std::vector<Variant> all = [] {
         std::vector<Variant> v;
         for (auto f : {xiter::variants_1, xiter::variants_2, xiter::variants_3, xiter::variants_4,
-                       xiter::variants_5, xiter::variants_6}) {
+                       xiter::variants_5, xiter::variants_6, xiter::variants_7}) {
             int n = 0;
             const Variant* p = f(&n);
             v.insert(v.end(), p, p + n);

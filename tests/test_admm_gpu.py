@@ -181,11 +181,11 @@ def test_headline_shape_parity(pkg, built_lib, variant, monkeypatch):
 
 
 @pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12), (5, 100, 16, 16),
-                                   (5, 120, 16, 12), (4, 30, 5, 3)])
+                                   (5, 114, 16, 12), (4, 30, 5, 3)])
 def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeypatch):
     """The D-step with d, g1, g3 held as half-spectra (the default on the fused path:
     Y3 transformed by the streaming register-FFT kernels -- Lg = 928, 496 and 528 here --
-    or for the other lengths -- Lg = 576 = 2^6 3^2 and 144 = 2^4 3^2 -- formed in the time domain and
+    or for the other lengths -- Lg = 552 = 2^3 3 23 and 144 = 2^4 3^2 -- formed in the time domain and
     transformed by cuFFT) against the same D-step in the time domain (CDLGB_DSPEC=0) and
     the FP64 oracle after 3 outer iterations.  The two run the same statements with
     different FP32 rounding, which the ADMM amplifies by itself (the FP32-ordered oracle
@@ -222,13 +222,15 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
                                     (100, 32, 16), (52, 32, 16), (68, 16, 16), (100, 32, 4),
                                     (136, 32, 16), (168, 64, 16), (184, 32, 16),
                                     (200, 32, 4), (200, 32, 12), (208, 64, 16), (96, 32, 4),
-                                    (104, 16, 4), (88, 32, 16)])
+                                    (104, 16, 4), (88, 32, 16), (120, 32, 12), (128, 32, 16),
+                                    (144, 32, 16), (160, 32, 16), (60, 16, 16), (84, 32, 16)])
 def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
     """The multi-iteration kernel at the other register-FFT lengths Lg = 4L + 8W:
     32 P for P = 17, 19, 23, 31 and the odd composites 21, 25, 27 (Lg = 672, 800, 864),
     16 P for P = 33, 21, 25 and 27 (Lg = 528, 336, 400; 432 = L 100 at the reference's
-    default W = 4), and the even per-lane lengths P = 26, 28, 30: 32 P = 832 (L 200 at
-    W = 4), 896 (L 200 at W = 12), 960, and 16 P = 416, 448, 480: it is among the
+    default W = 4), the even per-lane lengths P = 18, 20, 22, 24, 26, 28, 30: 32 P = 576,
+    640, 704, 768, 832 (L 200 at W = 4), 896 (L 200 at W = 12), 960, and 16 P = 416, 448,
+    480, and 16 x 23, 16 x 29 (Lg = 368, 464): it is among the
     candidates for the shape, and 2 outer iterations on 5 sequences match the FP64
     oracle at the stated tolerance."""
     synth = pkg.synth
@@ -249,11 +251,11 @@ def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
         assert "multi-iteration" in kinds
 
 
-@pytest.mark.parametrize("L,M,fs,fused", [(500, 32, 16, False), (120, 32, 12, True)])
+@pytest.mark.parametrize("L,M,fs,fused", [(500, 32, 16, False), (114, 32, 12, True)])
 def test_lengths_without_register_ffts(pkg, built_lib, monkeypatch, L, M, fs, fused):
     """Lengths without a register-FFT variant, as the automatic choice runs them, with
     the D-step on the spectral state (Y3 formed in the time domain and transformed by
-    cuFFT): Lg = 576 = 2^6 3^2 on the generic in-kernel-FFT X-step, Lg = 2128 = 2^4 7 19
+    cuFFT): Lg = 552 = 2^3 3 23 on the generic in-kernel-FFT X-step, Lg = 2128 = 2^4 7 19
     (whose generic layout would need one CTA per SM) on the cuFFT-transform X-step.  2
     outer iterations on 3 sequences against the FP64 oracle at the stated tolerance
     (DX and Td, derived fields, at 10x), and against the time-domain D-step

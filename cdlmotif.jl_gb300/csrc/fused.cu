@@ -529,12 +529,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_xstep_fused(XArgs A) {
 }
 
 // ------------------------------------------------------------------ host side
+// The radices of the Stockham passes, the odd primes first: a pass of radix R and span
+// p stores element r of a butterfly at q p R + k + r p, so the first pass (p = 1)
+// stores with stride R, which is free of shared-memory bank conflicts for an odd R and
+// 8-way conflicted for R = 8; with the powers of two last their spans are large.
 bool factorize(int Lg, int* fac, int* nfac) {
     int n = Lg, k = 0, twos = 0;
     while (n % 2 == 0) { n /= 2; ++twos; }
-    while (twos >= 3) { if (k >= kMaxFactors) return false; fac[k++] = 8; twos -= 3; }
-    if (twos == 2) fac[k++] = 4;
-    else if (twos == 1) fac[k++] = 2;
     for (int p : kPrimes) {
         while (n % p == 0) {
             if (k >= kMaxFactors) return false;
@@ -543,6 +544,9 @@ bool factorize(int Lg, int* fac, int* nfac) {
         }
     }
     if (n != 1) return false;
+    if (twos % 3 == 2) { if (k >= kMaxFactors) return false; fac[k++] = 4; }
+    else if (twos % 3 == 1) { if (k >= kMaxFactors) return false; fac[k++] = 2; }
+    for (; twos >= 3; twos -= 3) { if (k >= kMaxFactors) return false; fac[k++] = 8; }
     *nfac = k;
     return true;
 }

@@ -562,10 +562,12 @@ def run_lengths(args, shapes=((100, 16), (200, 16), (500, 16), (200, 4)), N: int
     pkg = _pkg()
     peak = measured_hbm_peak()
     out = []
-    for L, W in shapes:
-        wl = dict(WORKLOAD, N=N, L=L, M=K, filter_size=W, name=f"len_n{N}_l{L}_w{W}_k{K}")
+    for shape in shapes:
+        L, W = shape[0], shape[1]
+        Kx = shape[2] if len(shape) > 2 else K
+        wl = dict(WORKLOAD, N=N, L=L, M=Kx, filter_size=W, name=f"len_n{N}_l{L}_w{W}_k{Kx}")
         S = pkg.synth.onehot(dataset(wl))
-        setup = pkg.CDLSetup(M=K, filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
+        setup = pkg.CDLSetup(M=Kx, filter_size=wl["filter_size"], lambda_=wl["lam"], rho=wl["rho"],
                              sigma=wl["sigma"])
         ab = algorithmic_bytes(wl)
         with pkg.init_cdl(setup, S, seed=wl["seed"]) as c:
@@ -579,7 +581,7 @@ def run_lengths(args, shapes=((100, 16), (200, 16), (500, 16), (200, 4)), N: int
             sec = time.perf_counter() - t0
             pr = c.profile_read()
             xs, ds = pr["xstep"][0] / outer, pr["dstep"][0] / outer
-            out.append({"L": L, "W": W, "Lg": ab["Lg"], "N": N, "K": K, "outer_iter_per_s": outer / sec,
+            out.append({"L": L, "W": W, "Lg": ab["Lg"], "N": N, "K": Kx, "outer_iter_per_s": outer / sec,
                         "xstep_ms_per_outer": xs, "dstep_ms_per_outer": ds,
                         "objective_ms_per_outer": pr["objective"][0] / outer,
                         "xstep_frac_of_hbm_peak": (15 * ab["xstep"] / (xs / 1e3)) / (peak * 1e9) if xs else None,
@@ -819,7 +821,7 @@ def main():
     ap.add_argument("--lengths", action="store_true",
                     help="outer iterations/s and phase times at the batched mix's transform lengths")
     ap.add_argument("--length-shapes", default="100:16,200:16,500:16,200:4",
-                    help="L:W pairs for --lengths")
+                    help="L:W (or L:W:K) for --lengths")
     ap.add_argument("--interference", action="store_true",
                     help="GPU time a running training loses per dataset trained beside it")
     ap.add_argument("--precision", action="store_true",

@@ -78,10 +78,10 @@ struct IterPlan {
 
 }  // namespace
 
-// The first variant (in all_variants() order) whose transform length is Lg and whose filters per
-// CTA divide M into 1, 2, 4 or 8 CTAs; CDLGB_CLUSTER forces a cluster size and
-// CDLGB_XITER=0 turns the multi-iteration kernel off.  Returns nullptr when the size
-// has no variant.
+// The first variant (in all_variants() order) whose transform length is Lg, for an even M
+// on ceil(M / filters per CTA) <= 8 CTAs (the last one may hold fewer real filters);
+// CDLGB_CLUSTER forces a cluster size and CDLGB_XITER=0 turns the multi-iteration kernel
+// off.  Returns nullptr when the size has no variant.
 void* iter_plan_create(cdlgb_ctx* c, int* status) {
     *status = CDLGB_OK;
     if (const char* e = getenv("CDLGB_XITER"))
@@ -98,9 +98,10 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
     IterPlan* P = nullptr;
     const Variant* v = nullptr;
     for (const Variant& cand : all_variants()) {
-        if (cand.N1 * cand.P != c->Lg || c->M % cand.MC) continue;
-        const int cs = c->M / cand.MC;
-        if (cs != 1 && cs != 2 && cs != 4 && cs != 8) continue;
+        // M even; the last CTA of a cluster may hold fewer than MC filters
+        if (cand.N1 * cand.P != c->Lg || c->M % 2) continue;
+        const int cs = (c->M + cand.MC - 1) / cand.MC;
+        if (cs > 8) continue;
         if (want_cs && cs != want_cs) continue;
         const int ld = c->Lg;
         const int ld3 = 3 * cand.N1 / 4 * cand.P;

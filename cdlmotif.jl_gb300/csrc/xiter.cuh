@@ -196,23 +196,30 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
 
     if (RES)
         for (int t = threadIdx.x; t < 10 * (NT / 32); t += blockDim.x) (&rsum[0][0][0])[t] = 0.f;
+    // M need not be a multiple of MC: the last CTA of a cluster then holds Mr < MC real
+    // filters (M even, so whole pairs), and its other pair slots stay zero throughout --
+    // with zero G1-hat they add exactly nothing to P, and their X is never stored
+    const int m0 = rank * Mc;
+    const int Mr = max(0, min(Mc, M - m0));
     for (int t = threadIdx.x; t < P * N1; t += blockDim.x) tw2[t] = A.tw2[t];
     for (int t = threadIdx.x; t < F; t += blockDim.x) Ahs[t] = A.Ah[t];
+    for (int t = threadIdx.x; t < (B - Mr / 2) * BUF; t += blockDim.x)
+        bufs[(size_t)(Mr / 2) * BUF + t] = f2(0.f, 0.f);
     __syncthreads();
 
-    const int m0 = rank * Mc;
     float2 g1r[NFR][MC];
 #pragma unroll
     for (int r = 0; r < NFR; ++r) {
         const int f = threadIdx.x + r * NT;
 #pragma unroll
-        for (int m = 0; m < MC; ++m) g1r[r][m] = f < F ? A.G1h[(size_t)(m0 + m) * F + f] : f2(0.f, 0.f);
+        for (int m = 0; m < MC; ++m)
+            g1r[r][m] = f < F && m < Mr ? A.G1h[(size_t)(m0 + m) * F + f] : f2(0.f, 0.f);
     }
     const int lane = threadIdx.x & 31;
     const int grp = (threadIdx.x >> 5) * G + lane / N1;   // this lane group's slot
     const int gl = lane % N1;                             // lane within the group
-    const bool act = grp <= B;
-    const bool pair = grp < B;
+    const bool pair = grp < B && 2 * grp < Mr;            // a pair of real filters
+    const bool act = pair || grp == B;                    // ... or the U / DX group
     static_assert(MC % 2 == 0, "filters per CTA must pair up");
     float2* sb = bufs + (size_t)(act ? grp : 0) * BUF;
     float2* y2p = y2s + (size_t)(pair ? grp : 0) * ld + gl;
@@ -274,7 +281,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
 
         for (int t = 0; t < A.iters; ++t, ++it) {
             if (t == A.iters / 2 && threadIdx.x >= 32 && threadIdx.x < 64)
-                prefetch_next(A, n + nclusters, m0, MC, Lg, lane);
+                prefetch_next(A, n + nclusters, m0, Mr, Lg, lane);
             __syncwarp();
             fwd_step2<N1, P>(sb, gl, act);
             __syncthreads();

@@ -206,7 +206,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
         // ---------------- forward transforms, Q slots per lane group
         for (int q = 0; q < Q; ++q) {
             const int sl = grp + q * NG;
-            float2* sb = bufs + (size_t)sl * BUF;
+            // a group with no slot left (sl > B) still runs the row DFT's loads, reading
+            // slot 0 and storing nothing: its own slot would lie past the buffers
+            float2* sb = bufs + (size_t)(sl <= B ? sl : 0) * BUF;
             if (sl <= B) fwd_step1<N1, P>(sb, gl, tw2);
             __syncwarp();
             fwd_step2<N1, P>(sb, gl, sl <= B);
@@ -248,7 +250,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB) k_xstep_warp(WArgs A) {
         // ---------------- inverse transforms (rank 0 also transforms DX)
         for (int q = 0; q < Q; ++q) {
             const int sl = grp + q * NG;
-            float2* sb = bufs + (size_t)sl * BUF;
+            float2* sb = bufs + (size_t)(sl <= B ? sl : 0) * BUF;     // as in the forward pass
             const bool act = sl < B || (sl == B && rank == 0);
             inv_step2<N1, P>(sb, gl, act, tw2);
             if (act) inv_step1<N1, P>(sb, gl);

@@ -283,7 +283,9 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
             if (t == A.iters / 2 && threadIdx.x >= 32 && threadIdx.x < 64)
                 prefetch_next(A, n + nclusters, m0, Mr, Lg, lane);
             __syncwarp();
-            fwd_step2<N1, P>(sb, gl, act);
+            // a warp that is one idle lane group (padding pairs, 32-lane groups) skips the
+            // row DFT's store-free loads; two groups sharing a warp both run it
+            if (G > 1 || act) fwd_step2<N1, P>(sb, gl, act);
             __syncthreads();
 
             // ---------------- split + this CTA's part of P = sum_m G1h[m] Vh[m]
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
 
             // ---------------- inverse transforms; then either the next iteration's
             // inputs (in registers, straight into the forward DFT-P) or the results
-            inv_step2<N1, P, false>(sb, gl, act, tw2);
+            if (G > 1 || act) inv_step2<N1, P, false>(sb, gl, act, tw2);
             const bool last = t == A.iters - 1;
             if (act) inv_step1<N1, P, true>(sb, gl, tw2);   // X (or DX) at T[n2][gl], l = gl + N1 n2
             // residuals of the final iterate: what the next dual updates would add

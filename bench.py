@@ -62,11 +62,11 @@ def dataset(wl=WORKLOAD, N=None):
 
 # DRAM bytes (read + write) of one launch on 1000 sequences of the L=200, K=64 workload,
 # from the ncu captures summarised in profiles/
-XITER_DRAM_BYTES_N1000 = 1405720320      # k_xiter, one launch = 15 X-steps
+XITER_DRAM_BYTES_N1000 = 1394415360      # k_xiter, one launch = 15 X-steps
 XWARP_DRAM_BYTES_N1000 = 1391571456      # k_xstep_warp, one launch = 1 X-step
 # warp instructions issued per sequence and X-step by k_xiter<32, 29, 288, 1, 16>
 # (smsp__inst_executed.sum of the same 1000-sequence capture / (1000 x 15))
-XITER_WARP_INSTR_PER_SEQ_XSTEP = 129.4e3
+XITER_WARP_INSTR_PER_SEQ_XSTEP = 126.6e3
 N_SM, SCHEDULERS_PER_SM = 152, 4
 
 

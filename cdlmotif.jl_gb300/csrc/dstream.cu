@@ -21,6 +21,7 @@ const Variant* variants_2(int* n);
 const Variant* variants_3(int* n);
 const Variant* variants_4(int* n);
 const Variant* variants_5(int* n);
+const Variant* variants_6(int* n);
 }  // namespace dstream
 
 namespace {
@@ -37,7 +38,7 @@ const std::vector<Variant>& all_variants() {
     static const std::vector<Variant> all = [] {
         std::vector<Variant> v;
         for (auto f : {dstream::variants_1, dstream::variants_2, dstream::variants_3, dstream::variants_4,
-                       dstream::variants_5}) {
+                       dstream::variants_5, dstream::variants_6}) {
             int n = 0;
             const Variant* p = f(&n);
             v.insert(v.end(), p, p + n);

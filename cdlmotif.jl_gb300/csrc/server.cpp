@@ -75,8 +75,9 @@ namespace {
 // smallest whose transform length is a multiple of 16 with prime factors <= 31 (the
 // generic in-kernel FFTs)
 int friendly_L(int L, int fs) {
-    static const int kRegLg[] = {336, 368, 400, 416, 432, 448, 464, 480, 496, 528, 544, 576, 608,
-                                 640, 672, 704, 736, 768, 800, 832, 864, 896, 928, 960, 992};
+    static const int kRegLg[] = {288, 320, 336, 352, 368, 384, 400, 416, 432, 448, 464, 480, 496,
+                                 528, 544, 576, 608, 640, 672, 704, 736, 768, 800, 832, 864, 896,
+                                 928, 960, 992};
     const int lg = 4 * L + 8 * fs;
     for (int n : kRegLg)
         if (lg <= n && n <= 1.08 * lg && (n - 8 * fs) % 4 == 0) return (n - 8 * fs) / 4;

@@ -30,6 +30,7 @@ const Variant* variants_4(int* n);
 const Variant* variants_5(int* n);
 const Variant* variants_6(int* n);
 const Variant* variants_7(int* n);
+const Variant* variants_8(int* n);
 }  // namespace xiter
 
 namespace {
@@ -47,7 +48,7 @@ const std::vector<Variant>& all_variants() {
     static const std::vector<Variant> all = [] {
         std::vector<Variant> v;
         for (auto f : {xiter::variants_1, xiter::variants_2, xiter::variants_3, xiter::variants_4,
-                       xiter::variants_5, xiter::variants_6, xiter::variants_7}) {
+                       xiter::variants_5, xiter::variants_6, xiter::variants_7, xiter::variants_8}) {
             int n = 0;
             const Variant* p = f(&n);
             v.insert(v.end(), p, p + n);

@@ -37,8 +37,8 @@ def footprint_bytes(setup: CDLSetup, L: int, N: int, fft_mode: int = 0) -> int:
 
 
 # transform lengths of the multi-iteration X-step kernel's variants (csrc/xiter.cu)
-REGISTER_LG = (336, 368, 400, 416, 432, 448, 464, 480, 496, 528, 544, 576, 608, 640, 672, 704, 736,
-               768, 800, 832, 864, 896, 928, 960, 992)
+REGISTER_LG = (288, 320, 336, 352, 368, 384, 400, 416, 432, 448, 464, 480, 496, 528, 544, 576, 608,
+               640, 672, 704, 736, 768, 800, 832, 864, 896, 928, 960, 992)
 
 
 def friendly_length(L: int, filter_size: int) -> int:

@@ -225,14 +225,16 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
                                     (104, 16, 4), (88, 32, 16), (120, 32, 12), (128, 32, 16),
                                     (144, 32, 16), (160, 32, 16), (60, 16, 16), (84, 32, 16),
                                     (200, 10, 4), (100, 10, 4), (200, 20, 16), (104, 6, 16),
-                                    (200, 40, 16)])
+                                    (200, 40, 16), (40, 32, 16), (48, 16, 16), (56, 32, 16),
+                                    (88, 10, 4)])
 def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
     """The multi-iteration kernel at the other register-FFT lengths Lg = 4L + 8W:
     32 P for P = 17, 19, 23, 31 and the odd composites 21, 25, 27 (Lg = 672, 800, 864),
     16 P for P = 33, 21, 25 and 27 (Lg = 528, 336, 400; 432 = L 100 at the reference's
     default W = 4), the even per-lane lengths P = 18, 20, 22, 24, 26, 28, 30: 32 P = 576,
     640, 704, 768, 832 (L 200 at W = 4), 896 (L 200 at W = 12), 960, and 16 P = 416, 448,
-    480, and 16 x 23, 16 x 29 (Lg = 368, 464); and M that is not a multiple of the 16
+    480, and 16 x 23, 16 x 29 (Lg = 368, 464), 16 x 18, 20, 22, 24 (Lg = 288, 320, 352,
+    384); and M that is not a multiple of the 16
     filters per CTA (the reference's default M = 10 at W = 4; M = 20 and 40 on clusters
     whose last CTA holds 4 or 8 real filters; M = 6): it is among the candidates for the
     shape, and 2 outer iterations on 5 sequences match the FP64 oracle at the stated

@@ -56,11 +56,11 @@ def test_per_lane_tables_cover_every_variant():
 
 
 def test_friendly_padding_reaches_a_register_length_up_to_992(pkg):
-    """With the server's 8 % rule every transform length from 344 to 992 (W = 16: L from
-    54 to 216) pads to a register-FFT length."""
+    """With the server's 8 % rule every transform length from 300 to 992 (W = 16: L from
+    43 to 216) pads to a register-FFT length."""
     from cdlmotif_gb300 import serve
     reg = set(serve.REGISTER_LG)
-    for L in range(54, 217):
+    for L in range(43, 217):
         Lp = serve.friendly_length(L, 16)
         assert 4 * Lp + 128 in reg, L
     assert np.all(np.diff(serve.REGISTER_LG) > 0)

@@ -270,7 +270,7 @@ const char* cdlgb_last_error(const cdlgb_ctx* c) { return c ? c->err : "null con
 
 static int pick_fused(const cdlgb_params* p, int Lg) {
     if (p->fft_mode == 1) return 0;
-    int ok = fused_supported(Lg, p->M);
+    int ok = fused_supported(Lg, p->M, Lg - 8 * p->filter_size);
     if (p->fft_mode == 2) return ok ? 1 : -1;
     return ok;
 }

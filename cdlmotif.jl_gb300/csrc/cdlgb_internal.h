@@ -199,7 +199,8 @@ size_t admm_footprint(const cdlgb_params* p, int L4, int N, int fused);
 int cdlgb_set_plan_streams(cdlgb_ctx* c);
 
 // ---- fused.cu ----
-int fused_supported(int Lg, int M);
+int fused_supported(int Lg, int M, int L4);
+int iter_variant_fits(int Lg, int M, int L4);
 int fused_setup(cdlgb_ctx* c);
 void fused_free(cdlgb_ctx* c);
 int fused_xstep(cdlgb_ctx* c, const float* Xin, float* Xout, int accum_abs);

@@ -66,7 +66,6 @@ void* dfwd_plan_create(cdlgb_ctx* c, int* status) {
     *status = CDLGB_OK;
     if (const char* e = getenv("CDLGB_DSTREAM"))
         if (atoi(e) == 0) return nullptr;
-    if (c->M % 2) return nullptr;
     const Variant* v = nullptr;
     for (const Variant& cand : all_variants())
         if (cand.N1 * cand.P == c->Lg) v = &cand;

@@ -3,7 +3,9 @@
 // and the inverse k_dinv (further down, d = irfft(d-hat) per filter pair).
 //
 // For every (sequence n, filter pair a = 2s, b = 2s + 1) a lane group forms, straight
-// from the state arrays, the three packed real pairs the D-step transforms --
+// from the state arrays, the three packed real pairs the D-step transforms (for an odd M
+// the last pair has no filter b: that lane group reads and transforms filter a's row in
+// its place and stores filter a's spectrum only) --
 //   Y3 = projectionX!(X + y3)                 (X + y3 on the rows l % 4 == 0, else 0)
 //   H  = (G1 - g1) + (G3 - g3)                (the filter-domain terms of sherman_CDL_RHS!)
 //   d  (the previous iterate)
@@ -65,24 +67,28 @@ using dstream::FArgs;
 using dstream::IArgsD;
 
 // split the packed spectrum Z = A + i B of two real sequences held in natural order in
-// `buf` and store A[f], B[f] for f = 0..Lg/2 (lanes over f)
+// `buf` and store A[f], B[f] for f = 0..Lg/2 (lanes over f).  B is stored first: with
+// ob == oa (a pair without a second sequence) A is what remains.
 template <int Lg, int N1>
 __device__ __forceinline__ void split_store(const float2* __restrict__ buf, int gl,
-                                            float2* __restrict__ oa, float2* __restrict__ ob) {
+                                            float2* oa, float2* ob) {
     constexpr int F = Lg / 2 + 1;
     for (int f = gl; f < F; f += N1) {
         const float2 z1 = buf[f], z2 = buf[f == 0 ? 0 : Lg - f];
-        oa[f] = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
         ob[f] = f2(0.5f * (z1.y + z2.y), 0.5f * (z2.x - z1.x));
+        oa[f] = f2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
     }
 }
 
 // one of the three transforms of k_dfwd for the lane group's (sequence, filter pair):
 // WHICH 0: Y3 = projectionX!(X + y3) (rows l % 4 == 0 only), 1: H = (G1 - g1) + (G3 - g3),
 // 2: the previous d.  The state is read through the read-only path; P rows per column.
+// bo: the offset of filter b's rows from filter a's (Lg; 0 for the last pair of an odd M,
+// which has no filter b), fo the same for the spectra (F; 0).
 template <int N1, int P, int WHICH>
 __device__ __forceinline__ void dfwd_one(const FArgs& A, float2* sb, int gl, const float2* tw2,
-                                         bool act, bool keep, size_t ra, size_t pa, size_t oa) {
+                                         bool act, bool keep, int bo, int fo, size_t ra, size_t pa,
+                                         size_t oa) {
     constexpr int Lg = N1 * P;
     constexpr int RS = N1 + 1;
     constexpr int F = Lg / 2 + 1;
@@ -95,14 +101,14 @@ __device__ __forceinline__ void dfwd_one(const FArgs& A, float2* sb, int gl, con
                 // Y3 = X + y3 on the kept rows.  Every X-step leaves y3 = +0 exactly there
                 // (projectionX! keeps X + y3, so y3' = (y3 + X) - Y3 is set to +0, as
                 // initialisation does), so X + 0 gives the same bits without reading y3.
-                v = keep ? f2(__ldg(A.X + ra + o) + 0.f, __ldg(A.X + ra + Lg + o) + 0.f)
+                v = keep ? f2(__ldg(A.X + ra + o) + 0.f, __ldg(A.X + ra + bo + o) + 0.f)
                          : f2(0.f, 0.f);
             } else if (WHICH == 1) {
                 v = f2((__ldg(A.G1 + pa + o) - __ldg(A.g1 + ra + o)) + (__ldg(A.G3 + pa + o) - __ldg(A.g3 + ra + o)),
-                       (__ldg(A.G1 + pa + Lg + o) - __ldg(A.g1 + ra + Lg + o)) +
-                           (__ldg(A.G3 + pa + Lg + o) - __ldg(A.g3 + ra + Lg + o)));
+                       (__ldg(A.G1 + pa + bo + o) - __ldg(A.g1 + ra + bo + o)) +
+                           (__ldg(A.G3 + pa + bo + o) - __ldg(A.g3 + ra + bo + o)));
             } else {
-                v = f2(__ldg(A.d + ra + o), __ldg(A.d + ra + Lg + o));
+                v = f2(__ldg(A.d + ra + o), __ldg(A.d + ra + bo + o));
             }
             sb[n2 * RS + gl] = v;
         }
@@ -112,7 +118,7 @@ __device__ __forceinline__ void dfwd_one(const FArgs& A, float2* sb, int gl, con
     fwd_step2<N1, P>(sb, gl, act);
     if (act) {
         float2* out = WHICH == 0 ? A.Yh : WHICH == 1 ? A.Hh : A.Dh;
-        split_store<Lg, N1>(sb, gl, out + oa, out + oa + F);
+        split_store<Lg, N1>(sb, gl, out + oa, out + oa + fo);
     }
     __syncwarp();
 }
@@ -136,7 +142,7 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
     const int groups = (blockDim.x >> 5) * G;
     const bool keep = (gl & 3) == 0;                       // l = gl + N1 n2, N1 % 4 == 0
     float2* sb = bufs + (size_t)gw * BUF;
-    const int pairs = A.M / 2;
+    const int pairs = (A.M + 1) / 2;
     const long items = (long)A.cn * pairs;
     const long stride = (long)gridDim.x * groups;
     // every lane group of a warp runs the same number of rounds (the row DFT syncs the warp)
@@ -150,9 +156,11 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
         const size_t ra = ((size_t)n * A.M + ma) * Lg + gl;   // row of filter a at lane gl
         const size_t pa = (size_t)ma * Lg + gl;
         const size_t oa = ((size_t)n * A.M + ma) * F;
-        dfwd_one<N1, P, 0>(A, sb, gl, tw2, act, keep, ra, pa, oa);
-        if (A.Hh) dfwd_one<N1, P, 1>(A, sb, gl, tw2, act, keep, ra, pa, oa);   // uniform
-        if (A.Dh) dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, ra, pa, oa);
+        const bool hb = ma + 1 < A.M;
+        const int bo = hb ? Lg : 0, fo = hb ? F : 0;
+        dfwd_one<N1, P, 0>(A, sb, gl, tw2, act, keep, bo, fo, ra, pa, oa);
+        if (A.Hh) dfwd_one<N1, P, 1>(A, sb, gl, tw2, act, keep, bo, fo, ra, pa, oa);   // uniform
+        if (A.Dh) dfwd_one<N1, P, 2>(A, sb, gl, tw2, act, keep, bo, fo, ra, pa, oa);
     }
 }
 
@@ -160,7 +168,8 @@ __global__ void __launch_bounds__(256, 2) k_dfwd(FArgs A) {
 // as they are read) are packed into one full spectrum Z = Dh_a + i Dh_b (Z[f], and Z[Lg - f] =
 // conj(Dh_a[f]) + i conj(Dh_b[f])), inverted with the register four-step FFT, and
 // d[a] = Re, d[b] = Im written (as a C2R per filter, the imaginary parts of the
-// half-spectrum's f = 0 and f = Lg/2 bins are dropped).
+// half-spectrum's f = 0 and f = Lg/2 bins are dropped; for an odd M the last pair reads
+// Dh_a for both halves and writes d[a] only: its Im store goes to d[a] first).
 
 template <int N1, int P>
 __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
@@ -181,7 +190,7 @@ __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
     const int gl = lane % N1;
     const int groups = (blockDim.x >> 5) * G;
     float2* sb = bufs + (size_t)gw * BUF;
-    const int pairs = A.M / 2;
+    const int pairs = (A.M + 1) / 2;
     const long items = (long)A.cn * pairs;
     const long stride = (long)gridDim.x * groups;
     const long rounds = (items + stride - 1) / stride;
@@ -191,10 +200,12 @@ __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
         const long n = act ? item / pairs : 0;
         const int s = act ? (int)(item - n * pairs) : 0;
         const size_t ia = ((size_t)n * A.M + 2 * s) * F;
+        const bool hb = 2 * s + 1 < A.M;                   // false: the last pair of an odd M
+        const size_t ib = ia + (hb ? F : 0);
         if (act) {
 #pragma unroll 5
             for (int f = gl; f < F; f += N1) {
-                float2 a = __ldg(A.Dh + ia + f), b = __ldg(A.Dh + ia + F + f);
+                float2 a = __ldg(A.Dh + ia + f), b = __ldg(A.Dh + ib + f);
                 a = f2(a.x * A.scale, a.y * A.scale);
                 b = f2(b.x * A.scale, b.y * A.scale);
                 if (f == 0 || f == half) {
@@ -210,11 +221,12 @@ __global__ void __launch_bounds__(256, 2) k_dinv(IArgsD A) {
         if (act) {
             inv_step1<N1, P, true>(sb, gl, tw2);
             const size_t ra = ((size_t)n * A.M + 2 * s) * Lg + gl;
+            const size_t rb = ra + (hb ? Lg : 0);
 #pragma unroll 4
             for (int n2 = 0; n2 < P; ++n2) {
                 const float2 v = sb[n2 * RS + gl];
+                A.d[rb + N1 * n2] = v.y;
                 A.d[ra + N1 * n2] = v.x;
-                A.d[ra + Lg + N1 * n2] = v.y;
             }
         }
         __syncwarp();

@@ -580,8 +580,11 @@ bool choose_cluster(int Lg, int M, int* CS, int* Mc) {
 
 }  // namespace
 
-int fused_supported(int Lg, int M) {
+// A fused X-step exists for Lg and M (L4 = Lg minus the two margins): the multi-iteration
+// kernel, the one-X-step kernel, or the generic in-kernel-FFT kernel.
+int fused_supported(int Lg, int M, int L4) {
     int fac[kMaxFactors], nf = 0, cs = 0, mc = 0;
+    if (iter_variant_fits(Lg, M, L4)) return 1;
     if (warp_variant_exists(Lg, M)) return 1;
     if (Lg % 4) return 0;
     if (!factorize(Lg, fac, &nf)) return 0;

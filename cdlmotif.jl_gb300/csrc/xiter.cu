@@ -68,6 +68,28 @@ size_t iter_smem(int N1, int P, int slots, int Mc, int ld, int ld3, int L4) {
            ((size_t)Lg + Fp + L4) * sizeof(float);
 }
 
+// the static checks of a variant for Lg, M and the window length L4: its transform
+// length, an even M (filters are transformed in pairs) on ceil(M / MC) <= 8 CTAs (exactly
+// want_cs when that is set), and its shared memory
+bool variant_fits(const Variant& v, int Lg, int M, int L4, int want_cs, int* cs, size_t* smem) {
+    if (v.N1 * v.P != Lg || M < 2 || M % 2) return false;
+    *cs = (M + v.MC - 1) / v.MC;
+    if (*cs > 8 || (want_cs && *cs != want_cs)) return false;
+    *smem = iter_smem(v.N1, v.P, (v.MC + 1) / 2 + 1, v.MC, Lg, 3 * v.N1 / 4 * v.P, L4);
+    return *smem <= (v.minb == 2 ? kCap2 : kCap1);
+}
+
+bool xiter_off() {
+    if (getenv("CDLGB_GENERIC_FFT")) return true;
+    const char* e = getenv("CDLGB_XITER");
+    return e && atoi(e) == 0;
+}
+
+int env_cluster() {
+    const char* e = getenv("CDLGB_CLUSTER");
+    return e ? atoi(e) : 0;
+}
+
 struct IterPlan {
     kern_t k, kr;
     int CS, Mc, ld, ld3, threads, grid;
@@ -85,11 +107,19 @@ struct IterPlan {
 // off.  Returns nullptr when the size has no variant.
 void* iter_plan_create(cdlgb_ctx* c, int* status) {
     *status = CDLGB_OK;
-    if (const char* e = getenv("CDLGB_XITER"))
-        if (atoi(e) == 0) return nullptr;
-    int want_cs = 0;
-    if (const char* e = getenv("CDLGB_CLUSTER")) want_cs = atoi(e);
-    return iter_plan_create_nth(c, 0, want_cs, status);
+    if (xiter_off()) return nullptr;
+    return iter_plan_create_nth(c, 0, env_cluster(), status);
+}
+
+// Whether iter_plan_create would find a variant for Lg, M and L4 (the checks that need
+// no device: the cluster's occupancy is checked when the plan is made).
+int iter_variant_fits(int Lg, int M, int L4) {
+    if (xiter_off()) return 0;
+    int cs = 0;
+    size_t sm = 0;
+    for (const Variant& v : all_variants())
+        if (variant_fits(v, Lg, M, L4, env_cluster(), &cs, &sm)) return 1;
+    return 0;
 }
 
 // The nth variant (in all_variants() order) that fits Lg and M, optionally only with
@@ -99,15 +129,12 @@ void* iter_plan_create_nth(cdlgb_ctx* c, int nth, int want_cs, int* status) {
     IterPlan* P = nullptr;
     const Variant* v = nullptr;
     for (const Variant& cand : all_variants()) {
-        // M even; the last CTA of a cluster may hold fewer than MC filters
-        if (cand.N1 * cand.P != c->Lg || c->M % 2) continue;
-        const int cs = (c->M + cand.MC - 1) / cand.MC;
-        if (cs > 8) continue;
-        if (want_cs && cs != want_cs) continue;
+        // the last CTA of a cluster may hold fewer than MC filters
+        int cs = 0;
+        size_t sm = 0;
+        if (!variant_fits(cand, c->Lg, c->M, c->L4, want_cs, &cs, &sm)) continue;
         const int ld = c->Lg;
         const int ld3 = 3 * cand.N1 / 4 * cand.P;
-        const size_t sm = iter_smem(cand.N1, cand.P, (cand.MC + 1) / 2 + 1, cand.MC, ld, ld3, c->L4);
-        if (sm > (cand.minb == 2 ? kCap2 : kCap1)) continue;
         if (nth-- > 0) continue;
         v = &cand;
         P = new IterPlan();

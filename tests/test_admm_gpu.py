@@ -226,7 +226,7 @@ def test_spectral_dstep_matches_time_domain_dstep(pkg, built_lib, shape, monkeyp
                                     (144, 32, 16), (160, 32, 16), (60, 16, 16), (84, 32, 16),
                                     (200, 10, 4), (100, 10, 4), (200, 20, 16), (104, 6, 16),
                                     (200, 40, 16), (40, 32, 16), (48, 16, 16), (56, 32, 16),
-                                    (88, 10, 4)])
+                                    (88, 10, 4), (200, 34, 4)])
 def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
     """The multi-iteration kernel at the other register-FFT lengths Lg = 4L + 8W:
     32 P for P = 17, 19, 23, 31 and the odd composites 21, 25, 27 (Lg = 672, 800, 864),
@@ -236,9 +236,9 @@ def test_multi_iteration_other_lengths(pkg, built_lib, L, M, fs):
     480, and 16 x 23, 16 x 29 (Lg = 368, 464), 16 x 18, 20, 22, 24 (Lg = 288, 320, 352,
     384); and M that is not a multiple of the 16
     filters per CTA (the reference's default M = 10 at W = 4; M = 20 and 40 on clusters
-    whose last CTA holds 4 or 8 real filters; M = 6): it is among the candidates for the
-    shape, and 2 outer iterations on 5 sequences match the FP64 oracle at the stated
-    tolerance."""
+    whose last CTA holds 4 or 8 real filters; M = 6; M = 34 at Lg = 832 on 3 CTAs, a
+    shape no other fused X-step fits): it is among the candidates for the shape, and 2
+    outer iterations on 5 sequences match the FP64 oracle at the stated tolerance."""
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(17, 5, L, [8, 12], [0.4, 0.4])
     S = synth.onehot(bases)
@@ -328,13 +328,13 @@ def test_multi_iteration_kernel_matches_one_step_kernel(pkg, built_lib, shape, m
     np.testing.assert_allclose(out["1"]["objs"], out["0"]["objs"], rtol=1e-6)
 
 
-@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12)])
+@pytest.mark.parametrize("shape", [(6, 200, 64, 16), (7, 100, 16, 12), (5, 200, 9, 16)])
 def test_dstep_variants_against_oracle(pkg, built_lib, shape, monkeypatch):
     """One D-step from the same state through each D-step implementation -- the default
     (streaming register-FFT forward transforms + cuFFT inverse) and the all-cuFFT one --
     against the FP64 oracle: every field the D-step writes is
     within the parity tolerance, and within twice the all-cuFFT path's error
-    (Lg = 928 and 496)."""
+    (Lg = 928 and 496; M = 9, whose last filter has no partner in the paired transforms)."""
     N, L, M, fs = shape
     synth = pkg.synth
     bases, _, _ = synth.plant_dataset(13, N, L, [8, 12], [0.4, 0.4])

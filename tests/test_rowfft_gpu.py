@@ -20,9 +20,11 @@ TOL_X = 1e-4
 TOL_OBJ = 1e-5
 
 # (N, L, M, W): Lg = 4L + 8W = 928 = 32 x 29, 496 = 16 x 31, 544 = 32 x 17, 992 = 32 x 31,
-# 528 = 16 x 33, 432 = 16 x 27, 800 = 32 x 25, 832 = 32 x 26, 416 = 16 x 26
+# 528 = 16 x 33, 432 = 16 x 27, 800 = 32 x 25, 832 = 32 x 26, 416 = 16 x 26; odd M (7, 9):
+# each sequence's last filter row is paired with zeros
 SHAPES = [(5, 200, 8, 16), (7, 100, 16, 12), (4, 104, 16, 16), (3, 216, 16, 16), (5, 100, 16, 16),
-          (5, 100, 8, 4), (3, 168, 16, 16), (5, 200, 16, 4), (4, 96, 8, 4)]
+          (5, 100, 8, 4), (3, 168, 16, 16), (5, 200, 16, 4), (4, 96, 8, 4), (5, 100, 7, 16),
+          (3, 200, 9, 16)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)

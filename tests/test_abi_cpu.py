@@ -106,3 +106,26 @@ def test_params_struct_layout_matches_header(pkg, built_lib, tmp_path):
     vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert vals[0] == C.sizeof(CdlgbParams)
     assert vals[1:] == [getattr(CdlgbParams, n).offset for n in names]
+
+
+def test_fused_path_choice(pkg, built_lib, monkeypatch):
+    """Which path a shape takes is host logic, visible without a GPU through
+    cdlgb_footprint (the fused path holds other buffers than the cuFFT-transform path):
+    at Lg = 832 (L = 200, W = 4) M = 34 fits only the multi-iteration X-step (the generic
+    kernel's layout needs 150 KB of shared memory at 2 CTAs of 17 filters, and there is no
+    one-X-step variant for 832), so the automatic choice is the fused path while that
+    kernel is on and the cuFFT-transform path with CDLGB_XITER=0; M = 32 also fits the
+    generic kernel (4 CTAs of 8 filters) and stays fused either way."""
+    from cdlmotif_gb300 import serve
+
+    def fp(M, mode):
+        return serve.footprint_bytes(pkg.CDLSetup(M=M, filter_size=4), 200, 100, mode)
+
+    monkeypatch.delenv("CDLGB_XITER", raising=False)
+    monkeypatch.delenv("CDLGB_GENERIC_FFT", raising=False)
+    monkeypatch.delenv("CDLGB_CLUSTER", raising=False)
+    fused34, fused32 = fp(34, 2), fp(32, 2)
+    assert fp(34, 0) == fused34 and fp(32, 0) == fused32
+    monkeypatch.setenv("CDLGB_XITER", "0")
+    assert fp(34, 0) != fused34
+    assert fp(32, 0) == fp(32, 2) == fused32

@@ -129,3 +129,72 @@ def test_fused_path_choice(pkg, built_lib, monkeypatch):
     monkeypatch.setenv("CDLGB_XITER", "0")
     assert fp(34, 0) != fused34
     assert fp(32, 0) == fp(32, 2) == fused32
+
+
+_C_SCALARS = {"int32_t": (4, "i"), "uint32_t": (4, "i"), "int64_t": (8, "i"), "uint64_t": (8, "i"),
+              "size_t": (8, "i"), "int": (4, "i"), "uint8_t": (1, "i"), "char": (1, "i"),
+              "float": (4, "f"), "double": (8, "f")}
+
+
+def _c_param(decl):
+    """(pointer depth, base type) of one parameter declaration"""
+    decl = re.sub(r"\bconst\b", "", decl).strip()
+    depth = decl.count("*")
+    words = decl.replace("*", " ").split()
+    base = words[0] if len(words) > 1 or depth else words[0]
+    return depth, base
+
+
+def _header_params():
+    txt = open(os.path.join(ROOT, "include", "cdlgb.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for ret, name, params in re.findall(r"([\w\s\*]+?)\b(cdlgb_\w+)\s*\(([^()]*)\)\s*;", txt):
+        ps = [p for p in params.split(",") if p.strip() and p.strip() != "void"]
+        out[name] = (_c_param(ret + " r"), [_c_param(p) for p in ps])
+    return out
+
+
+def _ct_kind(t):
+    import ctypes as C
+    if t is C.c_void_p or t is C.c_char_p:
+        return ("ptr", None)
+    if isinstance(t, type) and issubclass(t, C._Pointer):
+        return ("ptr", t._type_)
+    if isinstance(t, type) and issubclass(t, C.Structure):
+        return ("struct", t)
+    cls = "f" if t in (C.c_float, C.c_double) else "i"
+    return ("scalar", (C.sizeof(t), cls))
+
+
+def _compatible(cparam, ct):
+    import ctypes as C
+    depth, base = cparam
+    kind, info = _ct_kind(ct)
+    if depth == 0:
+        return kind == "scalar" and _C_SCALARS.get(base) == info
+    if kind != "ptr":
+        return False
+    if info is None:                      # c_void_p / c_char_p: any pointer
+        return True
+    if depth > 1:                         # T** against POINTER(c_void_p)
+        return _ct_kind(info)[0] == "ptr"
+    if base in _C_SCALARS:
+        pk = _ct_kind(info)
+        return pk[0] == "scalar" and pk[1] == _C_SCALARS[base]
+    return issubclass(info, C.Structure) or info is C.c_void_p   # struct or opaque pointee
+
+
+def test_ctypes_signatures_match_header(pkg, built_lib):
+    """Every ctypes signature of the binding has the header prototype's parameter count
+    and, parameter by parameter, the same kind: scalars of the same size and class,
+    pointers to elements of the same size and class (c_void_p for any pointer)."""
+    from cdlmotif_gb300 import _lib
+    protos = _header_params()
+    assert len(protos) == len(_lib.SIGNATURES)
+    for name, (res, args) in _lib.SIGNATURES.items():
+        cret, cparams = protos[name]
+        assert len(args) == len(cparams), name
+        for i, (cp, ct) in enumerate(zip(cparams, args)):
+            assert _compatible(cp, ct), (name, i, cp, ct)
+        assert _compatible(cret, res), (name, "result", cret, res)

@@ -85,27 +85,32 @@ def test_golden_scan_pfms_from_counts(pkg, built_lib):
     assert SO.transfac_text(g["pfms"][0, :, : g["lens"][0]]) == str(g["transfac"])
 
 
-def test_params_struct_layout_matches_header(pkg, built_lib, tmp_path):
-    """The ctypes mirror of cdlgb_params has the C struct's size and field offsets."""
+@pytest.mark.parametrize("py_name,c_name", [("CdlgbParams", "cdlgb_params"),
+                                             ("ServerConfig", "cdlgb_server_config"),
+                                             ("RequestInfo", "cdlgb_request_info")])
+def test_struct_layouts_match_header(pkg, built_lib, tmp_path, py_name, c_name):
+    """The ctypes mirrors of the header's structs have the C structs' sizes and field
+    offsets (compiled against include/cdlgb.h)."""
     import ctypes as C
     import shutil
     import subprocess
-    from cdlmotif_gb300._lib import CdlgbParams
+    from cdlmotif_gb300 import _lib
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
         pytest.skip("no C compiler")
-    names = [f[0] for f in CdlgbParams._fields_]
+    st = getattr(_lib, py_name)
+    names = [f[0] for f in st._fields_]
     cnames = ["lambda" if n == "lambda_" else n for n in names]
     src = tmp_path / "layout.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "cdlgb.h"\nint main(void){\n'
-                   'printf("%zu\\n", sizeof(cdlgb_params));\n' +
-                   "".join(f'printf("%zu\\n", offsetof(cdlgb_params, {n}));\n' for n in cnames) +
+                   f'printf("%zu\\n", sizeof({c_name}));\n' +
+                   "".join(f'printf("%zu\\n", offsetof({c_name}, {n}));\n' for n in cnames) +
                    "return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    assert vals[0] == C.sizeof(CdlgbParams)
-    assert vals[1:] == [getattr(CdlgbParams, n).offset for n in names]
+    assert vals[0] == C.sizeof(st)
+    assert vals[1:] == [getattr(st, n).offset for n in names]
 
 
 def test_fused_path_choice(pkg, built_lib, monkeypatch):

@@ -77,7 +77,8 @@ __global__ void k_colnorm(const float2* __restrict__ Gh, float* __restrict__ A, 
 __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
                                        float& na, float& nb, float& v) {
     float t = x + a;                                        // X + y2
-    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);    // shrink!  (csc_kernels.jl:53-64)
+    // shrink! (csc_kernels.jl:53-64) at lambda, not lambda / rho (REF_QUIRK_Q4, :61)
+    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);
     float Y3 = keep ? x + b : 0.f;                          // projectionX! (:68-82)
     na = (a + x) - Y2;                                      // y2 .+ X .- Y2  (train.jl:13)
     nb = (b + x) - Y3;                                      // y3 .+ X .- Y3  (train.jl:14)
@@ -111,7 +112,8 @@ __global__ void k_xprep_ln(float* __restrict__ y1, const float* __restrict__ DX,
     }
 }
 
-// Per (f, n): the Sherman-Morrison code solve (csc_kernels.jl:8-49, train.jl:18-27).
+// Per (f, n): the Sherman-Morrison code solve (csc_kernels.jl:8-49, train.jl:18-27), with
+// the consensus G1-hat, not d-hat (REF_QUIRK_Q5).
 __global__ void k_xsolve(float2* __restrict__ Vh, const float2* __restrict__ Uh,
                          const float2* __restrict__ G1h, const float* __restrict__ Ah,
                          float2* __restrict__ DXh, int F, int M, int nfb, float kc, float scale) {
@@ -250,6 +252,7 @@ __global__ void __launch_bounds__(kDsBins * kDsWarps) k_dsolve(
     const float2 beta = make_float2(fmaf(z.x, B, Q.x) * inv, fmaf(z.y, B, Q.y) * inv);
     const float2 W = make_float2(z.x - beta.x, z.y - beta.y);
     for (int m = w; m < M; m += kDsWarps) {
+        // REF_QUIRK_Q1: the combine has no 1/2, unlike the X-step's (cdl_kernels.jl:30)
         const float2 h = STAGE ? cjfma(ys[m * kDsBins + lane], W, hs[m * kDsBins + lane])
                                : cjfma(Yh[base + (size_t)m * F], W, Hh[base + (size_t)m * F]);
         Dh[base + (size_t)m * F] = make_float2(h.x * scale_out, h.y * scale_out);
@@ -354,7 +357,8 @@ __global__ void k_dfinish(const float* __restrict__ part, float* __restrict__ v1
 }
 
 // prox_simplex_zeros! (cdl_kernels.jl:53-66), group index as in the reference: for
-// 1-based row l the group is rows i+1..i+4 with i = 4*floor(l/4).
+// 1-based row l the group is rows i+1..i+4 with i = 4*floor(l/4) (REF_QUIRK_Q2: rows
+// l = 4, 8, ... take the next group, cdl_kernels.jl:59).
 __global__ void k_dprox(const float* __restrict__ v1, float* __restrict__ G1, int Lg, int M,
                         int flen) {
     size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;

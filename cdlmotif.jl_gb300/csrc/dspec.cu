@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(kBins * kWarps, 1) k_dspec(SArgs A) {
             for (int k = 0; k < MW; ++k) {
                 const int m = w + kWarps * k;
                 if (m >= M) continue;
+                // REF_QUIRK_Q1: the combine has no 1/2, unlike the X-step's (cdl_kernels.jl:30)
                 float2 dh = cjfma2(yv[k], W, hv[k]);
                 if (edge) dh.y = 0.f;                      // the transform of a real d
                 const size_t i = (size_t)n * M * F + (size_t)m * F + f;

@@ -283,7 +283,8 @@ __device__ float2* fft_all(float2* a, float2* b, int nslots, int Lg, const int* 
 __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
                                        float& na, float& nb, float& v) {
     float t = x + a;                                        // X + y2
-    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);    // shrink!  (csc_kernels.jl:53-64)
+    // shrink! (csc_kernels.jl:53-64) at lambda, not lambda / rho (REF_QUIRK_Q4, :61)
+    float Y2 = copysignf(fmaxf(fabsf(t) - lam, 0.f), t);
     float Y3 = keep ? x + b : 0.f;                          // projectionX! (:68-82)
     na = (a + x) - Y2;                                      // train.jl:13
     nb = (b + x) - Y3;                                      // train.jl:14

@@ -258,7 +258,8 @@ __device__ __forceinline__ void inv_step2(float2* __restrict__ buf, int j, bool 
 // shrink!, projectionX! and the dual updates of one entry (train.jl:12-14,
 // csc_kernels.jl:53-82), returning V = (Y2 - y2') + (Y3 - y3') in na, nb, v:
 //   Y2 = t - clamp(t, -lam, lam), t = X + y2 (= sign(t) max(|t| - lam, 0), the soft
-//        threshold at lam, up to the sign of a zero result);  y2' = (y2 + X) - Y2;
+//        threshold at lam -- not lam / rho, REF_QUIRK_Q4, csc_kernels.jl:61 -- up to the
+//        sign of a zero result);  y2' = (y2 + X) - Y2;
 //   on the rows projectionX! keeps (keep): Y3 = X + y3 and y3' = (y3 + X) - Y3 = +0;
 //   elsewhere Y3 = 0 and y3' = y3 + X.
 __device__ __forceinline__ void xprep1(float x, float a, float b, float lam, bool keep,
@@ -296,7 +297,8 @@ __device__ __forceinline__ float2 xprep2(float2 x, float2& y2, float2& y3, float
 // intrinsics, so that every kernel using these phases rounds identically.
 constexpr int kSlotChunk = 4;
 
-// this CTA's part of P = sum_m G1h[m] Vh[m] at bin f (train.jl:18-25, the RHS dot)
+// this CTA's part of P = sum_m G1h[m] Vh[m] at bin f (train.jl:18-25, the RHS dot; the
+// consensus dictionary's G1-hat, not the per-sequence d-hat: REF_QUIRK_Q5)
 template <int Lg>
 __device__ __forceinline__ float2 partial_P(const float2* __restrict__ bufs, int BUF, int B,
                                            int Mc, int F, int f, const float2* g1) {

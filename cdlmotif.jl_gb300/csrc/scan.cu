@@ -2,7 +2,7 @@
 //
 // Scores are summed in float32 with one rounded multiply and one rounded add per
 // term (__fmul_rn / __fadd_rn: no FMA contraction), in the order of the reference
-// path being replaced, so positions and scores are bit-identical to it:
+// path being replaced, so positions and scores are bit-identical to it (REF_QUIRK_Q7):
 //   greedy_search! (scan.jl:223-239): position-major, ind outer, nucleotide inner;
 //   scan_n (scan.jl:10-21):           nucleotide-major, j outer, k inner.
 #include "cdlgb_internal.h"
@@ -74,6 +74,7 @@ __global__ void k_scan_fwd(const float* __restrict__ data, const float* __restri
             best = vi_best(best, VI{v, l});
         }
         VI r = block_argmax(best, red);
+        // REF_QUIRK_Q3: a best hit at the first position reads as no hit (scan.jl:197)
         if (threadIdx.x == 0) pos[k + (size_t)K * n] = (r.i == 0) ? 0 : r.i + 1;
     }
 }
@@ -277,6 +278,7 @@ __global__ void k_scan_fwd_sparse(const float* __restrict__ data, const float* _
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
         VI r{-INFINITY, 0x7fffffff};
         for (int v = 0; v < nw; ++v) r = vi_best(r, wb[(size_t)k * nw + v]);
+        // REF_QUIRK_Q3: a best hit at the first position reads as no hit (scan.jl:197)
         pos[k + (size_t)K * n] = (r.i == 0) ? 0 : r.i + 1;
     }
 }

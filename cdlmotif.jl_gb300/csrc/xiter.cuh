@@ -249,7 +249,8 @@ __global__ void __launch_bounds__(NT, MINB) k_xiter(IArgs A) {
             }
             fwd_step1<N1, P>(sb, gl, tw2);
         } else if (act) {
-            // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12)
+            // U = Y1 - y1', y1' = y1 + DX - Y1  (train.jl:12; REF_QUIRK_Q6: the previous
+            // iteration's Y1, as the y3 update uses the previous Y3 and y2 the fresh Y2)
             __syncwarp(gmask);                  // the previous sequence's reads of Ss are done
             // the window in batches of 8 loads per lane, all issued before their stores
             const float* Sn = A.S + (size_t)n * A.L4;

@@ -64,6 +64,7 @@ struct cdlgb_server {
     bool stop = false;
     std::vector<std::thread> workers;
     clk::time_point t0;
+    std::mutex emu;                 // guards err (written by failing calls of any thread)
     char err[512];
 };
 
@@ -169,7 +170,10 @@ void worker(cdlgb_server* s) {
 }
 
 int serr(cdlgb_server* s, int code, const char* msg) {
-    if (s) snprintf(s->err, sizeof(s->err), "%s", msg);
+    if (s) {
+        std::lock_guard<std::mutex> lk(s->emu);
+        snprintf(s->err, sizeof(s->err), "%s", msg);
+    }
     return code;
 }
 
@@ -286,21 +290,27 @@ int cdlgb_server_poll(cdlgb_server* s, int64_t id, int32_t wait_ms, cdlgb_reques
     }
     memset(info, 0, sizeof(*info));
     info->state = r->state;
-    info->status = r->status;
     info->N = r->N;
     info->L4 = r->L4;
-    info->M = r->M;
-    info->Lg = r->Lg;
-    info->outer_done = r->outer_done;
     info->footprint_bytes = r->footprint;
-    info->obj_best = r->obj_best;
-    info->code_thresh = r->code_thresh;
     const auto now = clk::now();
     info->t_submit = secs(s->t0, r->t_submit);
     info->t_admit = r->state == CDLGB_REQ_PENDING ? -1.0 : secs(s->t0, r->t_admit);
-    info->t_done = (r->state == CDLGB_REQ_DONE || r->state == CDLGB_REQ_FAILED) ? secs(s->t0, r->t_done) : -1.0;
     info->t_now = secs(s->t0, now);
-    snprintf(info->error, sizeof(info->error), "%s", r->err.c_str());
+    // the results are written by the worker while the request runs, without the lock,
+    // and published under it with the final state: read them only then
+    if (r->state == CDLGB_REQ_DONE || r->state == CDLGB_REQ_FAILED) {
+        info->status = r->status;
+        info->M = r->M;
+        info->Lg = r->Lg;
+        info->outer_done = r->outer_done;
+        info->obj_best = r->obj_best;
+        info->code_thresh = r->code_thresh;
+        info->t_done = secs(s->t0, r->t_done);
+        snprintf(info->error, sizeof(info->error), "%s", r->err.c_str());
+    } else {
+        info->t_done = -1.0;
+    }
     return CDLGB_OK;
 }
 
@@ -348,7 +358,15 @@ int cdlgb_server_stats(cdlgb_server* s, int32_t* pending, int32_t* running, uint
     return CDLGB_OK;
 }
 
-const char* cdlgb_server_last_error(const cdlgb_server* s) { return s ? s->err : "no server"; }
+// a copy in the calling thread's own buffer: another thread's failing call may rewrite
+// the server's message meanwhile
+const char* cdlgb_server_last_error(const cdlgb_server* s) {
+    static thread_local char buf[512];
+    if (!s) return "no server";
+    std::lock_guard<std::mutex> lk(const_cast<cdlgb_server*>(s)->emu);
+    snprintf(buf, sizeof(buf), "%s", s->err);
+    return buf;
+}
 
 int cdlgb_server_destroy(cdlgb_server* s) {
     if (!s) return CDLGB_OK;

@@ -446,7 +446,9 @@ int cdlgb_server_submit(cdlgb_server* s, const float* onehot, int32_t L4, int32_
 int cdlgb_server_submit_fasta(cdlgb_server* s, const char* text, size_t nbytes,
                               int32_t max_entries, int64_t* request_id);
 /* State of a request; wait_ms > 0 waits up to that long for it to finish, < 0 waits
- * until it does, 0 returns at once. */
+ * until it does, 0 returns at once.  The result fields (status, M, Lg, outer_done,
+ * obj_best, code_thresh, t_done, error) are filled once the request is done or
+ * failed, and zero (t_done -1) before. */
 int cdlgb_server_poll(cdlgb_server* s, int64_t request_id, int32_t wait_ms, cdlgb_request_info* info);
 /* Copy a finished request's results: D_best (Lg, M) float32 (D_bytes = 4 Lg M), up to
  * objs_cap objectives, X_best (Lg, M, N) float32 when keep_codes; NULL skips one. */
@@ -457,6 +459,8 @@ int cdlgb_server_release(cdlgb_server* s, int64_t request_id);
 /* Queue depth, trainings in flight, admitted bytes and the budget. */
 int cdlgb_server_stats(cdlgb_server* s, int32_t* pending, int32_t* running, uint64_t* in_use,
                        uint64_t* budget);
+/* The message of the server's last failed call, copied into a buffer of the calling
+ * thread (valid until that thread's next call of this function). */
 const char* cdlgb_server_last_error(const cdlgb_server* s);
 /* Wait for the trainings in flight, drop the requests not yet admitted, free everything. */
 int cdlgb_server_destroy(cdlgb_server* s);

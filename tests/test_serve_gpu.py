@@ -72,6 +72,12 @@ def test_server_calls_from_threads(pkg, built_lib):
         for t in th:
             t.join()
         assert len(set(ids)) == len(data)
+        for rid in ids:
+            # the result fields are published with the final state only
+            info = srv.poll(rid, wait_ms=0)
+            if info["state"] in ("pending", "running"):
+                assert info["status"] == 0 and info["error"] is None and info["t_done"] == -1.0
+                assert info["M"] == 0 and info["outer_done"] == 0 and info["obj_best"] == 0.0
         for i, rid in enumerate(ids):
             info = srv.poll(rid, wait_ms=-1)
             assert info["state"] == "done", info

@@ -1,0 +1,164 @@
+"""The training server's host logic (csrc/server.cpp) on a machine without a GPU: every
+training fails at cdlgb_create, so each request runs through admission, a worker, the
+failure path and release without device work.  Covers the request life cycle and its
+timestamps, polls concurrent with submissions from several threads, admission refusal
+by footprint, the friendly-length padding, and argument errors.  Skipped where a GPU is present (the
+trainings would then succeed; tests/test_serve_gpu.py covers that side)."""
+import threading
+
+import numpy as np
+import pytest
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+pytestmark = pytest.mark.skipif(_has_gpu(), reason="trainings succeed on a GPU")
+
+ECUDA, EINVAL, ENOMEM_BUDGET, ESTATE = -3, -1, -2, -5
+BUDGET = 8 << 30
+
+
+def _data(pkg, seed, N=6, L=40):
+    bases, _, _ = pkg.synth.plant_dataset(seed, N, L, [6], [0.5])
+    return pkg.synth.onehot(bases)
+
+
+def _setup(pkg):
+    return pkg.CDLSetup(M=4, filter_size=2)
+
+
+def test_failed_trainings_are_reported_and_released(pkg, built_lib):
+    from cdlmotif_gb300 import serve
+    with serve.Server(_setup(pkg), slots=2, hbm_budget=BUDGET, iter_num=1) as srv:
+        ids = [srv.submit(_data(pkg, s)) for s in range(5)]
+        assert len(set(ids)) == 5
+        for rid in ids:
+            info = srv.poll(rid, wait_ms=-1)
+            assert info["state"] == "failed" and info["status"] == ECUDA and info["error"]
+            assert 0 <= info["t_submit"] <= info["t_admit"] <= info["t_done"] <= info["t_now"]
+            assert info["N"] == 6 and info["L4"] == 160 and info["footprint_bytes"] > 0
+            with pytest.raises(pkg.CDLGBError) as e:
+                srv.fetch(rid)
+            assert e.value.status == ESTATE
+            srv.release(rid)
+            with pytest.raises(pkg.CDLGBError) as e:
+                srv.poll(rid)
+            assert e.value.status == EINVAL
+        assert srv.stats() == {"pending": 0, "running": 0, "in_use": 0, "budget": BUDGET}
+
+
+def test_results_published_with_the_final_state(pkg, built_lib):
+    """Four threads submit while a fifth polls every known request without waiting, and
+    nothing fails or crashes; a request seen pending or running carries no result fields
+    yet (status 0, no message, t_done -1) -- here the failures are immediate, so such
+    states are seldom seen (tests/test_serve_gpu.py sees them during real trainings);
+    every request ends failed with its status and message."""
+    from cdlmotif_gb300 import serve
+    data = [_data(pkg, s) for s in range(4)]
+    with serve.Server(_setup(pkg), slots=3, hbm_budget=BUDGET, iter_num=1) as srv:
+        ids, lock, done = [], threading.Lock(), threading.Event()
+        errors = []
+
+        def submitter(k):
+            try:
+                for j in range(6):
+                    rid = srv.submit(data[(k + j) % 4])
+                    with lock:
+                        ids.append(rid)
+            except Exception as e:          # reported below
+                errors.append(e)
+
+        seen_unfinished = []
+
+        def poller():
+            try:
+                while not done.is_set():
+                    with lock:
+                        cur = list(ids)
+                    for rid in cur:
+                        info = srv.poll(rid, wait_ms=0)
+                        if info["state"] in ("pending", "running"):
+                            seen_unfinished.append(info)
+            except Exception as e:
+                errors.append(e)
+
+        pt = threading.Thread(target=poller)
+        pt.start()
+        th = [threading.Thread(target=submitter, args=(k,)) for k in range(4)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        for rid in ids:
+            assert srv.poll(rid, wait_ms=-1)["state"] == "failed"
+        done.set()
+        pt.join()
+        assert not errors, errors
+        assert len(set(ids)) == 24
+        for info in seen_unfinished:
+            assert info["status"] == 0 and info["error"] is None and info["t_done"] == -1.0
+            assert info["M"] == 0 and info["outer_done"] == 0
+        for rid in ids:
+            info = srv.poll(rid)
+            assert info["status"] == ECUDA and info["error"]
+            srv.release(rid)
+        assert srv.stats()["in_use"] == 0
+
+
+def test_admission_refuses_what_never_fits(pkg, built_lib):
+    from cdlmotif_gb300 import serve
+    S = _data(pkg, 1)
+    fp = serve.footprint_bytes(_setup(pkg), S.shape[1] // 4, S.shape[0])
+    with serve.Server(_setup(pkg), slots=1, hbm_budget=fp - 1, iter_num=1) as srv:
+        with pytest.raises(pkg.CDLGBError) as e:
+            srv.submit(S)
+        assert e.value.status == ENOMEM_BUDGET and "budget" in str(e.value)
+        assert srv.stats()["pending"] == 0
+    with serve.Server(_setup(pkg), slots=1, hbm_budget=fp, iter_num=1) as srv:
+        assert srv.poll(srv.submit(S), wait_ms=-1)["footprint_bytes"] == fp
+
+
+@pytest.mark.parametrize("L", [43, 101, 150])
+def test_friendly_padding_of_submissions(pkg, built_lib, L):
+    """With pad_friendly the server pads each sequence to the length the Python mirror
+    (serve.friendly_length) names, for one-hot and FASTA submissions alike."""
+    from cdlmotif_gb300 import serve
+    setup = pkg.CDLSetup(M=4, filter_size=16)
+    bases, _, _ = pkg.synth.plant_dataset(3, 4, L, [6], [0.5])
+    Lp = serve.friendly_length(L, 16)
+    with serve.Server(setup, slots=1, hbm_budget=BUDGET, iter_num=1, pad_friendly=True) as srv:
+        a = srv.poll(srv.submit(pkg.synth.onehot(bases)), wait_ms=-1)
+        b = srv.poll(srv.submit_fasta(pkg.synth.to_fasta(bases)), wait_ms=-1)
+    assert a["L4"] == b["L4"] == 4 * Lp and a["N"] == b["N"] == 4
+
+
+def test_bad_arguments(pkg, built_lib):
+    from cdlmotif_gb300 import serve
+    with pytest.raises(pkg.CDLGBError) as e:
+        serve.Server(_setup(pkg), slots=0, hbm_budget=BUDGET)
+    assert e.value.status == EINVAL
+    with serve.Server(_setup(pkg), slots=1, hbm_budget=BUDGET, iter_num=1) as srv:
+        with pytest.raises(pkg.CDLGBError) as e:
+            srv.submit(np.zeros((3, 6), np.float32))        # 4L not a multiple of 4
+        assert e.value.status == EINVAL
+        with pytest.raises(pkg.CDLGBError) as e:
+            srv.poll(12345)
+        assert e.value.status == EINVAL
+        with pytest.raises(pkg.CDLGBError) as e:
+            srv.release(12345)
+        assert e.value.status == EINVAL
+
+
+def test_destroy_with_requests_queued(pkg, built_lib):
+    """Closing the server while requests wait drops them and returns."""
+    from cdlmotif_gb300 import serve
+    srv = serve.Server(_setup(pkg), slots=1, hbm_budget=BUDGET, iter_num=1)
+    for s in range(8):
+        srv.submit(_data(pkg, s))
+    srv.close()

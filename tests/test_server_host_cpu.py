@@ -162,3 +162,41 @@ def test_destroy_with_requests_queued(pkg, built_lib):
     for s in range(8):
         srv.submit(_data(pkg, s))
     srv.close()
+
+
+_FASTA = {
+    "multi-line records, lower case": b">a\nACGTAC\nGTAC\n>b desc\nacgtacgtac\n>c\nTTTTGGGGCC\n",
+    "records with N dropped": b">a\nACGTN\n>b\nACGTA\n>c\nacgtn\n>d\nCCCCA\n",
+    "empty chunks and no final newline": b">>a\nACGT\n>\n>b\nTTGA",
+    "ragged lengths": b">a\nACGTACGT\n>b\nACG\n>c\nGGGGCCCC\n",
+    "max entries after the N filter": b">a\nAAAN\n>b\nACGT\n>c\nCCCC\n>d\nGGGG\n>e\nTTTT\n",
+}
+
+
+@pytest.mark.parametrize("name", sorted(_FASTA))
+def test_fasta_submissions_match_the_oracle_reader(pkg, built_lib, name):
+    """The server parses FASTA submissions on the host by read_fasta's rules
+    (src/LOAD/read.jl:2-28): its dataset sizes equal the oracle reader's."""
+    from cdlmotif_gb300 import serve
+    from oracle import search_oracle as SO
+    text = _FASTA[name]
+    cap = 3 if name.startswith("max") else 10000
+    S_ref, reads = SO.read_fasta_onehot(text, cap)
+    with serve.Server(_setup(pkg), slots=1, hbm_budget=BUDGET, iter_num=1) as srv:
+        info = srv.poll(srv.submit_fasta(text, cap), wait_ms=-1)
+    assert (info["N"], info["L4"]) == S_ref.shape, (name, reads)
+
+
+@pytest.mark.parametrize("text", [b">a\r\nACGT\r\n>b\r\nACGT\r\n",   # CR kept, as split("\n") keeps it
+                                  b">a\nACGU\n",                    # not a base
+                                  b">a\nNNNN\n>b\nACGN\n",          # every record dropped
+                                  b"", b">a\n\n>b\nACGT\n"])       # nothing, or an empty first record
+def test_fasta_submissions_rejected(pkg, built_lib, text):
+    """Inputs the reference's reader fails on (a character dummy[] has no entry for) or
+    that leave no usable first record are refused at submission, before any device work."""
+    from cdlmotif_gb300 import serve
+    with serve.Server(_setup(pkg), slots=1, hbm_budget=BUDGET, iter_num=1) as srv:
+        with pytest.raises(pkg.CDLGBError) as e:
+            srv.submit_fasta(text)
+        assert e.value.status == EINVAL and str(e.value)
+        assert srv.stats()["pending"] == 0

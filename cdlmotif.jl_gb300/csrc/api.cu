@@ -411,7 +411,8 @@ int cdlgb_load_fasta(cdlgb_ctx* c, const char* text, size_t nbytes, int32_t max_
 }
 
 int cdlgb_dims(const cdlgb_ctx* c, int32_t* L4, int32_t* N, int32_t* M, int32_t* gamma, int32_t* Lg) {
-    if (!c || !c->loaded) return CDLGB_ESTATE;
+    if (!c) return CDLGB_EINVAL;
+    if (!c->loaded) return CDLGB_ESTATE;
     if (L4) *L4 = c->L4;
     if (N) *N = c->N;
     if (M) *M = c->M;

@@ -119,7 +119,7 @@ class CDL:
         h = C.c_void_p()
         st = L.cdlgb_create(C.byref(self._p), C.byref(h))
         if st != 0:
-            raise CDLGBError(st, "cdlgb_create failed")
+            raise CDLGBError(st, L.cdlgb_last_error(None).decode())
         self._h = h
         self.N = self.M = self.L = self.gamma = self.Lg = None
 
@@ -667,7 +667,7 @@ class ActivationRecord:
         h = C.c_void_p()
         st = _lib.lib().cdlgb_ar_create(int(N), int(L), int(M), int(T), int(device), C.byref(h))
         if st != 0:
-            raise CDLGBError(st, "cdlgb_ar_create failed")
+            raise CDLGBError(st, _lib.lib().cdlgb_ar_last_error(None).decode())
         self._h = h
         self.N, self.L, self.M, self.T = N, L, M, T
 

@@ -8,6 +8,20 @@
 #include <string>
 #include <vector>
 
+namespace {
+thread_local char t_noctx_err[512];
+}
+
+int noctx_seterr(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_noctx_err, sizeof(t_noctx_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+const char* noctx_err() { return t_noctx_err[0] ? t_noctx_err : nullptr; }
+
 int cdlgb_seterr(cdlgb_ctx* c, int code, const char* fmt, ...) {
     if (c) {
         va_list ap;
@@ -212,20 +226,24 @@ static int check_params(cdlgb_ctx* c, const cdlgb_params* p) {
 }
 
 int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out) {
-    if (!p || !out) return CDLGB_EINVAL;
+    if (!p || !out) return noctx_seterr(CDLGB_EINVAL, "cdlgb_create: null argument");
     *out = nullptr;
     cdlgb_ctx* c = new (std::nothrow) cdlgb_ctx();
-    if (!c) return CDLGB_EINVAL;
+    if (!c) return noctx_seterr(CDLGB_EINVAL, "cdlgb_create: out of host memory");
     c->err[0] = 0;
     c->p = *p;
     int st = check_params(c, p);
-    if (st) { fprintf(stderr, "cdlgb_create: %s\n", c->err); delete c; return st; }
+    if (st) {
+        noctx_seterr(st, "cdlgb_create: %s", c->err);
+        delete c;
+        return st;
+    }
     c->dev = p->device;
     c->res_on = p->track_residuals != 0 || p->stop_tol > 0.f;
     cudaError_t e = cudaSetDevice(c->dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
-        fprintf(stderr, "cdlgb_create: %s\n", cudaGetErrorString(e));
+        noctx_seterr(CDLGB_ECUDA, "cdlgb_create: device %d: %s", c->dev, cudaGetErrorString(e));
         delete c;
         return CDLGB_ECUDA;
     }
@@ -266,7 +284,11 @@ int cdlgb_destroy(cdlgb_ctx* c) {
     return CDLGB_OK;
 }
 
-const char* cdlgb_last_error(const cdlgb_ctx* c) { return c ? c->err : "null context"; }
+const char* cdlgb_last_error(const cdlgb_ctx* c) {
+    if (c) return c->err;
+    const char* m = noctx_err();
+    return m ? m : "null context";
+}
 
 static int pick_fused(const cdlgb_params* p, int Lg) {
     if (p->fft_mode == 1) return 0;

@@ -143,6 +143,11 @@ struct cdlgb_ctx {
 };
 
 int cdlgb_seterr(cdlgb_ctx* c, int code, const char* fmt, ...);
+// the calling thread's message for a failure with no handle to hold it (creating a
+// context, record or server; the allocation-free objective), returned by the
+// *_last_error calls given a null handle; nullptr when there is none
+int noctx_seterr(int code, const char* fmt, ...);
+const char* noctx_err();
 
 #define CU_TRY(c, call)                                                                 \
     do {                                                                                \

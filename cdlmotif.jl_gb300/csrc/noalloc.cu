@@ -97,22 +97,21 @@ __global__ void k_obj_total(const double* __restrict__ part, int N, double lam,
 }
 
 // device address of the scratch on the current device, looked up once per device
-int scratch_for_current_device(double** out) {
+cudaError_t scratch_for_current_device(double** out) {
     int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CDLGB_ECUDA;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_scratch_mu);
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            fprintf(stderr, "cdlgb_objective_noalloc: cudaGetSymbolAddress failed: %s\n",
-                    cudaGetErrorString(e));
-            return CDLGB_ECUDA;
-        }
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        if (!p) return cudaErrorInvalidSymbol;
         g_scratch_addr[dev] = (double*)p;
     }
     *out = g_scratch_addr[dev];
-    return CDLGB_OK;
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -121,26 +120,24 @@ int scratch_for_current_device(double** out) {
 // (and the module loaded) while the caller's memory is still free.
 int noalloc_warm_current_device() {
     double* p = nullptr;
-    return scratch_for_current_device(&p);
+    return scratch_for_current_device(&p) == cudaSuccess ? CDLGB_OK : CDLGB_ECUDA;
 }
 
 extern "C" int cdlgb_objective_noalloc(const float* X, const float* DX, const float* S,
                                        int32_t L4, int32_t N, int32_t M, int32_t gamma,
                                        float lambda, double* obj, void* stream) {
-    if (!X || !DX || !S || !obj || L4 <= 0 || N <= 0 || M <= 0 || gamma < 0 || (L4 % 4)) {
-        fprintf(stderr, "cdlgb_objective_noalloc: invalid argument\n");
-        return CDLGB_EINVAL;
-    }
-    if (N > CDLGB_NOALLOC_MAX_SEQ) {
-        fprintf(stderr,
-                "cdlgb_objective_noalloc: N=%d sequences exceeds the fixed scratch of %d "
-                "sequences; use cdlgb_objective on a context instead\n",
-                N, CDLGB_NOALLOC_MAX_SEQ);
-        return CDLGB_EINVAL;
-    }
+    if (!X || !DX || !S || !obj || L4 <= 0 || N <= 0 || M <= 0 || gamma < 0 || (L4 % 4))
+        return noctx_seterr(CDLGB_EINVAL, "cdlgb_objective_noalloc: invalid argument");
+    if (N > CDLGB_NOALLOC_MAX_SEQ)
+        return noctx_seterr(CDLGB_EINVAL,
+                            "cdlgb_objective_noalloc: N=%d sequences exceeds the fixed scratch of %d "
+                            "sequences; use cdlgb_objective on a context instead",
+                            N, CDLGB_NOALLOC_MAX_SEQ);
     double* scratch = nullptr;
-    int st = scratch_for_current_device(&scratch);
-    if (st != CDLGB_OK) return st;
+    cudaError_t se = scratch_for_current_device(&scratch);
+    if (se != cudaSuccess)
+        return noctx_seterr(CDLGB_ECUDA, "cdlgb_objective_noalloc: scratch lookup: %s",
+                            cudaGetErrorString(se));
     cudaStream_t s = (cudaStream_t)stream;
     const int Lg = L4 + 2 * gamma;
     k_obj_per_seq<<<N, kThreads, 0, s>>>(X, DX, S, L4, Lg, M, gamma, scratch);
@@ -149,9 +146,7 @@ extern "C" int cdlgb_objective_noalloc(const float* X, const float* DX, const fl
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(obj, res, sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-        fprintf(stderr, "cdlgb_objective_noalloc: %s\n", cudaGetErrorString(e));
-        return CDLGB_ECUDA;
-    }
+    if (e != cudaSuccess)
+        return noctx_seterr(CDLGB_ECUDA, "cdlgb_objective_noalloc: %s", cudaGetErrorString(e));
     return CDLGB_OK;
 }

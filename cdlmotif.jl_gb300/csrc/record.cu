@@ -190,10 +190,12 @@ __global__ void k_pair_finish(const float* __restrict__ part, const int* __restr
 extern "C" {
 
 int cdlgb_ar_create(int32_t N, int32_t L, int32_t M, int32_t T, int32_t device, cdlgb_ar** out) {
-    if (!out || N <= 0 || L <= 0 || M <= 0 || T <= 0 || L > 65535) return CDLGB_EINVAL;
+    if (!out || N <= 0 || L <= 0 || M <= 0 || T <= 0 || L > 65535)
+        return noctx_seterr(CDLGB_EINVAL, "cdlgb_ar_create: N=%d, L=%d, M=%d, T=%d (L <= 65535)",
+                            N, L, M, T);
     *out = nullptr;
     cdlgb_ar* a = new (std::nothrow) cdlgb_ar();
-    if (!a) return CDLGB_EINVAL;
+    if (!a) return noctx_seterr(CDLGB_EINVAL, "cdlgb_ar_create: out of host memory");
     a->err[0] = 0;
     a->dev = device;
     a->N = N; a->C = L; a->M = M; a->T = T;
@@ -209,7 +211,7 @@ int cdlgb_ar_create(int32_t N, int32_t L, int32_t M, int32_t T, int32_t device, 
     if (e == cudaSuccess) e = cudaMalloc((void**)&a->ktrain, kcap * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc((void**)&a->dthresh, T * sizeof(float));
     if (e != cudaSuccess) {
-        fprintf(stderr, "cdlgb_ar_create: %s\n", cudaGetErrorString(e));
+        noctx_seterr(CDLGB_ECUDA, "cdlgb_ar_create: %s", cudaGetErrorString(e));
         cdlgb_ar_destroy(a);
         return CDLGB_ECUDA;
     }
@@ -229,7 +231,11 @@ int cdlgb_ar_destroy(cdlgb_ar* a) {
     return CDLGB_OK;
 }
 
-const char* cdlgb_ar_last_error(const cdlgb_ar* a) { return a ? a->err : "null record"; }
+const char* cdlgb_ar_last_error(const cdlgb_ar* a) {
+    if (a) return a->err;
+    const char* m = noctx_err();
+    return m ? m : "null record";
+}
 
 int cdlgb_ar_record(cdlgb_ar* a, cdlgb_ctx* c, double thresh, int32_t train_num,
                     int32_t filter_size, int32_t* added) {

@@ -107,7 +107,7 @@ void train(cdlgb_server* s, Req& r) {
     int st = cdlgb_create(&p, &c);
     auto fail = [&](int code) {
         r.status = code;
-        r.err = c ? cdlgb_last_error(c) : "cdlgb_create failed";
+        r.err = cdlgb_last_error(c);        // this worker's creation message when c is null
     };
     if (st != CDLGB_OK) { fail(st); return; }
     const int iters = s->cfg.iter_num > 0 ? s->cfg.iter_num : p.iter_num;
@@ -182,20 +182,25 @@ int serr(cdlgb_server* s, int code, const char* msg) {
 extern "C" {
 
 int cdlgb_server_create(const cdlgb_params* p, const cdlgb_server_config* cfg, cdlgb_server** out) {
-    if (!p || !cfg || !out) return CDLGB_EINVAL;
+    if (!p || !cfg || !out) return noctx_seterr(CDLGB_EINVAL, "cdlgb_server_create: null argument");
     *out = nullptr;
-    if (cfg->slots < 1 || cfg->slots > 64 || cfg->iter_num < 0) return CDLGB_EINVAL;
+    if (cfg->slots < 1 || cfg->slots > 64 || cfg->iter_num < 0)
+        return noctx_seterr(CDLGB_EINVAL, "cdlgb_server_create: slots=%d (1..64), iter_num=%d (>= 0)",
+                            cfg->slots, cfg->iter_num);
     cdlgb_server* s = new (std::nothrow) cdlgb_server();
-    if (!s) return CDLGB_EINVAL;
+    if (!s) return noctx_seterr(CDLGB_EINVAL, "cdlgb_server_create: out of host memory");
     s->p = *p;
     s->cfg = *cfg;
     s->err[0] = 0;
     s->budget = cfg->hbm_budget_bytes;
     if (s->budget == 0) {
         size_t fr = 0, tot = 0;
-        if (cudaSetDevice(cfg->device) != cudaSuccess || cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaError_t e = cudaSetDevice(cfg->device);
+        if (e == cudaSuccess) e = cudaMemGetInfo(&fr, &tot);
+        if (e != cudaSuccess) {
             delete s;
-            return CDLGB_ECUDA;
+            return noctx_seterr(CDLGB_ECUDA, "cdlgb_server_create: device %d: %s", cfg->device,
+                                cudaGetErrorString(e));
         }
         s->budget = (uint64_t)((double)fr * 0.85);
     }
@@ -362,7 +367,10 @@ int cdlgb_server_stats(cdlgb_server* s, int32_t* pending, int32_t* running, uint
 // the server's message meanwhile
 const char* cdlgb_server_last_error(const cdlgb_server* s) {
     static thread_local char buf[512];
-    if (!s) return "no server";
+    if (!s) {
+        const char* m = noctx_err();
+        return m ? m : "no server";
+    }
     std::lock_guard<std::mutex> lk(const_cast<cdlgb_server*>(s)->emu);
     snprintf(buf, sizeof(buf), "%s", s->err);
     return buf;

@@ -90,7 +90,7 @@ class Server:
         h = C.c_void_p()
         st = L.cdlgb_server_create(C.byref(self._p), C.byref(cfg), C.byref(h))
         if st != 0:
-            raise CDLGBError(st, "cdlgb_server_create failed")
+            raise CDLGBError(st, L.cdlgb_server_last_error(None).decode())
         self._h = h
         self.iter_num = cfg.iter_num
 

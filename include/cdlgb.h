@@ -12,8 +12,11 @@
  *   - Device memory is owned by the library (one context = one dataset's ADMM
  *     state, resident in HBM until cdlgb_destroy).
  *   - Every call returns a cdlgb_status; 0 = OK, negative = error, with the
- *     message available from cdlgb_last_error(ctx).  No call aborts the process
- *     and no kernel traps.
+ *     message available from cdlgb_last_error(ctx).  A failure with no handle to
+ *     hold its message (cdlgb_create, cdlgb_ar_create, cdlgb_server_create,
+ *     cdlgb_objective_noalloc) leaves it for the calling thread: the *_last_error
+ *     call given a null handle returns it.  The library prints nothing, no call
+ *     aborts the process and no kernel traps.
  *   - A context is used by one host thread at a time and owns its own CUDA stream.
  *
  * Reference interfaces replaced (paths within kchu25/CDLmotif.jl):
@@ -133,6 +136,8 @@ int cdlgb_params_default(cdlgb_params* p);
  * handle; its state is the `cdl` struct built by init_cdl. */
 int cdlgb_create(const cdlgb_params* p, cdlgb_ctx** out);
 int cdlgb_destroy(cdlgb_ctx* ctx);
+/* The context's last error message; with ctx = NULL, the calling thread's last failure
+ * that had no handle (a failed cdlgb_create, ...), or "null context". */
 const char* cdlgb_last_error(const cdlgb_ctx* ctx);
 
 /* Device memory a dataset of N sequences x L bases needs, for admission control.  Where
@@ -332,6 +337,7 @@ int64_t cdlgb_transfac_format(const float* pfm, int32_t w, int32_t reverse_compl
  * thresholds; filter k = (training, m) for every filter with an activation. */
 int cdlgb_ar_create(int32_t N, int32_t L, int32_t M, int32_t T, int32_t device, cdlgb_ar** out);
 int cdlgb_ar_destroy(cdlgb_ar* ar);
+/* ar = NULL: the calling thread's last failure without a handle (cdlgb_ar_create, ...). */
 const char* cdlgb_ar_last_error(const cdlgb_ar* ar);
 
 /* record_training_result! (src/SEARCH/store.jl:1-40): codes of ctx's X_best, activations
@@ -460,7 +466,8 @@ int cdlgb_server_release(cdlgb_server* s, int64_t request_id);
 int cdlgb_server_stats(cdlgb_server* s, int32_t* pending, int32_t* running, uint64_t* in_use,
                        uint64_t* budget);
 /* The message of the server's last failed call, copied into a buffer of the calling
- * thread (valid until that thread's next call of this function). */
+ * thread (valid until that thread's next call of this function); s = NULL: the calling
+ * thread's last failure without a handle (cdlgb_server_create, ...). */
 const char* cdlgb_server_last_error(const cdlgb_server* s);
 /* Wait for the trainings in flight, drop the requests not yet admitted, free everything. */
 int cdlgb_server_destroy(cdlgb_server* s);

@@ -6,6 +6,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 _CHILD = r'''
@@ -51,3 +53,31 @@ def test_null_arguments_are_refused(pkg, built_lib):
             assert int(val) == 0, name
         else:
             assert int(val) == -1, (name, val)        # CDLGB_EINVAL
+
+
+def test_creation_failures_carry_their_message(pkg, built_lib):
+    """Failures with no handle to hold the message (creating a context, a record or a
+    server; the allocation-free objective) leave it for the calling thread, and the
+    Python wrappers raise with it.  The checks below run before any device call."""
+    import ctypes as C
+    from cdlmotif_gb300 import _lib, serve
+    with pytest.raises(pkg.CDLGBError) as e:
+        pkg.CDL(pkg.CDLSetup(M=4, filter_size=2), fft_mode=5)
+    assert e.value.status == -1 and "fft_mode=5" in str(e.value)
+    with pytest.raises(pkg.CDLGBError) as e:
+        pkg.ActivationRecord(10, 70000, 4)
+    assert e.value.status == -1 and "L <= 65535" in str(e.value)
+    with pytest.raises(pkg.CDLGBError) as e:
+        serve.Server(pkg.CDLSetup(M=4, filter_size=2), slots=65, hbm_budget=1 << 30)
+    assert e.value.status == -1 and "slots=65" in str(e.value)
+    L = _lib.lib()
+    obj = C.c_double()
+    assert L.cdlgb_objective_noalloc(None, None, None, 0, 0, 0, 0, 0.0, C.byref(obj), None) == -1
+    assert b"cdlgb_objective_noalloc" in L.cdlgb_last_error(None)
+    # the message belongs to the thread that failed
+    import threading
+    seen = []
+    t = threading.Thread(target=lambda: seen.append(L.cdlgb_last_error(None)))
+    t.start()
+    t.join()
+    assert seen == [b"null context"]

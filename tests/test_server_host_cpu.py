@@ -40,7 +40,8 @@ def test_failed_trainings_are_reported_and_released(pkg, built_lib):
         assert len(set(ids)) == 5
         for rid in ids:
             info = srv.poll(rid, wait_ms=-1)
-            assert info["state"] == "failed" and info["status"] == ECUDA and info["error"]
+            assert info["state"] == "failed" and info["status"] == ECUDA
+            assert info["error"].startswith("cdlgb_create: device 0:")   # the worker's reason
             assert 0 <= info["t_submit"] <= info["t_admit"] <= info["t_done"] <= info["t_now"]
             assert info["N"] == 6 and info["L4"] == 160 and info["footprint_bytes"] > 0
             with pytest.raises(pkg.CDLGBError) as e:

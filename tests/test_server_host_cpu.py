@@ -201,3 +201,29 @@ def test_fasta_submissions_rejected(pkg, built_lib, text):
             srv.submit_fasta(text)
         assert e.value.status == EINVAL and str(e.value)
         assert srv.stats()["pending"] == 0
+
+
+def test_serve_stream_collects_refusals_and_failures(pkg, built_lib):
+    """The request replay behind `bench.py --serve` (serve.serve_stream): arrivals spaced
+    in time, one-hot and FASTA requests, one dataset refused at submission for its
+    footprint and the rest failing here; every request is accounted for and the
+    latency figures are empty rather than made up."""
+    import math
+    from cdlmotif_gb300 import serve
+    setup = _setup(pkg)
+    small = [_data(pkg, s) for s in range(3)]
+    big = _data(pkg, 9, N=400, L=120)
+    fp_small, fp_big = serve.footprint_bytes(setup, 40, 6), serve.footprint_bytes(setup, 120, 400)
+    budget = (fp_small + fp_big) // 2          # the small ones fit, the big one never does
+    assert fp_small <= budget < fp_big
+    bases, _, _ = pkg.synth.plant_dataset(4, 5, 40, [6], [0.5])
+    reqs = [(0.0, small[0]), (0.02, big), (0.04, small[1]),
+            (0.06, pkg.synth.to_fasta(bases)), (0.08, small[2])]
+    res = serve.serve_stream(setup, reqs, slots=2, iter_num=1, hbm_budget=budget)
+    assert res["requests"] == 5 and res["completed"] == 0 and res["results"] == {}
+    msgs = res["rejected"]
+    assert len(msgs) == 5
+    assert sum("budget" in m for m in msgs) == 1
+    assert sum(m.startswith("cdlgb_create") for m in msgs) == 4
+    assert math.isnan(res["p50_s"]) and math.isnan(res["p99_s"])
+    assert res["datasets_per_hr"] is None and res["mean_queue_s"] is None
